@@ -1,0 +1,130 @@
+"""ctypes binding of ``libcpfem_gb300.so`` (declared in ``include/cpfem_gb300.h``).
+
+The library must exist: there is no CPU fallback.  ``load()`` raises ``ImportError`` with
+the build command when the shared object is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libcpfem_gb300.so")
+
+MAX_SLIP = 24
+
+CPFEM_GP_MAXITER = 1
+CPFEM_GP_NONFINITE = 2
+
+
+class CPFEMError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+
+class Material(ctypes.Structure):
+    _fields_ = [
+        ("num_slip", ctypes.c_int32),
+        ("qmode", ctypes.c_int32),
+        ("max_sub_step", ctypes.c_int32),
+        ("max_iter", ctypes.c_int32),
+        ("local_tol", ctypes.c_double),
+        ("ao", ctypes.c_double),
+        ("C11", ctypes.c_double),
+        ("C12", ctypes.c_double),
+        ("C44", ctypes.c_double),
+        ("slip_d", (ctypes.c_double * 3) * MAX_SLIP),
+        ("slip_n", (ctypes.c_double * 3) * MAX_SLIP),
+    ]
+
+
+class GPArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_gp", ctypes.c_int64),
+        ("num_cells", ctypes.c_int32),
+        ("weight_jxw", ctypes.c_int32),
+        ("dt", ctypes.c_double),
+        ("u", ctypes.c_void_p),
+        ("cells", ctypes.c_void_p),
+        ("shape_grads", ctypes.c_void_p),
+        ("jxw", ctypes.c_void_p),
+        ("u_grad", ctypes.c_void_p),
+        ("fpi", ctypes.c_void_p),
+        ("g", ctypes.c_void_p),
+        ("slip", ctypes.c_void_p),
+        ("rot_table", ctypes.c_void_p),
+        ("rot_idx", ctypes.c_void_p),
+        ("param_table", ctypes.c_void_p),
+        ("param_idx", ctypes.c_void_p),
+        ("pk1", ctypes.c_void_p),
+        ("tangent", ctypes.c_void_p),
+        ("stress", ctypes.c_void_p),
+        ("fpi_new", ctypes.c_void_p),
+        ("g_new", ctypes.c_void_p),
+        ("slip_new", ctypes.c_void_p),
+        ("s_out", ctypes.c_void_p),
+        ("iters", ctypes.c_void_p),
+        ("status", ctypes.c_void_p),
+    ]
+
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+
+# name -> (restype, argtypes); every symbol declared in include/cpfem_gb300.h
+SIGNATURES = {
+    "cpfem_abi_version": (ctypes.c_int, []),
+    "cpfem_last_error": (ctypes.c_char_p, []),
+    "cpfem_pattern_count": (ctypes.c_int, [_I32, _P, _I32, _P]),
+    "cpfem_pattern_build": (ctypes.c_int, [_I32, _P, _I32, _P, _P, _P, _P]),
+    "cpfem_pattern_expand_csr": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
+    "cpfem_gp_eval": (ctypes.c_int, [ctypes.POINTER(Material), ctypes.POINTER(GPArgs), _P]),
+    "cpfem_elem_assemble": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "cpfem_apply_dirichlet": (ctypes.c_int, [_I32, _P, _P, _P, _P, _I32, _P, _P, _P, _P]),
+    "cpfem_bc_initial_guess": (ctypes.c_int, [_I64, _I32, _P, _P, _P, _P, _P]),
+    "cpfem_cell_average": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
+    "cpfem_axpy": (ctypes.c_int, [_I64, _D, _P, _P, _P]),
+    "cpfem_dot_workspace_bytes": (ctypes.c_size_t, [_I64]),
+    "cpfem_dot": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P]),
+    "cpfem_spmv": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P]),
+    "cpfem_spmv_t": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _P]),
+    "cpfem_bicgstab_workspace_bytes": (ctypes.c_size_t, [_I32]),
+    "cpfem_bicgstab": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _I32, _I32, _D, _D, _I32, _I32, _P,
+                                      _P, _P]),
+}
+
+_lib = None
+
+
+def load():
+    """Load the library once and declare every entry point's signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with "
+                          f"`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.cpfem_abi_version() != 1:
+        raise ImportError("libcpfem_gb300.so ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().cpfem_last_error().decode(errors="replace")
+        raise CPFEMError(f"cpfem call failed (status {rc}): {msg}")
+
+
+def ptr(t):
+    """Device (or host) address of a tensor / array, or None."""
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data

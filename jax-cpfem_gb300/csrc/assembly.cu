@@ -1,0 +1,425 @@
+// Constitutive pass, element assembly, Dirichlet row elimination and small vector
+// kernels of the cpfem_gb300 C ABI.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "cpfem_common.cuh"
+#include "gp_update.cuh"
+#include "reduce.cuh"
+
+namespace cpfem {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int make_matdev(const cpfem_material_t* m, MatDev* o) {
+  CPFEM_REQUIRE(m != nullptr && o != nullptr, "material is null");
+  CPFEM_REQUIRE(m->num_slip == 12 || m->num_slip == 24, "num_slip must be 12 or 24");
+  CPFEM_REQUIRE(m->qmode == 0 || m->qmode == 1, "qmode must be 0 or 1");
+  CPFEM_REQUIRE(m->max_sub_step >= 1 && m->max_iter >= 1, "max_sub_step and max_iter must be >= 1");
+  std::memset(o, 0, sizeof(*o));
+  o->num_slip = m->num_slip;
+  o->qmode = m->qmode;
+  o->max_sub_step = m->max_sub_step;
+  o->max_iter = m->max_iter;
+  o->local_tol = m->local_tol;
+  o->ao = m->ao;
+  o->C11 = m->C11;
+  o->C12 = m->C12;
+  o->C44 = m->C44;
+  for (int a = 0; a < m->num_slip; ++a) {
+    const double* d = m->slip_d[a];
+    const double* n = m->slip_n[a];
+    for (int i = 0; i < 3; ++i) {
+      o->d[a][i] = d[i];
+      o->n[a][i] = n[i];
+      for (int j = 0; j < 3; ++j) o->p9[a][3 * i + j] = d[i] * n[j];
+    }
+    o->pv[a][0] = d[0] * n[0];
+    o->pv[a][1] = d[1] * n[1];
+    o->pv[a][2] = d[2] * n[2];
+    o->pv[a][3] = d[1] * n[2] + d[2] * n[1];
+    o->pv[a][4] = d[0] * n[2] + d[2] * n[0];
+    o->pv[a][5] = d[0] * n[1] + d[1] * n[0];
+  }
+  return CPFEM_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Constitutive pass: one thread per Gauss point.
+// ------------------------------------------------------------------------------------
+template <int NS, bool TANGENT>
+__global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_args_t a) {
+  const int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t G = a.num_gp;
+  if (gp >= G) return;
+
+  double F[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) F[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  if (a.u != nullptr) {
+    // u_grad = sum_b u_b (x) dN_b/dX at this quad (models_copper.py:277-278)
+    const int64_t e = gp >> 3;
+    const int32_t* cn = a.cells + e * 8;
+    const double* sg = a.shape_grads + gp * 24;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int64_t nb = cn[b];
+      const double u0 = a.u[3 * nb], u1 = a.u[3 * nb + 1], u2 = a.u[3 * nb + 2];
+      const double g0 = sg[3 * b], g1 = sg[3 * b + 1], g2 = sg[3 * b + 2];
+      F[0] = fma(u0, g0, F[0]); F[1] = fma(u0, g1, F[1]); F[2] = fma(u0, g2, F[2]);
+      F[3] = fma(u1, g0, F[3]); F[4] = fma(u1, g1, F[4]); F[5] = fma(u1, g2, F[5]);
+      F[6] = fma(u2, g0, F[6]); F[7] = fma(u2, g1, F[7]); F[8] = fma(u2, g2, F[8]);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) F[k] += a.u_grad[k * G + gp];
+  }
+  double Fpi[9], R[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Fpi[k] = a.fpi[k * G + gp];
+  const int64_t ri = a.rot_idx[gp];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) R[k] = a.rot_table[9 * ri + k];
+  const int64_t pi = (a.param_idx != nullptr) ? a.param_idx[gp] : 0;
+  const double gss_a = a.param_table[5 * pi + 0];
+  const double hh = a.param_table[5 * pi + 1];
+  const double t_sat = a.param_table[5 * pi + 2];
+  const double xm = a.param_table[5 * pi + 3];
+  const double rq = a.param_table[5 * pi + 4];
+
+  double g[NS], ig[NS];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    g[s] = a.g[s * G + gp];
+    ig[s] = 1.0 / g[s];
+  }
+  double A[9], AR[9], Ct[9];
+  mm3(F, Fpi, A);
+  mm3(A, R, AR);
+  mm3_at(AR, AR, Ct);
+
+  GPSolve<NS> st;
+  cp_local_newton<NS>(m, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
+  if (a.status != nullptr) {
+    int bits = 0;
+    if (!(st.rn <= m.local_tol)) bits |= CPFEM_GP_MAXITER;
+    if (!isfinite(st.rn)) bits |= CPFEM_GP_NONFINITE;
+    if (bits) atomicOr(a.status, bits);
+  }
+
+  double Gm[9], H[9], P[9];
+  mm3(Fpi, R, Gm);
+  const double w = (a.weight_jxw && a.jxw != nullptr) ? a.jxw[gp] : 1.0;
+  double* tan = a.tangent;
+  auto store = [&](int kl, const double* col) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) tan[(int64_t)(9 * c + kl) * G + gp] = col[c] * w;
+  };
+  if (TANGENT && tan != nullptr)
+    cp_outputs<NS, true>(m, F, Gm, st, H, P, store);
+  else
+    cp_outputs<NS, false>(m, F, Gm, st, H, P, store);
+
+  if (a.pk1 != nullptr)
+#pragma unroll
+    for (int c = 0; c < 9; ++c) a.pk1[c * G + gp] = P[c] * w;
+  if (a.stress != nullptr) {
+    // sigma = P F^T / det F (models_copper.py:307-308)
+    double sig[9];
+    mm3_bt(P, F, sig);
+    const double idf = w / det3(F);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) a.stress[c * G + gp] = sig[c] * idf;
+  }
+  if (a.fpi_new != nullptr) {
+    double Fn[9];
+    mm3_bt(H, R, Fn);  // Fp^-1_old (I - R L R^T) = H R^T
+#pragma unroll
+    for (int c = 0; c < 9; ++c) a.fpi_new[c * G + gp] = Fn[c];
+  }
+  if (a.slip_new != nullptr)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) a.slip_new[s * G + gp] = a.slip[s * G + gp] + st.dg[s];
+  if (a.g_new != nullptr) {
+    double gn[NS];
+    cp_hardening<NS>(m, g, st.dg, hh, t_sat, gss_a, rq, gn);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) a.g_new[s * G + gp] = gn[s];
+  }
+  if (a.s_out != nullptr) {
+    double Sl[9], T1[9], Sg[9];
+    Sl[0] = st.s[0]; Sl[4] = st.s[1]; Sl[8] = st.s[2];
+    Sl[5] = Sl[7] = st.s[3];
+    Sl[2] = Sl[6] = st.s[4];
+    Sl[1] = Sl[3] = st.s[5];
+    mm3(R, Sl, T1);
+    mm3_bt(T1, R, Sg);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) a.s_out[c * G + gp] = Sg[c];
+  }
+  if (a.iters != nullptr) a.iters[gp] = st.iters;
+}
+
+// ------------------------------------------------------------------------------------
+// Element residual / tangent: one thread per (cell, node a) owns rows (a, 0..2).
+// ------------------------------------------------------------------------------------
+template <bool WITH_K>
+__global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ cells,
+                                                       const double* __restrict__ sg,
+                                                       const int32_t* __restrict__ nrp,
+                                                       const uint8_t* __restrict__ epos,
+                                                       const double* __restrict__ Pw,
+                                                       const double* __restrict__ Dw,
+                                                       double* __restrict__ res,
+                                                       double* __restrict__ vals) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t e = tid >> 3;
+  const int a = (int)(tid & 7);
+  if (e >= E) return;
+  const int64_t G = (int64_t)E * 8;
+  double K[3][24];
+  double Rr[3] = {0.0, 0.0, 0.0};
+  if (WITH_K) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int c = 0; c < 24; ++c) K[i][c] = 0.0;
+  }
+#pragma unroll 1
+  for (int q = 0; q < 8; ++q) {
+    const int64_t gp = e * 8 + q;
+    const double* sgq = sg + gp * 24;
+    const double ga0 = sgq[3 * a], ga1 = sgq[3 * a + 1], ga2 = sgq[3 * a + 2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      Rr[i] = fma(Pw[(3 * i) * G + gp], ga0, fma(Pw[(3 * i + 1) * G + gp], ga1, fma(Pw[(3 * i + 2) * G + gp], ga2, Rr[i])));
+    if (WITH_K) {
+      double Gm[27];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int kL = 0; kL < 9; ++kL)
+          Gm[9 * i + kL] = fma(ga0, Dw[(int64_t)(9 * (3 * i + 0) + kL) * G + gp],
+                           fma(ga1, Dw[(int64_t)(9 * (3 * i + 1) + kL) * G + gp],
+                               ga2 * Dw[(int64_t)(9 * (3 * i + 2) + kL) * G + gp]));
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const double gb0 = sgq[3 * b], gb1 = sgq[3 * b + 1], gb2 = sgq[3 * b + 2];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            K[i][3 * b + k] = fma(Gm[9 * i + 3 * k], gb0, fma(Gm[9 * i + 3 * k + 1], gb1,
+                              fma(Gm[9 * i + 3 * k + 2], gb2, K[i][3 * b + k])));
+      }
+    }
+  }
+  const int64_t na = cells[e * 8 + a];
+  if (res != nullptr)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) atomicAdd(&res[3 * na + i], Rr[i]);
+  if (WITH_K) {
+    const int64_t r0 = nrp[na];
+    const int64_t deg = nrp[na + 1] - r0;
+    const int64_t base = 9 * r0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int64_t pos = epos[e * 64 + 8 * a + b];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) atomicAdd(&vals[base + i * 3 * deg + 3 * pos + k], K[i][3 * b + k]);
+    }
+  }
+}
+
+// Row elimination for a list of unique Dirichlet dofs.
+__global__ void k_dirichlet(int32_t nbc, const int32_t* __restrict__ dofs, const double* __restrict__ bvals,
+                            const double* __restrict__ u, double* __restrict__ res,
+                            const int32_t* __restrict__ nrp, const int32_t* __restrict__ ncol,
+                            double* __restrict__ vals) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbc) return;
+  const int64_t d = dofs[t];
+  if (res != nullptr) {
+    double r = (u != nullptr) ? u[d] : 0.0;
+    res[d] = r - bvals[t];
+  }
+  if (vals != nullptr) {
+    const int64_t na = d / 3;
+    const int i = (int)(d % 3);
+    const int64_t r0 = nrp[na];
+    const int64_t deg = nrp[na + 1] - r0;
+    const int64_t base = 9 * r0 + i * 3 * deg;
+    for (int64_t v = 0; v < 3 * deg; ++v) vals[base + v] = 0.0;
+    for (int64_t j = 0; j < deg; ++j)
+      if (ncol[r0 + j] == na) vals[base + 3 * j + i] = 1.0;
+  }
+}
+
+__global__ void k_bc_guess(int32_t nbc, const int32_t* __restrict__ dofs, const double* __restrict__ bvals,
+                           const double* __restrict__ u, double* __restrict__ x0) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nbc) return;
+  const int64_t d = dofs[t];
+  x0[d] = bvals[t] - ((u != nullptr) ? u[d] : 0.0);
+}
+
+__global__ void k_cell_average(int32_t E, const double* __restrict__ jxw, const double* __restrict__ fw,
+                               double* __restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const int64_t G = (int64_t)E * 8;
+  double wsum = 0.0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) wsum += jxw[e * 8 + q];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc += fw[c * G + e * 8 + q];
+    out[e * 9 + c] = acc / wsum;
+  }
+}
+
+__global__ void k_axpy(int64_t n, double alpha, const double* __restrict__ x, double* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = fma(alpha, x[i], y[i]);
+}
+
+__global__ void __launch_bounds__(kVecThreads) k_dot(int64_t n, const double* __restrict__ x,
+                                                      const double* __restrict__ y, double* result,
+                                                      double* partials, unsigned int* counter) {
+  __shared__ double smem[32];
+  double v[1] = {0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[0] = fma(x[i], y[i], v[0]);
+  if (grid_sum<1>(v, partials, counter, smem) && threadIdx.x == 0) *result = v[0];
+}
+
+template <int NS>
+static int launch_gp(const MatDev& md, const cpfem_gp_args_t& a, cudaStream_t s) {
+  const int threads = 128;
+  const unsigned blocks = (unsigned)ceil_div(a.num_gp, threads);
+  if (a.tangent != nullptr)
+    k_gp_eval<NS, true><<<blocks, threads, 0, s>>>(md, a);
+  else
+    k_gp_eval<NS, false><<<blocks, threads, 0, s>>>(md, a);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+}  // namespace cpfem
+
+using namespace cpfem;
+
+extern "C" {
+
+int cpfem_abi_version(void) { return CPFEM_ABI_VERSION; }
+
+const char* cpfem_last_error(void) { return g_last_error.c_str(); }
+
+int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void* stream) {
+  CPFEM_REQUIRE(args != nullptr, "args is null");
+  MatDev md;
+  int rc = make_matdev(mat, &md);
+  if (rc != CPFEM_OK) return rc;
+  const cpfem_gp_args_t& a = *args;
+  if (a.num_gp == 0) return CPFEM_OK;
+  CPFEM_REQUIRE(a.num_gp > 0, "num_gp must be >= 0");
+  CPFEM_REQUIRE(a.fpi && a.g && a.rot_table && a.rot_idx && a.param_table, "state/table pointer is null");
+  CPFEM_REQUIRE(a.u != nullptr || a.u_grad != nullptr, "need u or u_grad");
+  if (a.u != nullptr) {
+    CPFEM_REQUIRE(a.cells && a.shape_grads, "u given without cells/shape_grads");
+    CPFEM_REQUIRE(a.num_gp == (int64_t)a.num_cells * 8, "num_gp must be 8*num_cells with nodal u");
+  }
+  CPFEM_REQUIRE(!(a.weight_jxw && a.jxw == nullptr), "weight_jxw without jxw");
+  CPFEM_REQUIRE(a.slip_new == nullptr || a.slip != nullptr, "slip_new needs slip");
+  CPFEM_REQUIRE(md.qmode == 0 || md.num_slip % 3 == 0, "qmode 1 needs num_slip % 3 == 0");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (md.num_slip == 12) return launch_gp<12>(md, a, s);
+  return launch_gp<24>(md, a, s);
+}
+
+int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* shape_grads,
+                        const int32_t* node_rowptr, const uint8_t* elem_pos, const double* pk1_w,
+                        const double* tangent_w, double* residual, double* values, void* stream) {
+  if (num_cells == 0) return CPFEM_OK;
+  CPFEM_REQUIRE(num_cells > 0 && cells && shape_grads && pk1_w, "bad element arguments");
+  CPFEM_REQUIRE((values == nullptr) == (tangent_w == nullptr), "values and tangent_w go together");
+  CPFEM_REQUIRE(values == nullptr || (node_rowptr && elem_pos), "values need the pattern");
+  const int threads = 128;
+  const unsigned blocks = (unsigned)ceil_div((int64_t)num_cells * 8, threads);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (values != nullptr)
+    k_elem_assemble<true><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, node_rowptr, elem_pos,
+                                                    pk1_w, tangent_w, residual, values);
+  else
+    k_elem_assemble<false><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, node_rowptr, elem_pos,
+                                                     pk1_w, nullptr, residual, nullptr);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+int cpfem_apply_dirichlet(int32_t num_bc, const int32_t* bc_dofs, const double* bc_vals, const double* u,
+                          double* residual, int32_t num_nodes, const int32_t* node_rowptr,
+                          const int32_t* node_cols, double* values, void* stream) {
+  if (num_bc == 0) return CPFEM_OK;
+  CPFEM_REQUIRE(num_bc > 0 && bc_dofs && bc_vals, "bad Dirichlet arguments");
+  CPFEM_REQUIRE(values == nullptr || (node_rowptr && node_cols && num_nodes > 0), "values need the pattern");
+  k_dirichlet<<<(unsigned)ceil_div(num_bc, 128), 128, 0, (cudaStream_t)stream>>>(
+      num_bc, bc_dofs, bc_vals, u, residual, node_rowptr, node_cols, values);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+int cpfem_bc_initial_guess(int64_t ndof, int32_t num_bc, const int32_t* bc_dofs, const double* bc_vals,
+                           const double* u, double* x0, void* stream) {
+  CPFEM_REQUIRE(ndof >= 0 && x0 != nullptr, "bad x0");
+  cudaStream_t s = (cudaStream_t)stream;
+  CPFEM_CUDA_TRY(cudaMemsetAsync(x0, 0, sizeof(double) * (size_t)ndof, s));
+  if (num_bc > 0) {
+    CPFEM_REQUIRE(bc_dofs && bc_vals, "bad Dirichlet arguments");
+    k_bc_guess<<<(unsigned)ceil_div(num_bc, 128), 128, 0, s>>>(num_bc, bc_dofs, bc_vals, u, x0);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+  }
+  return CPFEM_OK;
+}
+
+int cpfem_cell_average(int32_t num_cells, const double* jxw, const double* field_w, double* out,
+                       void* stream) {
+  if (num_cells == 0) return CPFEM_OK;
+  CPFEM_REQUIRE(num_cells > 0 && jxw && field_w && out, "bad cell-average arguments");
+  k_cell_average<<<(unsigned)ceil_div(num_cells, 128), 128, 0, (cudaStream_t)stream>>>(num_cells, jxw,
+                                                                                      field_w, out);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+int cpfem_axpy(int64_t n, double alpha, const double* x, double* y, void* stream) {
+  if (n == 0) return CPFEM_OK;
+  CPFEM_REQUIRE(n > 0 && x && y, "bad axpy arguments");
+  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
+  k_axpy<<<blocks, 256, 0, (cudaStream_t)stream>>>(n, alpha, x, y);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+size_t cpfem_dot_workspace_bytes(int64_t) { return 256 + sizeof(double) * kVecBlocks; }
+
+int cpfem_dot(int64_t n, const double* x, const double* y, double* result, void* workspace, void* stream) {
+  CPFEM_REQUIRE(n >= 0 && x && y && result && workspace, "bad dot arguments");
+  CPFEM_REQUIRE(((uintptr_t)workspace & 255) == 0, "workspace must be 256-byte aligned");
+  unsigned int* counter = (unsigned int*)workspace;
+  double* partials = (double*)((char*)workspace + 256);
+  cudaStream_t s = (cudaStream_t)stream;
+  CPFEM_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s));
+  k_dot<<<kVecBlocks, kVecThreads, 0, s>>>(n, x, y, result, partials, counter);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,185 @@
+// Shared helpers of the cpfem_gb300 CUDA sources: error reporting through the C ABI,
+// the device-side material block and small fixed-size linear algebra in registers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/cpfem_gb300.h"
+
+namespace cpfem {
+
+// Thread-local text behind cpfem_last_error().
+void set_error(const std::string& msg);
+
+#define CPFEM_CUDA_TRY(expr)                                                              \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      ::cpfem::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));             \
+      return CPFEM_ERR_CUDA;                                                              \
+    }                                                                                     \
+  } while (0)
+
+#define CPFEM_REQUIRE(cond, msg)                                                          \
+  do {                                                                                    \
+    if (!(cond)) {                                                                        \
+      ::cpfem::set_error(msg);                                                            \
+      return CPFEM_ERR_ARG;                                                               \
+    }                                                                                     \
+  } while (0)
+
+// Material block passed to kernels by value (it lands in the constant bank, so every
+// warp reads it as a broadcast).  Built on the host from cpfem_material_t.
+struct MatDev {
+  int num_slip;
+  int qmode;
+  int max_sub_step;
+  int max_iter;
+  double local_tol;
+  double ao;
+  double C11, C12, C44;
+  double d[CPFEM_MAX_SLIP][3];   // slip direction, lattice frame
+  double n[CPFEM_MAX_SLIP][3];   // slip-plane normal, lattice frame
+  double pv[CPFEM_MAX_SLIP][6];  // P = d n^T as (P11,P22,P33,P23+P32,P13+P31,P12+P21)
+  double p9[CPFEM_MAX_SLIP][9];  // P = d n^T row-major
+};
+
+int make_matdev(const cpfem_material_t* m, MatDev* out);
+
+// Launch geometry shared by the vector kernels: a fixed grid keeps the reduction order
+// (and so every dot product) identical from run to run.
+constexpr int kVecThreads = 256;
+constexpr int kVecBlocks = 2 * 152;
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---- 3x3 helpers (row-major) -------------------------------------------------------
+__device__ __forceinline__ void mm3(const double* A, const double* B, double* C) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[3 * i + j] = fma(A[3 * i + 0], B[0 + j], fma(A[3 * i + 1], B[3 + j], A[3 * i + 2] * B[6 + j]));
+}
+
+// C = A * B^T
+__device__ __forceinline__ void mm3_bt(const double* A, const double* B, double* C) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[3 * i + j] = fma(A[3 * i + 0], B[3 * j + 0], fma(A[3 * i + 1], B[3 * j + 1], A[3 * i + 2] * B[3 * j + 2]));
+}
+
+// C = A^T * B
+__device__ __forceinline__ void mm3_at(const double* A, const double* B, double* C) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[3 * i + j] = fma(A[0 + i], B[0 + j], fma(A[3 + i], B[3 + j], A[6 + i] * B[6 + j]));
+}
+
+__device__ __forceinline__ double det3(const double* A) {
+  return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+         A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+
+__device__ __forceinline__ void inv3(const double* A, double* Ai) {
+  const double c00 = A[4] * A[8] - A[5] * A[7];
+  const double c01 = A[5] * A[6] - A[3] * A[8];
+  const double c02 = A[3] * A[7] - A[4] * A[6];
+  const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+  const double id = 1.0 / det;
+  Ai[0] = c00 * id;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  Ai[3] = c01 * id;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  Ai[6] = c02 * id;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
+// Cubic stiffness applied to a symmetric tensor in 6-component form
+// (11,22,33,23,13,12), tensor components (not engineering shears).
+__device__ __forceinline__ void cubic_apply(const MatDev& m, const double* e, double* t) {
+  t[0] = fma(m.C11, e[0], m.C12 * (e[1] + e[2]));
+  t[1] = fma(m.C11, e[1], m.C12 * (e[0] + e[2]));
+  t[2] = fma(m.C11, e[2], m.C12 * (e[0] + e[1]));
+  const double c2 = 2.0 * m.C44;
+  t[3] = c2 * e[3];
+  t[4] = c2 * e[4];
+  t[5] = c2 * e[5];
+}
+
+// In-register LU with partial pivoting of an n x n matrix; all indices are static so
+// the matrix stays in registers.  Row swaps are done with predicated exchanges.
+template <int n>
+__device__ __forceinline__ void lu_factor(double* A, int* perm, double* dinv) {
+#pragma unroll
+  for (int i = 0; i < n; ++i) perm[i] = i;
+#pragma unroll
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double best = fabs(A[k * n + k]);
+#pragma unroll
+    for (int i = k + 1; i < n; ++i) {
+      const double v = fabs(A[i * n + k]);
+      if (v > best) { best = v; p = i; }
+    }
+#pragma unroll
+    for (int i = k + 1; i < n; ++i) {
+      if (p == i) {
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          const double t = A[k * n + j];
+          A[k * n + j] = A[i * n + j];
+          A[i * n + j] = t;
+        }
+        const int t = perm[k];
+        perm[k] = perm[i];
+        perm[i] = t;
+      }
+    }
+    const double inv = 1.0 / A[k * n + k];
+    dinv[k] = inv;
+#pragma unroll
+    for (int i = k + 1; i < n; ++i) {
+      const double l = A[i * n + k] * inv;
+      A[i * n + k] = l;
+#pragma unroll
+      for (int j = k + 1; j < n; ++j) A[i * n + j] = fma(-l, A[k * n + j], A[i * n + j]);
+    }
+  }
+}
+
+// Solve with the factors of lu_factor; b is overwritten by x.
+template <int n>
+__device__ __forceinline__ void lu_solve(const double* LU, const int* perm, const double* dinv, double* b) {
+  double y[n];
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+    double v = 0.0;
+#pragma unroll
+    for (int j = 0; j < n; ++j) v = (perm[i] == j) ? b[j] : v;
+    y[i] = v;
+  }
+#pragma unroll
+  for (int i = 0; i < n; ++i)
+#pragma unroll
+    for (int j = 0; j < i; ++j) y[i] = fma(-LU[i * n + j], y[j], y[i]);
+#pragma unroll
+  for (int i = n - 1; i >= 0; --i) {
+#pragma unroll
+    for (int j = i + 1; j < n; ++j) y[i] = fma(-LU[i * n + j], y[j], y[i]);
+    y[i] = y[i] * dinv[i];
+  }
+#pragma unroll
+  for (int i = 0; i < n; ++i) b[i] = y[i];
+}
+
+}  // namespace cpfem

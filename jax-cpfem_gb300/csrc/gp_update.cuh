@@ -1,0 +1,277 @@
+// Per-Gauss-point Kalidindi update, one thread per GP, everything in FP64 registers.
+//
+// The reference (singlecrystal_copper/models_copper.py:155-259) solves for the second
+// Piola-Kirchhoff stress S with 9 unknowns in the global frame:
+//   r(S) = S - C'(R) : (Fe^T Fe - I)/2,   Fe = F Fp^-1_old (I - sum_a dg_a R P_a R^T),
+//   dg_a = ao dt |tau_a/g_a|^(1/m) sign(tau_a),  tau_a = S : R P_a R^T.
+// Here the same Newton iterates are computed in the lattice frame with the 6 symmetric
+// unknowns s = R^T S R (11,22,33,23,13,12).  For an orthonormal R the residual norm, the
+// Newton step, the line search and the converged S are the reference's (the map is an
+// orthogonal change of variables, and from S0 = 0 the 9-unknown iterates stay
+// symmetric because C' : E is symmetric).  This costs a 6x6 rather than a 9x9 solve and
+// needs neither the rotated C' nor the rotated Schmid tensors.
+#pragma once
+
+#include "cpfem_common.cuh"
+
+namespace cpfem {
+
+template <int NS>
+struct GPSolve {
+  double s[6];      // converged lattice-frame S (tensor components)
+  double dg[NS];    // slip increments at s
+  double kk[NS];    // d(dg)/d(tau) at s
+  double B[9];      // I - L_p,lattice at s
+  double M[9];      // Ct * B at s
+  double rn;        // ||r|| at s
+  int iters;
+};
+
+// Residual at s.  Ct = (F Fp^-1_old R)^T (F Fp^-1_old R) (symmetric, full 3x3).
+template <int NS>
+__device__ __forceinline__ void cp_residual(const MatDev& m, const double* Ct, const double* ig,
+                                            double cdt, double pexp, const double* s, double* r,
+                                            double& rn, double* dg, double* kk, double* B,
+                                            double* M) {
+  double L[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) L[k] = 0.0;
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+    const double tau = fma(s[0], m.pv[a][0], fma(s[1], m.pv[a][1], fma(s[2], m.pv[a][2],
+                       fma(s[3], m.pv[a][3], fma(s[4], m.pv[a][4], s[5] * m.pv[a][5])))));
+    const double x = tau * ig[a];
+    const double ax = fabs(x);
+    // |x|^(p-1): dg = cdt |x|^(p-1) x = cdt |x|^p sign(tau) (g > 0), and the derivative
+    // p cdt |x|^(p-1) / g uses the same power.
+    const double pw1 = (ax > 0.0) ? pow(ax, pexp - 1.0) : 0.0;
+    const double d = cdt * pw1 * x;
+    dg[a] = d;
+    kk[a] = cdt * pexp * pw1 * ig[a];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) L[k] = fma(d, m.p9[a][k], L[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = ((k % 4) == 0 ? 1.0 : 0.0) - L[k];
+  mm3(Ct, B, M);
+  // E = (B^T M - I)/2 in 6-component form
+  double e[6];
+  e[0] = 0.5 * (fma(B[0], M[0], fma(B[3], M[3], B[6] * M[6])) - 1.0);
+  e[1] = 0.5 * (fma(B[1], M[1], fma(B[4], M[4], B[7] * M[7])) - 1.0);
+  e[2] = 0.5 * (fma(B[2], M[2], fma(B[5], M[5], B[8] * M[8])) - 1.0);
+  e[3] = 0.5 * fma(B[1], M[2], fma(B[4], M[5], B[7] * M[8]));
+  e[4] = 0.5 * fma(B[0], M[2], fma(B[3], M[5], B[6] * M[8]));
+  e[5] = 0.5 * fma(B[0], M[1], fma(B[3], M[4], B[6] * M[7]));
+  double t[6];
+  cubic_apply(m, e, t);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) r[k] = s[k] - t[k];
+  const double n2 = fma(r[0], r[0], fma(r[1], r[1], r[2] * r[2])) +
+                    2.0 * fma(r[3], r[3], fma(r[4], r[4], r[5] * r[5]));
+  rn = sqrt(n2);
+}
+
+// J = dr/ds = I + sum_a kk_a (C : sym(M^T d_a (x) n_a)) (x) pv_a
+template <int NS>
+__device__ __forceinline__ void cp_jacobian(const MatDev& m, const double* kk, const double* M,
+                                            double* J) {
+#pragma unroll
+  for (int i = 0; i < 36; ++i) J[i] = (i % 7 == 0) ? 1.0 : 0.0;
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+    const double* d = m.d[a];
+    const double* n = m.n[a];
+    double w[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) w[i] = fma(M[i], d[0], fma(M[3 + i], d[1], M[6 + i] * d[2]));
+    double q[6];
+    q[0] = w[0] * n[0];
+    q[1] = w[1] * n[1];
+    q[2] = w[2] * n[2];
+    q[3] = 0.5 * fma(w[1], n[2], w[2] * n[1]);
+    q[4] = 0.5 * fma(w[0], n[2], w[2] * n[0]);
+    q[5] = 0.5 * fma(w[0], n[1], w[1] * n[0]);
+    double t[6];
+    cubic_apply(m, q, t);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const double ti = kk[a] * t[i];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) J[6 * i + j] = fma(ti, m.pv[a][j], J[6 * i + j]);
+    }
+  }
+}
+
+// Local Newton from s0 = 0 with the cut-half line search of models_copper.py:218-245:
+// trial residuals at s + relax ds, relax = 1, 1/2, ..., until the norm drops below the
+// current one or max_sub_step trials were made; the last trial is taken.
+template <int NS>
+__device__ __forceinline__ void cp_local_newton(const MatDev& m, const double* Ct, const double* ig,
+                                                double cdt, double pexp, GPSolve<NS>& st) {
+  double r[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) st.s[k] = 0.0;
+  cp_residual<NS>(m, Ct, ig, cdt, pexp, st.s, r, st.rn, st.dg, st.kk, st.B, st.M);
+  int it = 0;
+  while (st.rn > m.local_tol && it < m.max_iter) {
+    double J[36];
+    int perm[6];
+    double dinv[6];
+    cp_jacobian<NS>(m, st.kk, st.M, J);
+    lu_factor<6>(J, perm, dinv);
+    double ds[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) ds[k] = -r[k];
+    lu_solve<6>(J, perm, dinv, ds);
+    const double rn0 = st.rn;
+    double relax = 1.0;
+    int sub = 0;
+    double st_s[6];
+    do {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) st_s[k] = fma(relax, ds[k], st.s[k]);
+      cp_residual<NS>(m, Ct, ig, cdt, pexp, st_s, r, st.rn, st.dg, st.kk, st.B, st.M);
+      relax *= 0.5;
+      ++sub;
+    } while (st.rn >= rn0 && sub < m.max_sub_step);
+    // s + 2 relax ds with the halved relax is exactly the last trial point
+#pragma unroll
+    for (int k = 0; k < 6; ++k) st.s[k] = st_s[k];
+    ++it;
+  }
+  st.iters = it;
+}
+
+// Stress and consistent tangent at the converged state.
+//   H = Fp^-1_old R B,  Fe_l = F H,  P = F Y,  Y = H s H^T / det H
+// dP/dF = d_ik Y_lJ + (dP/ds)(ds/dF) with ds/dF = J^-1 C : sym(Fe_l[k,:] (x) H[l,:]),
+// the implicit-function tangent of f_jvp (models_copper.py:251-259).
+// The tangent column for F_kl is handed to store_col(kl, col[9]) as soon as it is
+// known, so the 81 entries never need to be live at once.
+template <int NS, bool WITH_TANGENT, class StoreCol>
+__device__ __forceinline__ void cp_outputs(const MatDev& m, const double* F, const double* G /*Fp^-1_old R*/,
+                                           const GPSolve<NS>& st, double* H, double* P,
+                                           StoreCol store_col) {
+  double S[9], W[9], Y[9];
+  mm3(G, st.B, H);
+  S[0] = st.s[0]; S[4] = st.s[1]; S[8] = st.s[2];
+  S[5] = S[7] = st.s[3];
+  S[2] = S[6] = st.s[4];
+  S[1] = S[3] = st.s[5];
+  const double detH = det3(H);
+  const double idet = 1.0 / detH;
+  mm3_bt(S, H, W);           // W = s H^T
+  mm3(H, W, Y);              // H s H^T
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Y[k] *= idet;
+  mm3(F, Y, P);
+  if (!WITH_TANGENT) return;
+
+  // dP/ds for the 6 symmetric basis directions
+  double Bi[9];
+  inv3(st.B, Bi);
+  double dPds[6][9];
+#pragma unroll
+  for (int mm = 0; mm < 6; ++mm) {
+    double dL[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dL[k] = 0.0;
+#pragma unroll
+    for (int a = 0; a < NS; ++a) {
+      const double c = st.kk[a] * m.pv[a][mm];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dL[k] = fma(c, m.p9[a][k], dL[k]);
+    }
+    double trace = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) trace = fma(Bi[3 * i + j], dL[3 * j + i], trace);
+    double dH[9], V[9], dY[9];
+    mm3(G, dL, dH);          // G dL  (= -dH)
+    mm3(dH, W, V);           // V = (G dL) s H^T
+    const int ei = (mm < 3) ? mm : ((mm == 3) ? 1 : 0);
+    const int ej = (mm < 3) ? mm : ((mm == 5) ? 1 : 2);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double hh = H[3 * i + ei] * H[3 * j + ej];
+        if (mm >= 3) hh = fma(H[3 * i + ej], H[3 * j + ei], hh);
+        dY[3 * i + j] = fma(hh - V[3 * i + j] - V[3 * j + i], idet, Y[3 * i + j] * trace);
+      }
+    mm3(F, dY, dPds[mm]);
+  }
+
+  // ds/dF column by column through the factorised Jacobian at the converged s
+  double J[36];
+  int perm[6];
+  double dinv[6];
+  cp_jacobian<NS>(m, st.kk, st.M, J);
+  lu_factor<6>(J, perm, dinv);
+  double Fe[9];
+  mm3(F, H, Fe);
+#pragma unroll
+  for (int kl = 0; kl < 9; ++kl) {
+    const int k = kl / 3, l = kl % 3;
+    double a[3], b[3];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      a[t] = Fe[3 * k + t];
+      b[t] = H[3 * l + t];
+    }
+    double q[6], x[6];
+    q[0] = a[0] * b[0];
+    q[1] = a[1] * b[1];
+    q[2] = a[2] * b[2];
+    q[3] = 0.5 * fma(a[1], b[2], a[2] * b[1]);
+    q[4] = 0.5 * fma(a[0], b[2], a[2] * b[0]);
+    q[5] = 0.5 * fma(a[0], b[1], a[1] * b[0]);
+    cubic_apply(m, q, x);
+    lu_solve<6>(J, perm, dinv, x);
+    double col[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        double v = (i == k) ? Y[3 * l + j] : 0.0;
+#pragma unroll
+        for (int mm = 0; mm < 6; ++mm) v = fma(dPds[mm][3 * i + j], x[mm], v);
+        col[3 * i + j] = v;
+      }
+    store_col(kl, col);
+  }
+}
+
+// Explicit hardening and slip update after the local solve (models_copper.py:176-187;
+// per-GP parameters as in crystal_plasticity_OR_design/models_sens_rot.py:168-193).
+template <int NS>
+__device__ __forceinline__ void cp_hardening(const MatDev& m, const double* g, const double* dg,
+                                             double h, double t_sat, double gss_a, double rq,
+                                             double* g_new) {
+  double tmp[NS];
+  double total = 0.0;
+#pragma unroll
+  for (int b = 0; b < NS; ++b) {
+    const double ratio = 1.0 - g[b] / t_sat;
+    const double ar = fabs(ratio);
+    const double pw = (ar > 0.0) ? pow(ar, gss_a) : 0.0;
+    const double sg = (ratio > 0.0) ? 1.0 : ((ratio < 0.0) ? -1.0 : 0.0);
+    tmp[b] = h * fabs(dg[b]) * pw * sg;
+    total += tmp[b];
+  }
+  if (m.qmode == 0) {
+#pragma unroll
+    for (int a = 0; a < NS; ++a) g_new[a] = fma(rq, total, g[a]);
+  } else {
+#pragma unroll
+    for (int a0 = 0; a0 < NS; a0 += 3) {
+      const double blk = tmp[a0] + tmp[a0 + 1] + tmp[a0 + 2];
+      const double inc = fma(rq, total - blk, blk);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) g_new[a0 + j] = g[a0 + j] + inc;
+    }
+  }
+}
+
+}  // namespace cpfem

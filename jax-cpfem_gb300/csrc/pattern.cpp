@@ -1,0 +1,124 @@
+// Host-side sparsity pattern of a HEX8 mesh (node adjacency through shared cells).
+// The per-node sorted neighbour lists reproduce the column order scipy gives the
+// COO->CSR conversion of crystal_plasticity_OR_design/solver.py:279-282.
+#include <algorithm>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/cpfem_gb300.h"
+
+namespace cpfem {
+void set_error(const std::string& msg);
+}
+
+namespace {
+
+int check_cells(int32_t num_cells, const int32_t* cells, int32_t num_nodes) {
+  if (num_cells < 0 || num_nodes < 0 || (num_cells > 0 && cells == nullptr)) {
+    cpfem::set_error("bad mesh arguments");
+    return CPFEM_ERR_ARG;
+  }
+  for (int64_t i = 0; i < (int64_t)num_cells * 8; ++i)
+    if (cells[i] < 0 || cells[i] >= num_nodes) {
+      cpfem::set_error("cell node index out of range");
+      return CPFEM_ERR_ARG;
+    }
+  return CPFEM_OK;
+}
+
+// node -> incident cells (CSR)
+void incidence(int32_t num_cells, const int32_t* cells, int32_t num_nodes, std::vector<int64_t>& ptr,
+               std::vector<int32_t>& inc) {
+  ptr.assign((size_t)num_nodes + 1, 0);
+  for (int64_t i = 0; i < (int64_t)num_cells * 8; ++i) ptr[cells[i] + 1]++;
+  for (int32_t a = 0; a < num_nodes; ++a) ptr[a + 1] += ptr[a];
+  inc.resize((size_t)num_cells * 8);
+  std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+  for (int32_t e = 0; e < num_cells; ++e)
+    for (int k = 0; k < 8; ++k) inc[fill[cells[8 * (int64_t)e + k]]++] = e;
+}
+
+void neighbours(int32_t a, const int32_t* cells, const std::vector<int64_t>& ptr, const std::vector<int32_t>& inc,
+                std::vector<int32_t>& out) {
+  out.clear();
+  for (int64_t t = ptr[a]; t < ptr[a + 1]; ++t) {
+    const int32_t e = inc[t];
+    for (int k = 0; k < 8; ++k) out.push_back(cells[8 * (int64_t)e + k]);
+  }
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpfem_pattern_count(int32_t num_cells, const int32_t* cells, int32_t num_nodes, int64_t* num_blocks) {
+  int rc = check_cells(num_cells, cells, num_nodes);
+  if (rc) return rc;
+  if (!num_blocks) { cpfem::set_error("num_blocks is null"); return CPFEM_ERR_ARG; }
+  std::vector<int64_t> ptr;
+  std::vector<int32_t> inc, nb;
+  incidence(num_cells, cells, num_nodes, ptr, inc);
+  int64_t total = 0;
+  for (int32_t a = 0; a < num_nodes; ++a) {
+    neighbours(a, cells, ptr, inc, nb);
+    total += (int64_t)nb.size();
+  }
+  if (9 * total > INT32_MAX) { cpfem::set_error("pattern too large for int32 CSR"); return CPFEM_ERR_SIZE; }
+  *num_blocks = total;
+  return CPFEM_OK;
+}
+
+int cpfem_pattern_build(int32_t num_cells, const int32_t* cells, int32_t num_nodes, int32_t* node_rowptr,
+                        int32_t* node_cols, uint8_t* elem_pos, int32_t* node_tpos) {
+  int rc = check_cells(num_cells, cells, num_nodes);
+  if (rc) return rc;
+  if (!node_rowptr || !node_cols) { cpfem::set_error("pattern outputs are null"); return CPFEM_ERR_ARG; }
+  std::vector<int64_t> ptr;
+  std::vector<int32_t> inc, nb;
+  incidence(num_cells, cells, num_nodes, ptr, inc);
+  node_rowptr[0] = 0;
+  for (int32_t a = 0; a < num_nodes; ++a) {
+    neighbours(a, cells, ptr, inc, nb);
+    if (nb.size() > 255) { cpfem::set_error("node degree above 255"); return CPFEM_ERR_SIZE; }
+    std::copy(nb.begin(), nb.end(), node_cols + node_rowptr[a]);
+    node_rowptr[a + 1] = node_rowptr[a] + (int32_t)nb.size();
+  }
+  auto pos_of = [&](int32_t a, int32_t b) -> int32_t {
+    const int32_t* beg = node_cols + node_rowptr[a];
+    const int32_t* end = node_cols + node_rowptr[a + 1];
+    return (int32_t)(std::lower_bound(beg, end, b) - beg);
+  };
+  if (elem_pos)
+    for (int32_t e = 0; e < num_cells; ++e)
+      for (int a = 0; a < 8; ++a)
+        for (int b = 0; b < 8; ++b)
+          elem_pos[64 * (int64_t)e + 8 * a + b] = (uint8_t)pos_of(cells[8 * (int64_t)e + a], cells[8 * (int64_t)e + b]);
+  if (node_tpos)
+    for (int32_t a = 0; a < num_nodes; ++a)
+      for (int32_t j = node_rowptr[a]; j < node_rowptr[a + 1]; ++j) node_tpos[j] = pos_of(node_cols[j], a);
+  return CPFEM_OK;
+}
+
+int cpfem_pattern_expand_csr(int32_t num_nodes, const int32_t* node_rowptr, const int32_t* node_cols,
+                             int32_t* indptr, int32_t* indices) {
+  if (num_nodes < 0 || !node_rowptr || !node_cols || !indptr || !indices) {
+    cpfem::set_error("bad expand arguments");
+    return CPFEM_ERR_ARG;
+  }
+  indptr[0] = 0;
+  int64_t w = 0;
+  for (int32_t a = 0; a < num_nodes; ++a) {
+    const int32_t r0 = node_rowptr[a], r1 = node_rowptr[a + 1];
+    for (int i = 0; i < 3; ++i) {
+      for (int32_t j = r0; j < r1; ++j)
+        for (int k = 0; k < 3; ++k) indices[w++] = 3 * node_cols[j] + k;
+      indptr[3 * a + i + 1] = (int32_t)w;
+    }
+  }
+  return CPFEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,172 @@
+"""Global Newton solver with row elimination -- the ``solver(problem, solver_options)``
+entry point of ``crystal_plasticity_OR_design/solver.py`` (a vendored copy of JAX-FEM's
+solver), running on the GPU through the C ABI.
+
+Same control flow as the reference (``solver.py:310-437``):
+    res, A = newton_update_helper(dofs)
+    while rel_res > rel_tol and res > tol:
+        dofs = linear_incremental_solver(...)      # BiCGSTAB + Jacobi, optional line search
+        res, A = newton_update_helper(dofs)
+The tangent never leaves the device: assembly scatters into CSR values built on a
+pattern fixed at set-up, and the Dirichlet rows are eliminated in place.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _capi
+from .problem import DeviceCSR, _dev_ptr, _flat, _stream
+
+_KEYS = ("jax_solver", "umfpack_solver", "petsc_solver", "custom_solver")
+
+
+def _dot(problem, x, y):
+    ws = problem._buf("dot_ws", (int(problem.lib.cpfem_dot_workspace_bytes(x.numel())) // 8 + 64,))
+    out = problem._buf("dot_out", (1,))
+    _capi.check(problem.lib.cpfem_dot(x.numel(), _dev_ptr(x), _dev_ptr(y), _dev_ptr(out), _dev_ptr(ws), _stream()))
+    return float(out.item())
+
+
+def norm(problem, x):
+    return math.sqrt(_dot(problem, x, x))
+
+
+def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, check_every=32):
+    """``jax.scipy.sparse.linalg.bicgstab`` on the device CSR (``solver.py:34-40``).
+    precond: 0 none, 1 Jacobi 1/diag(A) (the reference), 2 3x3 block-Jacobi.
+    Returns (x, iterations or breakdown code, converged)."""
+    lib = problem.lib
+    x = x0.clone()
+    nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
+    ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
+    info = np.zeros(2, dtype=np.int32)
+    _capi.check(lib.cpfem_bicgstab(problem.num_nodes, _dev_ptr(problem.node_rowptr), _dev_ptr(problem.node_cols),
+                                   _dev_ptr(problem.node_tpos), _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
+                                   int(precond), 1 if A.transposed else 0, float(tol), float(atol), int(maxiter),
+                                   int(check_every), _dev_ptr(ws), info.ctypes.data, _stream()))
+    return x, int(info[0]), bool(info[1])
+
+
+def jax_solve(problem, A, b, x0, precond=True, opts=None):
+    """``solver.py:19-48``: BiCGSTAB, tol = atol = 1e-10, maxiter = 10000, then the
+    ``||Ax - b|| < 0.1`` check."""
+    opts = opts or {}
+    pc = opts.get("precond", precond)
+    pc = {True: 1, False: 0, "jacobi": 1, "block3": 2, "block_jacobi": 2}.get(pc, pc)
+    x, k, ok = bicgstab(problem, A, b, x0, precond=pc, tol=opts.get("tol", 1e-10),
+                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000),
+                        check_every=opts.get("check_every", 32))
+    problem.stats["krylov_iters"].append(k)
+    r = A.matvec(x)
+    r.sub_(b)
+    err = norm(problem, r)
+    if not err < 0.1:
+        raise RuntimeError(f"linear solver failed to converge with err = {err} (iterations {k})")
+    return x
+
+
+def linear_solver(problem, A, b, x0, solver_options):
+    """``solver.py:91-113``."""
+    if len(solver_options.keys() & set(_KEYS)) == 0:
+        solver_options["jax_solver"] = {}
+    if "jax_solver" in solver_options:
+        o = solver_options["jax_solver"] or {}
+        return jax_solve(problem, A, b, x0, o.get("precond", True), o)
+    if "custom_solver" in solver_options:
+        return solver_options["custom_solver"](A, b, x0, solver_options)
+    raise NotImplementedError("only 'jax_solver' (device BiCGSTAB) and 'custom_solver' run on the GPU; "
+                              "UMFPACK/PETSc host solvers are not part of the device path")
+
+
+def newton_update_helper(problem, dofs):
+    """Residual with BCs applied and the BC-eliminated device tangent (``solver.py:387-400``)."""
+    res_list = problem.newton_update(problem.unflatten_fn_sol_list(dofs))
+    res = res_list[0].reshape(-1)
+    problem.apply_dirichlet(res, dofs, problem.A_values)
+    return res, DeviceCSR(problem, problem.A_values)
+
+
+def residual_bc(problem, dofs):
+    res = problem.compute_residual(problem.unflatten_fn_sol_list(dofs))[0].reshape(-1)
+    problem.apply_dirichlet(res, dofs, None)
+    return res
+
+
+def initial_increment(problem, dofs):
+    """x0 = assign_bc(0) - copy_bc(dofs) (``solver.py:221-227``)."""
+    fe = problem.fes[0]
+    x0 = problem._buf("x0", (problem.num_total_dofs_all_vars,))
+    _capi.check(problem.lib.cpfem_bc_initial_guess(x0.numel(), int(fe.bc_dofs.numel()), _dev_ptr(fe.bc_dofs),
+                                                   _dev_ptr(fe.bc_vals), _dev_ptr(dofs), _dev_ptr(x0), _stream()))
+    return x0
+
+
+def line_search(problem, dofs, inc):
+    """``solver.py:240-276``: halve alpha up to 3 times while the BC residual norm drops."""
+    def res_norm(alpha):
+        d = dofs.clone()
+        _capi.check(problem.lib.cpfem_axpy(d.numel(), float(alpha), _dev_ptr(inc), _dev_ptr(d), _stream()))
+        return norm(problem, residual_bc(problem, d))
+    alpha = 1.0
+    rn = res_norm(alpha)
+    for _ in range(3):
+        alpha *= 0.5
+        rh = res_norm(alpha)
+        if rh > rn:
+            alpha *= 2.0
+            break
+        rn = rh
+    out = dofs.clone()
+    _capi.check(problem.lib.cpfem_axpy(out.numel(), float(alpha), _dev_ptr(inc), _dev_ptr(out), _stream()))
+    return out
+
+
+def linear_incremental_solver(problem, res_vec, A, dofs, solver_options):
+    """``solver.py:213-237``."""
+    b = torch.neg(res_vec)
+    x0 = initial_increment(problem, dofs)
+    inc = linear_solver(problem, A, b, x0, solver_options)
+    if solver_options.get("line_search_flag", False):
+        return line_search(problem, dofs, inc)
+    out = dofs.clone()
+    _capi.check(problem.lib.cpfem_axpy(out.numel(), 1.0, _dev_ptr(inc), _dev_ptr(out), _stream()))
+    return out
+
+
+def solver(problem, solver_options=None):
+    """Row-elimination Newton solve; returns ``[sol (num_nodes, 3)]``."""
+    solver_options = {} if solver_options is None else solver_options
+    start = time.time()
+    if solver_options.get("initial_guess") is not None:
+        dofs = _flat(solver_options["initial_guess"], problem.device).clone()
+    else:
+        dofs = torch.zeros(problem.num_total_dofs_all_vars, dtype=torch.float64, device=problem.device)
+    rel_tol = solver_options.get("rel_tol", 1e-8)
+    tol = solver_options.get("tol", 1e-6)
+    max_newton = solver_options.get("max_newton", 100)
+
+    res_vec, A = newton_update_helper(problem, dofs)
+    res_val = norm(problem, res_vec)
+    res_val_initial = res_val
+    rel_res_val = res_val / res_val_initial if res_val_initial > 0 else float("nan")
+    history = [res_val]
+    it = 0
+    while (rel_res_val > rel_tol) and (res_val > tol):
+        if it >= max_newton:
+            raise RuntimeError(f"global Newton did not converge in {max_newton} iterations (res = {res_val})")
+        dofs = linear_incremental_solver(problem, res_vec, A, dofs, solver_options)
+        res_vec, A = newton_update_helper(problem, dofs)
+        res_val = norm(problem, res_vec)
+        rel_res_val = res_val / res_val_initial
+        history.append(res_val)
+        it += 1
+    if not math.isfinite(res_val):
+        raise FloatingPointError("res_val contains NaN, stop the program!")
+    problem.stats["newton_iters"] = it
+    problem.stats["res_history"] = history
+    problem.stats["solve_time"] = time.time() - start
+    return problem.unflatten_fn_sol_list(dofs)

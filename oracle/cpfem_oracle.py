@@ -1,0 +1,606 @@
+"""CPU FP64 oracle for the CPFEM hot path -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
+
+This module is the checker.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+legs of ``bench.py`` (``cpu_baseline`` and ``--impl reference``) may import it; the
+product package never does, and it is never the thing measured as the GPU result.
+
+It is a plain numpy/scipy restatement of the reference algorithm, written so that each
+step can be read side by side with the reference source (paths relative to the
+reference project root):
+
+* per-Gauss-point Kalidindi update, S-based implicit local Newton with the cut-half
+  line search, linearised Fp^-1 update and explicit hardening:
+  ``singlecrystal_copper/models_copper.py:155-249`` (plain model) and
+  ``crystal_plasticity_OR_design/models_sens_rot.py:143-259`` (per-GP parameters);
+* the implicit-function tangent of the local solve (``custom_jvp`` ``f_jvp``,
+  ``models_copper.py:251-259``) -- here written out analytically;
+* HEX8 / 2x2x2 Gauss element residual ``int P : grad v`` and its tangent -- the
+  un-vendored JAX-FEM ``Problem`` kernels, restated from finite-element first principles
+  (call sites ``models_copper.py:277-278,315`` and ``crystal_plasticity_OR_design/solver.py:392``);
+* COO -> CSR with summed duplicates and sorted columns, row elimination of Dirichlet
+  rows (``solver.py:119-133,279-304``);
+* BiCGSTAB with the Jacobi preconditioner, tol = atol = 1e-10 (``solver.py:19-48``),
+  restating ``jax.scipy.sparse.linalg.bicgstab`` of JAX 0.4.x (the third-party
+  dependency; no version is pinned in the reference beyond a comment naming 0.4.13,
+  ``models_copper.py:206``);
+* the global Newton loop with its optional 3-halving line search (``solver.py:213-276,
+  310-437``);
+* ``compute_avg_stress`` / ``update_int_vars_gp`` (``models_copper.py:273-319``).
+
+Parity pins: the reference's own golden sigma_zz curves
+(``calibration/data/csv/calibration_case1/stress_strain_curve_copper.txt`` and
+``calibration/data/csv/calibration_case2/ss_curve_e-2.txt``), copied as fixtures under
+``tests/golden/`` by ``tests/golden/make_golden.py``.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+
+# ----------------------------------------------------------------------------------
+# Slip-system tables: rows are ``normal(3) direction(3)``, in the reference files' order
+# (``singlecrystal_copper/data/csv/input_slip_sys.txt``,
+#  ``polycrystal_DPsteel/data/csv/input_slip_sys_bcc12.txt``,
+#  ``polycrystal_DPsteel/data/csv/input_slip_sys_bcc24.txt``).  The order matters: the
+# latent-hardening matrix groups rows by the index rule 3*floor(i/3).
+# ----------------------------------------------------------------------------------
+FCC12 = np.array([
+    [1, 1, -1, 0, 1, 1], [1, 1, -1, 1, 0, 1], [1, 1, -1, 1, -1, 0],
+    [1, -1, -1, 0, 1, -1], [1, -1, -1, 1, 0, 1], [1, -1, -1, 1, 1, 0],
+    [1, -1, 1, 0, 1, 1], [1, -1, 1, 1, 0, -1], [1, -1, 1, 1, 1, 0],
+    [1, 1, 1, 0, 1, -1], [1, 1, 1, 1, 0, -1], [1, 1, 1, 1, -1, 0]], dtype=np.float64)
+
+BCC12 = np.array([
+    [1, 1, 0, -1, 1, 1], [1, 1, 0, 1, -1, 1], [1, -1, 0, 1, 1, 1], [1, -1, 0, 1, 1, -1],
+    [1, 0, 1, 1, 1, -1], [1, 0, 1, -1, 1, 1], [1, 0, -1, 1, 1, 1], [1, 0, -1, 1, -1, 1],
+    [0, 1, 1, 1, 1, -1], [0, 1, 1, 1, -1, 1], [0, 1, -1, 1, 1, 1], [0, 1, -1, -1, 1, 1]],
+    dtype=np.float64)
+
+BCC24 = np.concatenate([BCC12, np.array([
+    [1, 1, 2, 1, 1, -1], [-1, 1, 2, 1, -1, 1], [1, -1, 2, -1, 1, 1], [1, 1, -2, 1, 1, 1],
+    [1, 2, 1, 1, -1, 1], [-1, 2, 1, 1, 1, -1], [1, -2, 1, 1, 1, 1], [1, 2, -1, -1, 1, 1],
+    [2, 1, 1, -1, 1, 1], [-2, 1, 1, 1, 1, 1], [2, -1, 1, 1, 1, -1], [2, 1, -1, 1, -1, 1]],
+    dtype=np.float64)])
+
+SLIP_TABLES = {"fcc12": FCC12, "bcc12": BCC12, "bcc24": BCC24}
+
+
+def schmid_tensors(table):
+    """P_a = d_a (x) n_a with both vectors normalised (``models_copper.py:59-69``)."""
+    n = table[:, :3] / np.linalg.norm(table[:, :3], axis=1)[:, None]
+    d = table[:, 3:] / np.linalg.norm(table[:, 3:], axis=1)[:, None]
+    return np.einsum("ai,aj->aij", d, n)
+
+
+def q_matrix(num_slip, r, coplanar=True):
+    """Latent-hardening matrix.  ``coplanar=True`` follows ``models_copper.py:71-76``
+    (q = r, with ones on the 3-blocks given by 3*floor(i/3)); ``coplanar=False`` follows
+    ``models_sens_rot.py:170-175`` where the ``.at[].set`` result is discarded so q = r."""
+    q = r * np.ones((num_slip, num_slip))
+    if coplanar:
+        for i in range(num_slip):
+            for j in range(3):
+                q[i, i // 3 * 3 + j] = 1.0
+    return q
+
+
+def rot_mat(quat):
+    """Quaternion (scalar first, not normalised) -> rotation matrix (``models_copper.py:37-48``)."""
+    q = np.asarray(quat, dtype=np.float64)
+    q0, q1, q2, q3 = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    R = np.empty(q.shape[:-1] + (3, 3))
+    R[..., 0, 0] = q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3
+    R[..., 0, 1] = 2 * q1 * q2 - 2 * q0 * q3
+    R[..., 0, 2] = 2 * q1 * q3 + 2 * q0 * q2
+    R[..., 1, 0] = 2 * q1 * q2 + 2 * q0 * q3
+    R[..., 1, 1] = q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3
+    R[..., 1, 2] = 2 * q2 * q3 - 2 * q0 * q1
+    R[..., 2, 0] = 2 * q1 * q3 - 2 * q0 * q2
+    R[..., 2, 1] = 2 * q2 * q3 + 2 * q0 * q1
+    R[..., 2, 2] = q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3
+    return R
+
+
+def cubic_stiffness(C11, C12, C44):
+    """Fourth-order cubic stiffness with minor symmetries (``models_copper.py:92-130``)."""
+    C = np.zeros((3, 3, 3, 3))
+    for i in range(3):
+        C[i, i, i, i] = C11
+        for j in range(3):
+            if i != j:
+                C[i, i, j, j] = C12
+                C[i, j, i, j] = C44
+                C[i, j, j, i] = C44
+    return C
+
+
+def rotate_rank2(R, T):
+    """R T R^T for a stack of tensors (``models_copper.py:29-32``)."""
+    return np.einsum("...ia,...jb,...ab->...ij", R, R, T)
+
+
+def rotate_rank4(R, C):
+    """C'_ijkl = R_ia R_jb R_kc R_ld C_abcd (``models_copper.py:21-26``)."""
+    return np.einsum("...ia,...jb,...kc,...ld,abcd->...ijkl", R, R, R, R, C)
+
+
+# ----------------------------------------------------------------------------------
+# Per-GP constitutive update (vectorised over a batch of Gauss points)
+# ----------------------------------------------------------------------------------
+class GPBatch:
+    """Inputs of the local problem for G Gauss points.
+
+    Pr: (G,N,3,3) rotated Schmid tensors, Cr: (G,3,3,3,3) rotated stiffness,
+    Fpi: (G,3,3) old Fp^-1, g: (G,N) old slip resistance, xm: (G,) rate exponent m,
+    ao: reference slip rate, dt: time increment.
+    """
+
+    def __init__(self, F, Fpi, g, Pr, Cr, xm, ao, dt):
+        self.F, self.Fpi, self.g, self.Pr, self.Cr = F, Fpi, g, Pr, Cr
+        self.xm = np.broadcast_to(np.asarray(xm, dtype=np.float64), (F.shape[0],))
+        self.ao, self.dt = ao, dt
+        self.A = F @ Fpi
+
+    def subset(self, idx):
+        return GPBatch(self.F[idx], self.Fpi[idx], self.g[idx], self.Pr[idx], self.Cr[idx],
+                       self.xm[idx], self.ao, self.dt)
+
+
+def _slip_increment(b, S):
+    """tau, Delta gamma and d(Delta gamma)/d tau (``models_copper.py:173-174``)."""
+    tau = np.einsum("gij,gaij->ga", S, b.Pr)
+    x = tau / b.g
+    p = 1.0 / b.xm[:, None]
+    ax = np.abs(x)
+    dgam = b.ao * b.dt * ax ** p * np.sign(tau)
+    # derivative as JAX differentiates |x|**p * sign(tau): p |x|^(p-1) sign(x) sign(tau) / g
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kd = np.where(ax > 0, b.ao * b.dt * p * ax ** (p - 1.0) / b.g * np.sign(x) * np.sign(tau), 0.0)
+    return tau, dgam, kd
+
+
+def _kinematics(b, dgam):
+    """L_p increment, linearised Fp^-1 update and Fe (``models_copper.py:188-191``)."""
+    L = np.einsum("ga,gaij->gij", dgam, b.Pr)
+    Fpi_new = b.Fpi @ (np.eye(3) - L)
+    Fe = b.F @ Fpi_new
+    return Fpi_new, Fe
+
+
+def residual(b, S):
+    """r(S) = S - C' : (Fe^T Fe - I)/2 (``models_copper.py:195-201``).  S: (G,3,3)."""
+    _, dgam, _ = _slip_increment(b, S)
+    _, Fe = _kinematics(b, dgam)
+    E = 0.5 * (np.einsum("gki,gkj->gij", Fe, Fe) - np.eye(3))
+    return S - np.einsum("gijkl,gkl->gij", b.Cr, E)
+
+
+def jacobian(b, S):
+    """dr/dS (G,9,9), the quantity ``jax.jacfwd`` evaluates at ``models_copper.py:226``."""
+    _, dgam, kd = _slip_increment(b, S)
+    _, Fe = _kinematics(b, dgam)
+    dFe = -np.einsum("gij,gajk->gaik", b.A, b.Pr)             # dFe/dL contracted per system
+    Nsym = np.einsum("gki,gakj->gaij", Fe, dFe)
+    Nsym = 0.5 * (Nsym + np.swapaxes(Nsym, -1, -2))
+    CN = np.einsum("gijkl,gakl->gaij", b.Cr, Nsym)
+    J = -np.einsum("ga,gaij,gakl->gijkl", kd, CN, b.Pr).reshape(-1, 9, 9)
+    J += np.eye(9)
+    return J
+
+
+def local_newton(b, tol, max_sub_step, max_it=200):
+    """Local Newton on S from y0 = 0 with the cut-half line search, per lane exactly as
+    the batched ``lax.while_loop`` of ``models_copper.py:204-249`` behaves.
+
+    Returns S (G,3,3), iteration counts (G,), converged mask (G,).  ``max_it`` is a
+    safety cap the reference does not have; lanes that hit it report not-converged.
+    """
+    G = b.F.shape[0]
+    y = np.zeros((G, 3, 3))
+    r = residual(b, y)
+    rn = np.linalg.norm(r.reshape(G, 9), axis=1)
+    its = np.zeros(G, dtype=np.int64)
+    active = rn > tol
+    while active.any():
+        idx = np.nonzero(active & (its < max_it))[0]
+        if idx.size == 0:
+            break
+        bs = b.subset(idx)
+        ys, rs, rn0 = y[idx], r[idx], rn[idx]
+        J = jacobian(bs, ys)
+        dy = np.linalg.solve(J, -rs.reshape(-1, 9)[..., None])[..., 0].reshape(-1, 3, 3)
+        relax = np.ones(idx.size)
+        sub = np.zeros(idx.size, dtype=np.int64)
+        r_try, rn_try = rs.copy(), rn0.copy()
+        searching = (rn_try >= rn0) & (sub < max_sub_step)
+        while searching.any():
+            s = np.nonzero(searching)[0]
+            rt = residual(bs.subset(s), ys[s] + relax[s, None, None] * dy[s])
+            r_try[s] = rt
+            rn_try[s] = np.linalg.norm(rt.reshape(-1, 9), axis=1)
+            relax[s] *= 0.5
+            sub[s] += 1
+            searching = (rn_try >= rn0) & (sub < max_sub_step)
+        y[idx] = ys + 2.0 * relax[:, None, None] * dy
+        r[idx], rn[idx] = r_try, rn_try
+        its[idx] += 1
+        active = rn > tol
+    return y, its, ~(rn > tol)
+
+
+def first_pk_stress(b, S):
+    """sigma = Fe S Fe^T / det Fe ; P = det F sigma F^-T (``models_copper.py:155-162``)."""
+    _, dgam, _ = _slip_increment(b, S)
+    _, Fe = _kinematics(b, dgam)
+    sigma = (Fe @ S @ np.swapaxes(Fe, -1, -2)) / np.linalg.det(Fe)[:, None, None]
+    return np.linalg.det(b.F)[:, None, None] * sigma @ np.swapaxes(np.linalg.inv(b.F), -1, -2)
+
+
+def tangent(b, S):
+    """Consistent tangent dP/dF (G,3,3,3,3) at the converged S, via the implicit-function
+    theorem of ``f_jvp`` (``models_copper.py:251-259``): dS = -J_S^-1 (dr/dF) dF.
+
+    P = F X with X = Fp^-1 S Fp^-T / det(Fp^-1) (algebraically the reference P), and
+    Fp^-1 = Fp^-1_old (I - L(S)).
+    """
+    G = S.shape[0]
+    _, dgam, kd = _slip_increment(b, S)
+    Fpi_new, Fe = _kinematics(b, dgam)
+    I3 = np.eye(3)
+    # dr/dF_kl = -C' : sym(Fe^T e_k e_l^T Fpi_new)
+    T = np.einsum("gkm,gln->gklmn", Fe, Fpi_new)                  # (Fe^T e_k e_l^T Fpi)_mn
+    T = 0.5 * (T + np.swapaxes(T, -1, -2))
+    drdF = -np.einsum("gijmn,gklmn->gijkl", b.Cr, T).reshape(G, 9, 9)
+    J = jacobian(b, S)
+    dSdF = np.linalg.solve(J, -drdF)                               # (G, 9 [ij], 9 [kl])
+    detFpi = np.linalg.det(Fpi_new)
+    X = Fpi_new @ S @ np.swapaxes(Fpi_new, -1, -2) / detFpi[:, None, None]
+    # explicit part: dP_ij/dF_kl = delta_ik X_lj
+    D = np.einsum("ik,glj->gijkl", I3, X).reshape(G, 9, 9)
+    # dP/dS for the 9 basis directions e_mn of S
+    Finv_pi = np.linalg.inv(Fpi_new)
+    dPdS = np.empty((G, 9, 9))
+    for m in range(3):
+        for n in range(3):
+            dL = np.einsum("ga,ga,gaij->gij", kd, b.Pr[:, :, m, n], b.Pr)
+            dFpi = -b.Fpi @ dL
+            E = np.zeros((3, 3))
+            E[m, n] = 1.0
+            dX = (dFpi @ S @ np.swapaxes(Fpi_new, -1, -2) + Fpi_new @ E @ np.swapaxes(Fpi_new, -1, -2)
+                  + Fpi_new @ S @ np.swapaxes(dFpi, -1, -2)) / detFpi[:, None, None]
+            dX -= X * np.einsum("gij,gji->g", Finv_pi, dFpi)[:, None, None]
+            dPdS[:, :, 3 * m + n] = (b.F @ dX).reshape(G, 9)
+    D = D + dPdS @ dSdF
+    return D.reshape(G, 3, 3, 3, 3)
+
+
+def hardening_update(S, b, g, slip, h, t_sat, gss_a, r, coplanar):
+    """Explicit state update after the local solve (``models_copper.py:176-187``,
+    per-GP parameters as in ``models_sens_rot.py:168-193``)."""
+    _, dgam, _ = _slip_increment(b, S)
+    Fpi_new, _ = _kinematics(b, dgam)
+    ratio = 1.0 - g / t_sat[:, None]
+    tmp = h[:, None] * np.abs(dgam) * np.abs(ratio) ** gss_a[:, None] * np.sign(ratio)
+    N = g.shape[1]
+    qs = np.stack([q_matrix(N, ri, coplanar) for ri in np.unique(r)])
+    ridx = np.searchsorted(np.unique(r), r)
+    g_inc = np.einsum("gab,gb->ga", qs[ridx], tmp)
+    return Fpi_new, g + g_inc, slip + dgam
+
+
+# ----------------------------------------------------------------------------------
+# HEX8 element and mesh helpers (restated from FE first principles)
+# ----------------------------------------------------------------------------------
+HEX8_NODES = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1],
+                       [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], dtype=np.float64)
+_g = 1.0 / np.sqrt(3.0)
+HEX8_QUADS = np.array([[a, b, c] for c in (-_g, _g) for b in (-_g, _g) for a in (-_g, _g)])
+
+
+def hex8_dN_dxi(xi):
+    """dN_a/dxi_J at a point of the reference cube [-1,1]^3, gmsh node order."""
+    s = HEX8_NODES
+    t = 1.0 + s * xi[None, :]
+    d = np.empty((8, 3))
+    d[:, 0] = 0.125 * s[:, 0] * t[:, 1] * t[:, 2]
+    d[:, 1] = 0.125 * s[:, 1] * t[:, 0] * t[:, 2]
+    d[:, 2] = 0.125 * s[:, 2] * t[:, 0] * t[:, 1]
+    return d
+
+
+def shape_grads_and_jxw(points, cells):
+    """Physical shape-function gradients (E,8 quads,8 nodes,3) and JxW (E,8)."""
+    X = points[cells]                                              # (E,8,3)
+    E = cells.shape[0]
+    sg = np.empty((E, 8, 8, 3))
+    jxw = np.empty((E, 8))
+    for q, xi in enumerate(HEX8_QUADS):
+        dN = hex8_dN_dxi(xi)                                       # (8,3)
+        Jm = np.einsum("eai,aj->eij", X, dN)                       # dx_i/dxi_j
+        Jinv = np.linalg.inv(Jm)
+        sg[:, q] = np.einsum("aj,eji->eai", dN, Jinv)
+        jxw[:, q] = np.linalg.det(Jm) * 1.0                        # Gauss weight 1
+    return sg, jxw
+
+
+def box_mesh(nx, ny, nz, Lx=1.0, Ly=1.0, Lz=1.0):
+    """Structured hex8 box, nodes x-fastest, gmsh-ordered connectivity."""
+    xs, ys, zs = (np.linspace(0, L, n + 1) for L, n in ((Lx, nx), (Ly, ny), (Lz, nz)))
+    Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+    points = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    nid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    cells = np.stack([nid(i, j, k), nid(i + 1, j, k), nid(i + 1, j + 1, k), nid(i, j + 1, k),
+                      nid(i, j, k + 1), nid(i + 1, j, k + 1), nid(i + 1, j + 1, k + 1),
+                      nid(i, j + 1, k + 1)], axis=1).astype(np.int64)
+    return points, cells
+
+
+# ----------------------------------------------------------------------------------
+# Problem: internal variables, assembly, solver
+# ----------------------------------------------------------------------------------
+class OracleProblem:
+    """Restates the ``CrystalPlasticity(Problem)`` data model of the parameterised models
+    (``models_sens_rot.py:52-139``): internal_vars =
+    [Fp_inv (E,Q,3,3), g (E,Q,N), slip (E,Q,N), rot (E,Q,3,3), gss_a, h, t_sat, xm, r (E,Q)]."""
+
+    def __init__(self, points, cells, slip_table, C11, C12, C44, quat, cell_ori_inds,
+                 gss_initial, h, t_sat, gss_a, xm, r, ao=1e-3, coplanar=False,
+                 local_tol=1e-8, max_sub_step=5, bcs=()):
+        self.points, self.cells = np.asarray(points, np.float64), np.asarray(cells, np.int64)
+        self.E = self.cells.shape[0]
+        self.n_nodes = self.points.shape[0]
+        self.ndof = 3 * self.n_nodes
+        self.schmid = schmid_tensors(np.asarray(slip_table, np.float64))
+        self.N = self.schmid.shape[0]
+        self.C = cubic_stiffness(C11, C12, C44)
+        self.ao, self.coplanar = ao, coplanar
+        self.local_tol, self.max_sub_step = local_tol, max_sub_step
+        self.sg, self.jxw = shape_grads_and_jxw(self.points, self.cells)
+        rots = rot_mat(np.asarray(quat, np.float64))[np.asarray(cell_ori_inds)]
+        E, Q, N = self.E, 8, self.N
+        ones = np.ones((E, Q))
+        self.internal_vars = [
+            np.broadcast_to(np.eye(3), (E, Q, 3, 3)).copy(),
+            gss_initial * np.ones((E, Q, N)),
+            np.zeros((E, Q, N)),
+            np.repeat(rots[:, None], Q, axis=1),
+            gss_a * ones, h * ones, t_sat * ones, xm * ones, r * ones]
+        self.dt = 1.0
+        self.set_bcs(bcs)
+
+    # --- Dirichlet data: list of (node_inds, component, value) -------------------
+    def set_bcs(self, bcs):
+        self.bcs = [(np.asarray(n, np.int64), int(c), float(v)) for n, c, v in bcs]
+
+    def bc_dofs_vals(self):
+        dofs = np.concatenate([3 * n + c for n, c, _ in self.bcs]) if self.bcs else np.zeros(0, np.int64)
+        vals = np.concatenate([np.full(n.size, v) for n, _, v in self.bcs]) if self.bcs else np.zeros(0)
+        return dofs, vals
+
+    # --- per-GP batch ---------------------------------------------------------------
+    def u_grads(self, sol):
+        """u_grad (E,Q,3,3) = sum_a u_a (x) dN_a/dX (``models_copper.py:277-278``)."""
+        return np.einsum("eai,eqaj->eqij", sol.reshape(-1, 3)[self.cells], self.sg)
+
+    def gp_batch(self, sol, params):
+        Fpi, g, _, rot = params[:4]
+        xm = params[7]
+        G = self.E * 8
+        F = (self.u_grads(sol) + np.eye(3)).reshape(G, 3, 3)
+        R = rot.reshape(G, 3, 3)
+        # the rotated tables only depend on the rotation: compute once per distinct R
+        Ru, inv = np.unique(R.reshape(G, 9), axis=0, return_inverse=True)
+        Ru = Ru.reshape(-1, 3, 3)
+        Pr_u = np.einsum("uia,ujb,kab->ukij", Ru, Ru, self.schmid)
+        Cr_u = rotate_rank4(Ru, self.C)
+        inv = inv.reshape(-1)
+        return GPBatch(F, Fpi.reshape(G, 3, 3), g.reshape(G, self.N), Pr_u[inv], Cr_u[inv],
+                       xm.reshape(G), self.ao, self.dt)
+
+    def solve_gps(self, b):
+        S, its, ok = local_newton(b, self.local_tol, self.max_sub_step)
+        if not ok.all():
+            raise RuntimeError("oracle local Newton did not converge")
+        return S, its
+
+    # --- assembly ------------------------------------------------------------------
+    def newton_update(self, sol, params=None, need_tangent=True):
+        """Residual (ndof,) and, if asked, the CSR tangent with summed duplicates
+        (what JAX-FEM's newton_update + ``solver.py:279-282`` produce)."""
+        params = self.internal_vars if params is None else params
+        b = self.gp_batch(sol, params)
+        S, its = self.solve_gps(b)
+        self.last_local_its = its
+        E = self.E
+        P = first_pk_stress(b, S).reshape(E, 8, 3, 3)
+        res_e = np.einsum("eqij,eqaj,eq->eai", P, self.sg, self.jxw)
+        dof = (3 * self.cells[:, :, None] + np.arange(3)[None, None, :]).reshape(E, 24)
+        res = np.bincount(dof.ravel(), weights=res_e.ravel(), minlength=self.ndof)
+        if not need_tangent:
+            return res, None
+        D = tangent(b, S).reshape(E, 8, 3, 3, 3, 3)
+        Ke = np.einsum("eqaj,eqijkl,eqbl,eq->eaibk", self.sg, D, self.sg, self.jxw).reshape(E, 24, 24)
+        I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
+        J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
+        A = sp.csr_array((Ke.ravel(), (I, J)), shape=(self.ndof, self.ndof))
+        A.sum_duplicates()
+        A.sort_indices()
+        return res, A
+
+    def compute_residual(self, sol, params=None):
+        return self.newton_update(sol, params, need_tangent=False)[0]
+
+    # --- post-processing / state update -------------------------------------------
+    def compute_avg_stress(self, sol, params):
+        """Per-cell JxW-weighted Cauchy stress (``models_copper.py:297-319``)."""
+        b = self.gp_batch(sol, params)
+        S, _ = self.solve_gps(b)
+        P = first_pk_stress(b, S)
+        sigma = P @ np.swapaxes(b.F, -1, -2) / np.linalg.det(b.F)[:, None, None]
+        sigma = sigma.reshape(self.E, 8, 3, 3)
+        return np.einsum("eqij,eq->eij", sigma, self.jxw) / self.jxw.sum(1)[:, None, None]
+
+    def update_int_vars_gp(self, sol, params):
+        """New internal variables at the converged solution (``models_copper.py:273-282``)."""
+        b = self.gp_batch(sol, params)
+        S, _ = self.solve_gps(b)
+        G, E, N = S.shape[0], self.E, self.N
+        gss_a, h, t_sat, xm, r = (p.reshape(G) for p in params[4:9])
+        Fpi_new, g_new, slip_new = hardening_update(
+            S, b, params[1].reshape(G, N), params[2].reshape(G, N), h, t_sat, gss_a, r, self.coplanar)
+        return [Fpi_new.reshape(E, 8, 3, 3), g_new.reshape(E, 8, N), slip_new.reshape(E, 8, N)] + \
+            [p.copy() for p in params[3:]]
+
+    def set_params(self, params):
+        self.internal_vars = params
+
+
+# ----------------------------------------------------------------------------------
+# Linear solver and global Newton (``solver.py``)
+# ----------------------------------------------------------------------------------
+def bicgstab(A, b, x0, M, tol=1e-10, atol=1e-10, maxiter=10000):
+    """BiCGSTAB as ``jax.scipy.sparse.linalg.bicgstab`` (JAX 0.4.x) runs it: stop on
+    ||r||^2 <= max(tol^2 ||b||^2, atol^2) of the true residual, early exit on ||s||,
+    breakdown codes -10 (rho = 0) / -11 (alpha or omega = 0).  Returns (x, iterations)."""
+    atol2 = max(tol * tol * float(b @ b), atol * atol)
+    x = x0.copy()
+    r = b - A @ x
+    rhat, p, q = r.copy(), r.copy(), r.copy()
+    rho = alpha = omega = 1.0
+    k = 0
+    while float(r @ r) > atol2 and 0 <= k < maxiter:
+        rho_ = float(rhat @ r)
+        beta = rho_ / rho * alpha / omega
+        p = r + beta * (p - omega * q)
+        phat = M(p)
+        q = A @ phat
+        alpha = rho_ / float(rhat @ q)
+        s = r - alpha * q
+        exit_early = float(s @ s) < atol2
+        shat = M(s)
+        t = A @ shat
+        omega = float(t @ s) / float(t @ t)
+        if exit_early:
+            x = x + alpha * phat
+            r = s
+        else:
+            x = x + (alpha * phat + omega * shat)
+            r = s - omega * t
+        k = -11 if (omega == 0 or alpha == 0) else k + 1
+        k = -10 if rho_ == 0 else k
+        rho = rho_
+    return x, k
+
+
+def apply_bc_rows(A, bc_dofs):
+    """PETSc ``zeroRows``: BC rows become unit rows (``solver.py:290-293``)."""
+    A = A.tolil() if False else A.copy()
+    A = A.tocsr()
+    rows = np.unique(bc_dofs)
+    mask = np.zeros(A.shape[0], dtype=bool)
+    mask[rows] = True
+    row_of = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+    A.data[mask[row_of]] = 0.0
+    diag_pos = mask[row_of] & (A.indices == row_of)
+    A.data[diag_pos] = 1.0
+    return A
+
+
+def solver(problem, solver_options=None):
+    """Global Newton with row elimination (``solver.py:310-437``).
+
+    Returns (dofs, info) with info = {newton_iters, krylov_iters: [...]}.
+    """
+    opts = dict(solver_options or {})
+    rel_tol = opts.get("rel_tol", 1e-8)
+    tol = opts.get("tol", 1e-6)
+    ls_flag = opts.get("line_search_flag", False)
+    dofs = np.array(opts["initial_guess"], dtype=np.float64).reshape(-1) if opts.get("initial_guess") is not None \
+        else np.zeros(problem.ndof)
+    bc_dofs, bc_vals = problem.bc_dofs_vals()
+
+    def res_bc(d, res):
+        res = res.copy()
+        res[bc_dofs] = d[bc_dofs]
+        res[bc_dofs] -= bc_vals
+        return res
+
+    def helper(d):
+        res, A = problem.newton_update(d)
+        return res_bc(d, res), apply_bc_rows(A, bc_dofs)
+
+    res, A = helper(dofs)
+    rv = np.linalg.norm(res)
+    r0 = rv
+    info = {"newton_iters": 0, "krylov_iters": [], "res_history": [rv]}
+    while (rv / r0 > rel_tol if r0 > 0 else False) and rv > tol:
+        x0 = np.zeros(problem.ndof)
+        x0[bc_dofs] = bc_vals
+        x0[bc_dofs] -= dofs[bc_dofs]
+        diag = A.diagonal()
+        inc, kk = bicgstab(A, -res, x0, lambda v: v * (1.0 / diag))
+        err = np.linalg.norm(A @ inc + res)
+        if not err < 0.1:
+            raise RuntimeError(f"oracle linear solver failed, err={err}")
+        info["krylov_iters"].append(kk)
+        if ls_flag:
+            dofs = _line_search(problem, dofs, inc, res_bc)
+        else:
+            dofs = dofs + inc
+        res, A = helper(dofs)
+        rv = np.linalg.norm(res)
+        info["newton_iters"] += 1
+        info["res_history"].append(rv)
+    if not (np.isfinite(rv) and np.all(np.isfinite(dofs))):
+        raise RuntimeError("oracle Newton produced non-finite values")
+    return dofs, info
+
+
+def _line_search(problem, dofs, inc, res_bc):
+    """Three halvings, keep the last improving alpha (``solver.py:240-276``)."""
+    def res_norm(alpha):
+        d = dofs + alpha * inc
+        return np.linalg.norm(res_bc(d, problem.compute_residual(d)))
+    alpha = 1.0
+    rn = res_norm(alpha)
+    for _ in range(3):
+        alpha *= 0.5
+        rh = res_norm(alpha)
+        if rh > rn:
+            alpha *= 2.0
+            break
+        rn = rh
+    return dofs + alpha * inc
+
+
+def face_nodes(points, axis, value, atol=1e-5):
+    return np.nonzero(np.isclose(points[:, axis], value, atol=atol))[0]
+
+
+def corner_nodes(points, xyz, atol=1e-5):
+    m = np.ones(points.shape[0], dtype=bool)
+    for a, v in enumerate(xyz):
+        m &= np.isclose(points[:, a], v, atol=atol)
+    return np.nonzero(m)[0]
+
+
+def run_load_steps(problem, disps, ts, make_bcs, solver_options=None, stress_fn=None):
+    """Driver loop of ``calibration_case1_singleCrystalCopper_GB.py:270-292``: per step
+    set dt and the top displacement, solve, record the stress, commit the state."""
+    sol = np.zeros(problem.ndof)
+    out = []
+    params = problem.internal_vars
+    for i in range(len(ts) - 1):
+        problem.dt = float(ts[i + 1] - ts[i])
+        problem.set_bcs(make_bcs(float(disps[i + 1])))
+        problem.set_params(params)
+        opts = dict(solver_options or {})
+        opts["initial_guess"] = sol
+        sol, _ = solver(problem, opts)
+        sig = problem.compute_avg_stress(sol, params)
+        out.append(stress_fn(sig) if stress_fn else sig)
+        params = problem.update_int_vars_gp(sol, params)
+    problem.set_params(params)
+    return np.array(out), sol

@@ -1,0 +1,149 @@
+"""Host-side checks that need no GPU: the shared library loads and exports every
+declared entry point, the host pattern builder reproduces scipy's COO->CSR, host logic."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(cpfem_\w+)\s*\(", src, re.M))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib(pkg):
+    from importlib import import_module
+    capi = import_module("jax-cpfem_gb300._capi")
+    if not os.path.exists(capi.LIB_PATH):
+        import_module("jax-cpfem_gb300.build").build()
+    return capi.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    from importlib import import_module
+    capi = import_module("jax-cpfem_gb300._capi")
+    assert names == set(capi.SIGNATURES), names ^ set(capi.SIGNATURES)
+    assert lib.cpfem_abi_version() == 1
+
+
+def _pattern(lib, cells, n_nodes):
+    cells = np.ascontiguousarray(cells, dtype=np.int32)
+    nb = np.zeros(1, np.int64)
+    assert lib.cpfem_pattern_count(cells.shape[0], cells.ctypes.data, n_nodes, nb.ctypes.data) == 0
+    nb = int(nb[0])
+    rp = np.zeros(n_nodes + 1, np.int32)
+    cols = np.zeros(nb, np.int32)
+    epos = np.zeros(cells.shape[0] * 64, np.uint8)
+    tpos = np.zeros(nb, np.int32)
+    assert lib.cpfem_pattern_build(cells.shape[0], cells.ctypes.data, n_nodes, rp.ctypes.data, cols.ctypes.data,
+                                   epos.ctypes.data, tpos.ctypes.data) == 0
+    indptr = np.zeros(3 * n_nodes + 1, np.int32)
+    indices = np.zeros(9 * nb, np.int32)
+    assert lib.cpfem_pattern_expand_csr(n_nodes, rp.ctypes.data, cols.ctypes.data, indptr.ctypes.data,
+                                        indices.ctypes.data) == 0
+    return rp, cols, epos, tpos, indptr, indices
+
+
+def _scipy_pattern(cells, n_nodes):
+    E = cells.shape[0]
+    dof = (3 * cells[:, :, None] + np.arange(3)).reshape(E, 24)
+    I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
+    J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
+    V = np.arange(I.size, dtype=np.float64) + 1.0
+    A = sp.csr_array((V, (I, J)), shape=(3 * n_nodes, 3 * n_nodes))
+    A.sum_duplicates()
+    A.sort_indices()
+    return A, I, J, V
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (3, 2, 2), (4, 4, 4)])
+def test_pattern_matches_scipy_coo_to_csr(lib, pkg, shape):
+    m = pkg.box_mesh(*shape)
+    n = m.points.shape[0]
+    rp, cols, epos, tpos, indptr, indices = _pattern(lib, m.cells, n)
+    A, I, J, V = _scipy_pattern(m.cells, n)
+    assert np.array_equal(indptr, A.indptr) and np.array_equal(indices, A.indices)
+    # scattering the COO values through elem_pos gives scipy's summed CSR values
+    vals = np.zeros(9 * cols.size)
+    E = m.cells.shape[0]
+    Ke = V.reshape(E, 8, 3, 8, 3)
+    for e in range(E):
+        for a in range(8):
+            na = m.cells[e, a]
+            deg = rp[na + 1] - rp[na]
+            for b in range(8):
+                pos = epos[64 * e + 8 * a + b]
+                for i in range(3):
+                    for k in range(3):
+                        vals[9 * rp[na] + i * 3 * deg + 3 * pos + k] += Ke[e, a, i, b, k]
+    assert np.array_equal(vals, A.data)
+    # transpose positions
+    for a in range(n):
+        for j in range(rp[a], rp[a + 1]):
+            b = cols[j]
+            assert cols[rp[b] + tpos[j]] == a
+
+
+def test_pattern_on_permuted_irregular_numbering(lib, pkg):
+    m = pkg.box_mesh(3, 3, 2)
+    n = m.points.shape[0]
+    perm = np.random.default_rng(0).permutation(n)
+    cells = perm[m.cells]
+    rp, cols, epos, tpos, indptr, indices = _pattern(lib, cells, n)
+    A, *_ = _scipy_pattern(cells, n)
+    assert np.array_equal(indptr, A.indptr) and np.array_equal(indices, A.indices)
+
+
+def test_pattern_rejects_bad_node_index(lib):
+    cells = np.arange(8, dtype=np.int32).reshape(1, 8)
+    nb = np.zeros(1, np.int64)
+    assert lib.cpfem_pattern_count(1, cells.ctypes.data, 7, nb.ctypes.data) != 0
+    assert b"out of range" in lib.cpfem_last_error()
+
+
+def test_material_struct_and_specs(pkg):
+    m = pkg.material.BENCH_TANTALUM.to_ctypes()
+    assert m.num_slip == 24 and m.qmode == 1 and m.C11 == 267.0e3
+    d = np.array([[m.slip_d[a][i] for i in range(3)] for a in range(24)])
+    nrm = np.array([[m.slip_n[a][i] for i in range(3)] for a in range(24)])
+    assert np.allclose(np.linalg.norm(d, axis=1), 1) and np.abs((d * nrm).sum(1)).max() < 1e-15
+    assert pkg.material.CALIB_CASE1.to_ctypes().qmode == 0
+
+
+def test_bc_lists_later_entry_wins(pkg):
+    import torch
+    from importlib import import_module
+    prob_mod = import_module("jax-cpfem_gb300.problem")
+    fe = prob_mod.FiniteElement.__new__(prob_mod.FiniteElement)
+    fe.device = torch.device("cpu")
+    fe.set_dirichlet_lists([np.array([0, 1]), np.array([1, 2])], [2, 2], [0.0, 5.0])
+    assert fe.bc_dofs.tolist() == [2, 5, 8] and fe.bc_vals.tolist() == [0.0, 5.0, 5.0]
+
+
+def test_orthonormal_check_rejects_unnormalised_quaternion(pkg):
+    R = pkg.material.rot_mat(np.array([[2.0, 0, 0, 0]]))
+    with pytest.raises(ValueError):
+        pkg.material.check_orthonormal(R)
+
+
+def test_product_code_never_imports_the_oracle():
+    pkg_dir = os.path.join(ROOT, "jax-cpfem_gb300")
+    for dirpath, _, files in os.walk(pkg_dir):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp")):
+                src = open(os.path.join(dirpath, f)).read()
+                assert "oracle" not in src.replace("oracle/_ref", ""), f

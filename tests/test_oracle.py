@@ -1,0 +1,133 @@
+"""CPU checks of the oracle itself: the reference's golden curves, FD of the tangent,
+the BiCGSTAB restatement, rotation conventions."""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from oracle import cpfem_oracle as O
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+
+
+def _one_element(table, C, params, coplanar, tol_local, max_sub):
+    pts, cells = O.box_mesh(1, 1, 1)
+    return pts, O.OracleProblem(pts, cells, table, *C, [[1, 0, 0, 0]], np.zeros(1, int), coplanar=coplanar,
+                                local_tol=tol_local, max_sub_step=max_sub, **params)
+
+
+def _corner_bcs(pts):
+    c = O.corner_nodes(pts, (0, 0, 0))
+    return lambda d: [(c, 0, 0.0), (c, 1, 0.0), (O.face_nodes(pts, 2, 0.0), 2, 0.0),
+                      (O.face_nodes(pts, 2, 1.0), 2, d)]
+
+
+def test_golden_case1_copper():
+    """calibration_case1: 1-element copper, 20 steps of 1.25e-3, dt 0.125, tol 1e-7."""
+    pts, prob = _one_element(O.FCC12, (1.684e5, 1.214e5, 0.754e5),
+                             dict(gss_initial=60.8, h=541.5, t_sat=109.8, gss_a=2.5, xm=0.1, r=1.0),
+                             False, 1e-8, 5)
+    s, _ = O.run_load_steps(prob, np.linspace(0, 0.025, 21), np.linspace(0, 2.5, 21), _corner_bcs(pts),
+                            {"tol": 1e-7}, stress_fn=lambda sg: sg[0, 2, 2])
+    gold = GOLD["case1_szz"][:20]
+    rel = np.abs(s - gold) / np.abs(gold)
+    assert rel.max() < 1e-8, rel
+
+
+def test_golden_case2_tantalum():
+    """calibration_case2: 1-element Ta (BCC12), compression 40 steps, global line search."""
+    pts, prob = _one_element(O.BCC12, (2.670e5, 1.610e5, 0.825e5),
+                             dict(gss_initial=67.4641, h=1959.1320, t_sat=7295.1754, gss_a=200.0,
+                                  xm=1.0 / 45.2726, r=1.0), False, 1e-8, 5)
+    s, _ = O.run_load_steps(prob, np.linspace(0, -0.10, 41), np.linspace(0, 10.0, 41), _corner_bcs(pts),
+                            {"tol": 1e-7, "line_search_flag": True}, stress_fn=lambda sg: sg[0, 2, 2])
+    gold = GOLD["case2_szz"][:40]
+    rel = np.abs(s - gold) / np.abs(gold)
+    assert rel.max() < 1e-10, rel
+
+
+def _batch(rng, n, table=O.FCC12, plastic=True):
+    N = table.shape[0]
+    ug = 3e-3 * rng.normal(size=(n, 3, 3))
+    fpi = np.eye(3) + (5e-3 * rng.normal(size=(n, 3, 3)) if plastic else 0.0)
+    g = rng.uniform(40.0, 160.0, size=(n, N))
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    R = O.rot_mat(q)
+    P = O.schmid_tensors(table)
+    Pr = np.einsum("gia,gjb,kab->gkij", R, R, P)
+    Cr = O.rotate_rank4(R, O.cubic_stiffness(168.4e3, 121.4e3, 75.4e3))
+    return lambda F: O.GPBatch(F, fpi, g, Pr, Cr, 0.05 * np.ones(n), 1e-3, 0.1), np.eye(3) + ug
+
+
+def test_tangent_matches_central_differences():
+    rng = np.random.default_rng(1)
+    mk, F = _batch(rng, 6)
+    b = mk(F)
+    S, _, ok = O.local_newton(b, 1e-10, 5)
+    assert ok.all()
+    D = O.tangent(b, S).reshape(-1, 9, 9)
+    h = 1e-6
+    Dfd = np.empty_like(D)
+    for kl in range(9):
+        E = np.zeros(9)
+        E[kl] = h
+        Fp, Fm = F + E.reshape(3, 3), F - E.reshape(3, 3)
+        bp, bm = mk(Fp), mk(Fm)
+        Sp = O.local_newton(bp, 1e-10, 5)[0]
+        Sm = O.local_newton(bm, 1e-10, 5)[0]
+        Dfd[:, :, kl] = ((O.first_pk_stress(bp, Sp) - O.first_pk_stress(bm, Sm)) / (2 * h)).reshape(-1, 9)
+    rel = np.abs(D - Dfd).max() / np.abs(D).max()
+    assert rel < 1e-5, rel
+
+
+def test_local_newton_zero_strain_gives_zero_stress():
+    rng = np.random.default_rng(2)
+    mk, F = _batch(rng, 4, plastic=False)
+    b = mk(np.broadcast_to(np.eye(3), (4, 3, 3)).copy())
+    S, its, ok = O.local_newton(b, 1e-8, 5)
+    assert ok.all() and (its == 0).all() and np.abs(S).max() == 0.0
+
+
+def test_bicgstab_restatement_solves_nonsymmetric_system():
+    rng = np.random.default_rng(3)
+    n = 60
+    A = sp.random(n, n, density=0.1, random_state=4) + sp.eye(n) * 4.0
+    A = A.tocsr()
+    b = rng.normal(size=n)
+    diag = A.diagonal()
+    x, k = O.bicgstab(A, b, np.zeros(n), lambda v: v / diag)
+    assert k > 0
+    x_ref = spla.spsolve(A.tocsc(), b)
+    assert np.abs(x - x_ref).max() / np.abs(x_ref).max() < 1e-8
+
+
+def test_euler_zyx_matches_scipy(pkg):
+    from scipy.spatial.transform import Rotation
+    ang = np.random.default_rng(5).uniform(-180, 180, size=(7, 3))
+    R = pkg.material.euler_zyx_deg(ang)
+    R_ref = Rotation.from_euler("zyx", ang, degrees=True).as_matrix()
+    assert np.abs(R - R_ref).max() < 1e-14
+
+
+def test_q_matrix_semantics():
+    q = O.q_matrix(12, 1.4, coplanar=True)
+    assert q[0, 0] == 1.0 and q[0, 2] == 1.0 and q[0, 3] == 1.4 and q[5, 3] == 1.0 and q[5, 6] == 1.4
+    assert (O.q_matrix(12, 1.4, coplanar=False) == 1.4).all()
+
+
+def test_slip_tables_agree_with_package(pkg):
+    for name, tab in (("fcc12", O.FCC12), ("bcc12", O.BCC12), ("bcc24", O.BCC24)):
+        assert np.array_equal(np.asarray(pkg.material.SLIP_SYSTEMS[name], float), tab)
+
+
+def test_box_mesh_matches_package(pkg):
+    pts, cells = O.box_mesh(3, 2, 4, 1.0, 2.0, 3.0)
+    m = pkg.box_mesh(3, 2, 4, 1.0, 2.0, 3.0)
+    assert np.array_equal(pts, m.points) and np.array_equal(cells, m.cells)
+    sg, jxw = O.shape_grads_and_jxw(pts, cells)
+    sg2, jxw2 = pkg.mesh.shape_grads_jxw(m)
+    assert np.abs(sg - sg2).max() < 1e-14 and np.abs(jxw - jxw2).max() < 1e-15
+    assert abs(jxw.sum() - 6.0) < 1e-12
