@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""Benchmark of the plain CPFEM method on the 32^3 FCC polycrystal (64 Voronoi grains,
+304-steel-like constants, tension in 1e-3 strain steps, roller boundary conditions).
+
+One step = one load step of the reference driver loop (global Newton to convergence with
+BiCGSTAB + Jacobi, per-cell stress, committed internal variables), as
+``singlecrystal_copper/singlecrystal_copper.py:179-233`` runs it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``value`` = committed GP updates per second (Gauss points x timed
+load steps / device time), ``e2e`` = the same through the public API with host buffers.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GP updates/s; 32³ RVE s/load-step; grad÷fwd & batched÷serial time at 1e-8 err"
+UNIT = "GP updates/s"
+N_EDGE, N_GRAINS, SEED = 32, 64, 0
+STRAIN_STEP, DT = 1e-3, 0.1
+
+
+def workload_config(n=N_EDGE):
+    return {"workload": f"fcc-polycrystal-{n}^3-{N_GRAINS}grains-304steel-tension",
+            "cells": n ** 3, "gauss_points": 8 * n ** 3, "dofs": 3 * (n + 1) ** 3, "grains": N_GRAINS,
+            "strain_per_step": STRAIN_STEP, "dt_s": DT, "bcs": "rollers x=0,y=0,z=0; u_z(top)",
+            "linear_solver": "BiCGSTAB+Jacobi tol=atol=1e-10", "newton": "tol 1e-6 / rel_tol 1e-8",
+            "l2": "working set > L2 (state+tangent+CSR ~0.4 GB per step)"}
+
+
+def _pkg():
+    return importlib.import_module("jax-cpfem_gb300")
+
+
+def make_case(pkg, n=N_EDGE):
+    mesh = pkg.box_mesh(n, n, n)
+    ori, rng = pkg.mesh.voronoi_grains(mesh, N_GRAINS, SEED)
+    quat = pkg.material.random_quaternions(rng, N_GRAINS)
+    return mesh, quat, ori
+
+
+def roller_lists(pkg, mesh, disp):
+    p = mesh.points
+    fn = pkg.mesh.face_nodes
+    nodes = [fn(p, 0, 0.0), fn(p, 1, 0.0), fn(p, 2, 0.0), fn(p, 2, 1.0)]
+    return nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, disp]
+
+
+class Stepper:
+    """Device-resident load-step loop through the public API."""
+
+    def __init__(self, pkg, prob, solver_mod, mesh):
+        self.pkg, self.prob, self.solver, self.mesh = pkg, prob, solver_mod, mesh
+        self.i = 0
+        self.params = prob.internal_vars
+        import torch
+        self.sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
+
+    def step(self, host_io=None):
+        prob = self.prob
+        self.i += 1
+        prob.dt = DT
+        nodes, comps, vals = roller_lists(self.pkg, self.mesh, STRAIN_STEP * self.i)
+        prob.fes[0].set_dirichlet_lists(nodes, comps, vals)
+        prob.set_params(self.params)
+        if host_io is not None:
+            sol_h, sig_h = host_io
+            guess = sol_h.to("cuda", non_blocking=True)
+        else:
+            guess = self.sol
+        sol = self.solver.solver(prob, {"jax_solver": {}, "initial_guess": [guess.reshape(-1, 3)]})[0]
+        sig = prob.compute_avg_stress(sol, self.params)
+        self.params = prob.update_int_vars_gp(sol, self.params)
+        self.sol = sol.reshape(-1)
+        if host_io is not None:
+            sol_h.copy_(self.sol, non_blocking=True)
+            sig_h.copy_(sig.reshape(-1), non_blocking=True)
+        return sig
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+        return False
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def fp64_peak(lib, torch):
+    """Measured FP64 FMA throughput of this GPU (TFLOP/s), from cpfem_probe_dfma."""
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    flops = np.zeros(1)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = lib.cpfem_probe_dfma(4096, 8 * sms, out.data_ptr(), flops.ctypes.data,
+                                  torch.cuda.current_stream().cuda_stream)
+        e1.record()
+        torch.cuda.synchronize()
+        assert rc == 0
+        best = max(best, flops[0] / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def spmv_roofline(prob, torch, lib, reps=50):
+    """Average device time of one node-block SpMV on the final matrix (events)."""
+    x = torch.randn(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    args = (prob.num_nodes, prob.node_rowptr.data_ptr(), prob.node_cols.data_ptr(), prob.A_values.data_ptr(),
+            x.data_ptr(), y.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    for _ in range(3):
+        lib.cpfem_spmv(*args)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        lib.cpfem_spmv(*args)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / reps
+    nnz, nb, ndof = prob.nnz, prob.num_blocks, prob.num_total_dofs_all_vars
+    alg_bytes = 8 * nnz + 4 * nb + 4 * (prob.num_nodes + 1) + 8 * ndof + 8 * ndof
+    return t, alg_bytes, 2.0 * nnz
+
+
+def gp_flops_per_eval(num_slip, iters_mean, tangent=True):
+    """Algorithmic FP64 flops of one GP update (FMA = 2; pow, div, sqrt = 1 each):
+    per local iteration one residual (tau 12N, power/slip 6N, L_p 18N, 3x3 products and
+    strain 130) + one 6x6 Jacobian (N*(18+12+12+72)) + LU/solve (~230); the tangent adds
+    a Jacobian + LU, 6 dP/ds directions (20N+220 each) and 9 columns (~220 each)."""
+    N = num_slip
+    residual = 36 * N + 130
+    jac = 114 * N
+    lu = 230
+    per_iter = residual + jac + lu
+    setup = 120 + residual
+    tan = (jac + lu + 6 * (20 * N + 220) + 9 * 220) if tangent else 0
+    return setup + iters_mean * per_iter + tan + 60
+
+
+def cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters, budget_s=20.0):
+    """Oracle (numpy/scipy, 1 host thread) on a bounded sample of the workload, scaled
+    to s per load step: constitutive+tangent+assembly on a subset of cells x passes,
+    BiCGSTAB iterations on a matrix with the full 32^3 pattern."""
+    from oracle import cpfem_oracle as O
+    import scipy.sparse as sp
+    spec = pkg.material.BENCH_STEEL
+    E = mesh.cells.shape[0]
+    sub = 2048
+    cells = mesh.cells[:sub]
+    used, inv = np.unique(cells, return_inverse=True)
+    orc = O.OracleProblem(mesh.points[used], inv.reshape(cells.shape), O.FCC12, spec.C11, spec.C12, spec.C44,
+                          quat, ori[:sub], gss_initial=spec.gss_initial, h=spec.h, t_sat=spec.t_sat,
+                          gss_a=spec.gss_a, xm=spec.xm, r=spec.r, coplanar=True)
+    orc.dt = DT
+    u = np.zeros(orc.ndof)
+    u[2::3] = STRAIN_STEP * orc.points[:, 2]
+    t0 = time.perf_counter()
+    orc.newton_update(u)
+    t_asm = (time.perf_counter() - t0) * E / sub
+    # Krylov: iterations of the restated BiCGSTAB on the full pattern
+    dof = (3 * mesh.cells[:, :, None] + np.arange(3)).reshape(E, 24)
+    I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
+    J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
+    ndof = 3 * mesh.points.shape[0]
+    A = sp.csr_array((np.random.default_rng(0).random(I.size), (I, J)), shape=(ndof, ndof))
+    A.sum_duplicates()
+    A = A + sp.eye(ndof) * 100.0
+    b = np.ones(ndof)
+    d = A.diagonal()
+    it = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s / 2 and it < 200:
+        O.bicgstab(A, b, np.zeros(ndof), lambda v: v / d, tol=0.0, atol=0.0, maxiter=5)
+        it += 5
+    t_it = (time.perf_counter() - t0) / it
+    t_step = newton_passes * t_asm + krylov_iters * t_it
+    return {"value": 8 * E / t_step, "unit": UNIT, "cores": 1, "kind": "port",
+            "s_per_load_step": t_step,
+            "sample": (f"oracle newton_update on {sub} of {E} cells (x{E // sub}) timed {t_asm:.2f}s/pass x "
+                       f"{newton_passes} passes + {it} BiCGSTAB iterations on the full {ndof}-dof pattern "
+                       f"({t_it * 1e3:.1f} ms/it) x {krylov_iters} iterations; counts from this GPU run")}
+
+
+def run_reference(args):
+    """The reference's CPU path is JAX; JAX is not installed, so the reference arm times
+    the CPU restatement of the same algorithm (the oracle port) on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pkg = _pkg()
+    mesh, quat, ori = make_case(pkg)
+    # counts of this workload's load steps measured on the GPU path (same algorithm)
+    newton_passes, krylov_iters = REF_COUNTS["passes_per_step"], REF_COUNTS["krylov_iters_per_step"]
+    vals = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters, budget_s=8.0)
+        if k >= args.warmup:
+            vals.append(r)
+    v = float(np.median([r["value"] for r in vals]))
+    cb = dict(vals[-1])
+    cb["value"] = v
+    cb["cores"] = 1
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 8 * N_EDGE ** 3 / v * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": workload_config(), "impl": "reference",
+           "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "reference JAX/JAX-FEM path not installable offline; oracle port of the same algorithm"}
+    print(json.dumps(out))
+
+
+# Per-load-step counts of this workload on the GPU path (tension steps 1..20):
+# constitutive+tangent passes (Newton iterations + 1) and BiCGSTAB iterations summed over
+# the step's linear solves.  Refreshed from the GPU bench run.
+REF_COUNTS = {"passes_per_step": 4, "krylov_iters_per_step": 1500}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--edge", type=int, default=N_EDGE, help="cube edge in cells (32 = the benchmark)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    pkg = _pkg()
+    problem_mod, solver_mod = pkg.load()
+    from importlib import import_module
+    lib = import_module("jax-cpfem_gb300._capi").load()
+
+    n = args.edge
+    mesh, quat, ori = make_case(pkg, n)
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=pkg.material.BENCH_STEEL)
+    st = Stepper(pkg, prob, solver_mod, mesh)
+    for _ in range(args.warmup):
+        st.step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    prob.timing = True
+    prob.stats["krylov_iters"] = []
+    passes0 = prob.stats["gp_passes"]
+    newton = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            st.step()
+            newton.append(prob.stats["newton_iters"])
+        e1.record()
+        torch.cuda.synchronize()
+    barrier()
+    t = e0.elapsed_time(e1) * 1e-3
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    regions = prob.timer_ms()
+    prob.timing = False
+    krylov = list(prob.stats["krylov_iters"])
+    passes = prob.stats["gp_passes"] - passes0
+    G = prob.num_gp
+    value = world * G * args.steps / t
+    clocks = clk.summary()
+
+    # end-to-end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        sol_h = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64).pin_memory()
+        sol_h.copy_(st.sol.cpu())
+        sig_h = torch.zeros(prob.num_cells * 9, dtype=torch.float64).pin_memory()
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            st.step(host_io=(sol_h, sig_h))
+        torch.cuda.synchronize()
+        te = time.perf_counter() - w0
+        e2e = {"value": world * G * args.steps / te, "unit": UNIT,
+               "h2d_bytes_per_step": int(sol_h.numel() * 8), "d2h_bytes_per_step": int((sol_h.numel() + sig_h.numel()) * 8),
+               "s_per_load_step": te / args.steps}
+
+    # roofline of the dominant kernel(s)
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    fp64 = fp64_peak(lib, torch)
+    t_spmv, spmv_bytes, spmv_flops = spmv_roofline(prob, torch, lib)
+    its_t = prob.stats.get("local_iters_mean", 6.0)
+    gp_n, gp_ms = regions.get("gp_eval_tangent", (0, 0.0))
+    gp_t = gp_ms * 1e-3 / max(gp_n, 1)
+    gp_flops = G * gp_flops_per_eval(prob.num_slip, its_t)
+    kr_n, kr_ms = regions.get("bicgstab", (0, 0.0))
+    gp_share = (gp_ms + regions.get("gp_eval_post", (0, 0))[1]) / (t * 1e3)
+    kr_share = kr_ms / (t * 1e3)
+    spmv_roof = {"bound": "hbm", "achieved": spmv_bytes / t_spmv / 1e9, "peak": hbm, "unit": "GB/s",
+                 "frac": (spmv_bytes / t_spmv / 1e9) / hbm if hbm else None, "traffic": None,
+                 "kernel": "k_spmv (node-block CSR)", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                 "fp64_frac": (spmv_flops / t_spmv / 1e12) / fp64}
+    gp_roof = {"bound": "fp64", "achieved": gp_flops / gp_t / 1e12 if gp_t else None, "peak": fp64,
+               "unit": "TFLOP/s", "frac": (gp_flops / gp_t / 1e12) / fp64 if gp_t else None, "traffic": None,
+               "kernel": "k_gp_eval<12,tangent>", "peak_source": "cpfem_probe_dfma (of measured)"}
+    dominant = spmv_roof if kr_share >= gp_share else gp_roof
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        kps = sum(max(k, 0) for k in krylov) / args.steps
+        cpu = cpu_baseline_sample(pkg, mesh, quat, ori, passes / args.steps, kps)
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": dict(workload_config(n), parallelism="replicas" if world > 1 else "single-gpu"),
+           "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
+           "roofline": dominant, "roofline_kernels": {"spmv": spmv_roof, "gp_eval": gp_roof},
+           "cpu_baseline": cpu,
+           "regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
+           "newton_iters_per_step": newton, "krylov_iters": krylov, "gp_passes": passes,
+           "gpu_launches": None}
+    out["gpu_launches"] = count_launches(regions, krylov)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def count_launches(regions, krylov):
+    """Our kernels launched in the timed region: one per gp_eval / elem_assemble call,
+    5 per BiCGSTAB iteration + precond + init per solve, plus dots, BC and axpy calls."""
+    n = 0
+    for k, (cnt, _) in regions.items():
+        if k.startswith("gp_eval") or k == "elem_assemble":
+            n += cnt
+    n += sum(5 * max(k, 0) + 2 for k in krylov)
+    return n
+
+
+if __name__ == "__main__":
+    main()

@@ -200,6 +200,15 @@ int cpfem_bicgstab(int32_t num_nodes, const int32_t* node_rowptr, const int32_t*
                    int32_t transpose, double tol, double atol, int32_t maxiter,
                    int32_t check_every, void* workspace, int32_t* info, void* stream);
 
+/*
+ * FP64 FMA throughput probe (measurement only, not on the solve path): launches `blocks`
+ * blocks of 256 threads, each running 8 independent FMA chains of `iters` steps; *flops
+ * receives the FP64 flop count of the launch (an FMA counts 2).  Time it with events on
+ * `stream`.  No reference counterpart: it supplies the roofline denominator of the
+ * constitutive kernel, which the measured peaks do not include.
+ */
+int cpfem_probe_dfma(int64_t iters, int32_t blocks, double* out, double* flops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcpfem_gb300.so")
 
-CUDA_SOURCES = ["assembly.cu", "krylov.cu"]
+CUDA_SOURCES = ["assembly.cu", "krylov.cu", "probe.cu"]
 CXX_SOURCES = ["pattern.cpp"]
 HEADERS = ["cpfem_common.cuh", "gp_update.cuh", "reduce.cuh"]
 

@@ -8,6 +8,9 @@
 
 #include "../../include/cpfem_gb300.h"
 
+// Small math helpers are host+device so the same code can be checked on the host.
+#define CPFEM_HD __host__ __device__ __forceinline__
+
 namespace cpfem {
 
 // Thread-local text behind cpfem_last_error().
@@ -56,7 +59,7 @@ constexpr int kVecBlocks = 2 * 152;
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // ---- 3x3 helpers (row-major) -------------------------------------------------------
-__device__ __forceinline__ void mm3(const double* A, const double* B, double* C) {
+CPFEM_HD void mm3(const double* A, const double* B, double* C) {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -65,7 +68,7 @@ __device__ __forceinline__ void mm3(const double* A, const double* B, double* C)
 }
 
 // C = A * B^T
-__device__ __forceinline__ void mm3_bt(const double* A, const double* B, double* C) {
+CPFEM_HD void mm3_bt(const double* A, const double* B, double* C) {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -74,7 +77,7 @@ __device__ __forceinline__ void mm3_bt(const double* A, const double* B, double*
 }
 
 // C = A^T * B
-__device__ __forceinline__ void mm3_at(const double* A, const double* B, double* C) {
+CPFEM_HD void mm3_at(const double* A, const double* B, double* C) {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -82,12 +85,12 @@ __device__ __forceinline__ void mm3_at(const double* A, const double* B, double*
       C[3 * i + j] = fma(A[0 + i], B[0 + j], fma(A[3 + i], B[3 + j], A[6 + i] * B[6 + j]));
 }
 
-__device__ __forceinline__ double det3(const double* A) {
+CPFEM_HD double det3(const double* A) {
   return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
          A[2] * (A[3] * A[7] - A[4] * A[6]);
 }
 
-__device__ __forceinline__ void inv3(const double* A, double* Ai) {
+CPFEM_HD void inv3(const double* A, double* Ai) {
   const double c00 = A[4] * A[8] - A[5] * A[7];
   const double c01 = A[5] * A[6] - A[3] * A[8];
   const double c02 = A[3] * A[7] - A[4] * A[6];
@@ -106,7 +109,7 @@ __device__ __forceinline__ void inv3(const double* A, double* Ai) {
 
 // Cubic stiffness applied to a symmetric tensor in 6-component form
 // (11,22,33,23,13,12), tensor components (not engineering shears).
-__device__ __forceinline__ void cubic_apply(const MatDev& m, const double* e, double* t) {
+CPFEM_HD void cubic_apply(const MatDev& m, const double* e, double* t) {
   t[0] = fma(m.C11, e[0], m.C12 * (e[1] + e[2]));
   t[1] = fma(m.C11, e[1], m.C12 * (e[0] + e[2]));
   t[2] = fma(m.C11, e[2], m.C12 * (e[0] + e[1]));
@@ -119,7 +122,7 @@ __device__ __forceinline__ void cubic_apply(const MatDev& m, const double* e, do
 // In-register LU with partial pivoting of an n x n matrix; all indices are static so
 // the matrix stays in registers.  Row swaps are done with predicated exchanges.
 template <int n>
-__device__ __forceinline__ void lu_factor(double* A, int* perm, double* dinv) {
+CPFEM_HD void lu_factor(double* A, int* perm, double* dinv) {
 #pragma unroll
   for (int i = 0; i < n; ++i) perm[i] = i;
 #pragma unroll
@@ -159,7 +162,7 @@ __device__ __forceinline__ void lu_factor(double* A, int* perm, double* dinv) {
 
 // Solve with the factors of lu_factor; b is overwritten by x.
 template <int n>
-__device__ __forceinline__ void lu_solve(const double* LU, const int* perm, const double* dinv, double* b) {
+CPFEM_HD void lu_solve(const double* LU, const int* perm, const double* dinv, double* b) {
   double y[n];
 #pragma unroll
   for (int i = 0; i < n; ++i) {

@@ -29,7 +29,7 @@ struct GPSolve {
 
 // Residual at s.  Ct = (F Fp^-1_old R)^T (F Fp^-1_old R) (symmetric, full 3x3).
 template <int NS>
-__device__ __forceinline__ void cp_residual(const MatDev& m, const double* Ct, const double* ig,
+CPFEM_HD void cp_residual(const MatDev& m, const double* Ct, const double* ig,
                                             double cdt, double pexp, const double* s, double* r,
                                             double& rn, double* dg, double* kk, double* B,
                                             double* M) {
@@ -73,7 +73,7 @@ __device__ __forceinline__ void cp_residual(const MatDev& m, const double* Ct, c
 
 // J = dr/ds = I + sum_a kk_a (C : sym(M^T d_a (x) n_a)) (x) pv_a
 template <int NS>
-__device__ __forceinline__ void cp_jacobian(const MatDev& m, const double* kk, const double* M,
+CPFEM_HD void cp_jacobian(const MatDev& m, const double* kk, const double* M,
                                             double* J) {
 #pragma unroll
   for (int i = 0; i < 36; ++i) J[i] = (i % 7 == 0) ? 1.0 : 0.0;
@@ -106,7 +106,7 @@ __device__ __forceinline__ void cp_jacobian(const MatDev& m, const double* kk, c
 // trial residuals at s + relax ds, relax = 1, 1/2, ..., until the norm drops below the
 // current one or max_sub_step trials were made; the last trial is taken.
 template <int NS>
-__device__ __forceinline__ void cp_local_newton(const MatDev& m, const double* Ct, const double* ig,
+CPFEM_HD void cp_local_newton(const MatDev& m, const double* Ct, const double* ig,
                                                 double cdt, double pexp, GPSolve<NS>& st) {
   double r[6];
 #pragma unroll
@@ -149,7 +149,7 @@ __device__ __forceinline__ void cp_local_newton(const MatDev& m, const double* C
 // The tangent column for F_kl is handed to store_col(kl, col[9]) as soon as it is
 // known, so the 81 entries never need to be live at once.
 template <int NS, bool WITH_TANGENT, class StoreCol>
-__device__ __forceinline__ void cp_outputs(const MatDev& m, const double* F, const double* G /*Fp^-1_old R*/,
+CPFEM_HD void cp_outputs(const MatDev& m, const double* F, const double* G /*Fp^-1_old R*/,
                                            const GPSolve<NS>& st, double* H, double* P,
                                            StoreCol store_col) {
   double S[9], W[9], Y[9];
@@ -246,7 +246,7 @@ __device__ __forceinline__ void cp_outputs(const MatDev& m, const double* F, con
 // Explicit hardening and slip update after the local solve (models_copper.py:176-187;
 // per-GP parameters as in crystal_plasticity_OR_design/models_sens_rot.py:168-193).
 template <int NS>
-__device__ __forceinline__ void cp_hardening(const MatDev& m, const double* g, const double* dg,
+CPFEM_HD void cp_hardening(const MatDev& m, const double* g, const double* dg,
                                              double h, double t_sat, double gss_a, double rq,
                                              double* g_new) {
   double tmp[NS];

@@ -61,7 +61,7 @@ class MaterialSpec:
     per_gp_params: bool = False
     local_tol: float = 1e-8
     max_sub_step: int = 5
-    max_iter: int = 100
+    max_iter: int = 300
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)

@@ -199,6 +199,8 @@ class CrystalPlasticity:
         self._bufs = {}
         self._post_cache = None
         self.stats = {"gp_passes": 0, "krylov_iters": [], "local_iters_max": 0}
+        self.timing = False
+        self.timers = {}
         self.custom_init(*additional_info)
 
     # ------------------------------------------------------------------ set-up
@@ -355,8 +357,26 @@ class CrystalPlasticity:
     def _state(self):
         return (self.fpi, self.g, self.slip, self.rot_table, self.rot_idx, self.param_table, self.param_idx)
 
-    def _run_gp(self, args):
-        _capi.check(self.lib.cpfem_gp_eval(self.mat_c, args, _stream()))
+    def region(self, name):
+        """Context manager timing the enclosed library calls with CUDA events."""
+        return _Region(self, name)
+
+    def timer_ms(self, reset=True):
+        """{region: (launches, total ms)} of the recorded regions (synchronises)."""
+        torch.cuda.synchronize()
+        out = {k: (len(v), sum(a.elapsed_time(b) for a, b in v)) for k, v in self.timers.items()}
+        acc = self._bufs.get("iters_acc")
+        if acc is not None and float(acc[1]) > 0:
+            self.stats["local_iters_mean"] = float(acc[0] / acc[1])
+        if reset:
+            self.timers = {}
+            if acc is not None:
+                acc.zero_()
+        return out
+
+    def _run_gp(self, args, name="gp_eval"):
+        with self.region(name):
+            _capi.check(self.lib.cpfem_gp_eval(self.mat_c, args, _stream()))
         self.stats["gp_passes"] += 1
 
     def _check_status(self, status):
@@ -380,13 +400,20 @@ class CrystalPlasticity:
             values = self._buf("values", (self.nnz,))
             values.zero_()
             dw = self._buf("tangent_w", (81, G))
-        args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True)
-        self._run_gp(args)
+        its = self._buf("iters", (G,), torch.int32) if self.timing else None
+        args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
+                             iters=its)
+        self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
+        if its is not None and need_tangent:
+            acc = self._bufs.setdefault("iters_acc", torch.zeros(2, dtype=torch.float64, device=self.device))
+            acc[0] += its.sum()
+            acc[1] += G
         fe = self.fes[0]
-        _capi.check(self.lib.cpfem_elem_assemble(self.num_cells, _dev_ptr(fe.cells), _dev_ptr(fe.shape_grads),
+        with self.region("elem_assemble"):
+            _capi.check(self.lib.cpfem_elem_assemble(self.num_cells, _dev_ptr(fe.cells), _dev_ptr(fe.shape_grads),
                                                  _dev_ptr(self.node_rowptr), _dev_ptr(self.elem_pos),
-                                                 _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res), _dev_ptr(values),
-                                                 _stream()))
+                                                     _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res), _dev_ptr(values),
+                                                     _stream()))
         return res, values, status
 
     def apply_dirichlet(self, res, u, values=None):
@@ -418,7 +445,7 @@ class CrystalPlasticity:
             return self.gp_map(u_grad, *ivars)[0]
         return tensor_map
 
-    def gp_map(self, u_grad, *ivars, need_tangent=True, dt=None):
+    def gp_map(self, u_grad, *ivars, need_tangent=True, dt=None, check=True):
         """Batched constitutive update at arbitrary GPs.  Returns
         (P (...,3,3), dP/dF (...,3,3,3,3) or None, new state list, local iterations)."""
         u_grad = torch.as_tensor(u_grad, dtype=torch.float64, device=self.device)
@@ -450,7 +477,8 @@ class CrystalPlasticity:
                              u_grad=ug, num_gp=n, pk1=P, tangent=D, fpi_new=fn, g_new=gn, slip_new=sn,
                              iters=its, status=status)
         self._run_gp(args)
-        self._check_status(status)
+        if check:
+            self._check_status(status)
         out_P = P.t().reshape(*lead, 3, 3)
         out_D = D.t().reshape(*lead, 3, 3, 3, 3) if D is not None else None
         state = [fn.t().reshape(*lead, 3, 3), gn.t().reshape(*lead, N), sn.t().reshape(*lead, N)]
@@ -477,7 +505,7 @@ class CrystalPlasticity:
         status.zero_()
         args = self._gp_args(self._state(), self.dt, u=u, stress=sw, fpi_new=fn, g_new=gn, slip_new=sn,
                              status=status, weight_jxw=True)
-        self._run_gp(args)
+        self._run_gp(args, "gp_eval_post")
         sig = torch.empty((self.num_cells, 3, 3), dtype=torch.float64, device=self.device)
         _capi.check(self.lib.cpfem_cell_average(self.num_cells, _dev_ptr(self.fes[0].JxW), _dev_ptr(sw),
                                                 _dev_ptr(sig), _stream()))
@@ -503,6 +531,26 @@ class CrystalPlasticity:
         print(f"Fp = \n{Fp.cpu().numpy()}")
         print(f"slip_resistance index 0 = {float(g0)}, max slip_resistance = {float(params[1].max())}")
         return Fp[2, 2], g0, params[2][0, 0, 0]
+
+
+class _Region:
+    """CUDA-event bracket of one library call on the current stream (when enabled)."""
+
+    def __init__(self, problem, name):
+        self.p, self.name = problem, name
+
+    def __enter__(self):
+        if self.p.timing:
+            self.e0 = torch.cuda.Event(enable_timing=True)
+            self.e0.record()
+        return self
+
+    def __exit__(self, *exc):
+        if self.p.timing:
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record()
+            self.p.timers.setdefault(self.name, []).append((self.e0, e1))
+        return False
 
 
 def _flat(sol_list, device):

@@ -44,10 +44,11 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
-    _capi.check(lib.cpfem_bicgstab(problem.num_nodes, _dev_ptr(problem.node_rowptr), _dev_ptr(problem.node_cols),
-                                   _dev_ptr(problem.node_tpos), _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
-                                   int(precond), 1 if A.transposed else 0, float(tol), float(atol), int(maxiter),
-                                   int(check_every), _dev_ptr(ws), info.ctypes.data, _stream()))
+    with problem.region("bicgstab"):
+        _capi.check(lib.cpfem_bicgstab(problem.num_nodes, _dev_ptr(problem.node_rowptr), _dev_ptr(problem.node_cols),
+                                       _dev_ptr(problem.node_tpos), _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
+                                       int(precond), 1 if A.transposed else 0, float(tol), float(atol),
+                                       int(maxiter), int(check_every), _dev_ptr(ws), info.ctypes.data, _stream()))
     return x, int(info[0]), bool(info[1])
 
 

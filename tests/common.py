@@ -33,11 +33,15 @@ def gpu_problem(pkg, problem_mod, spec, mesh, quat, ori, bcs=()):
     return p
 
 
-def random_gp_inputs(rng, n, N, strain=2e-3, plastic=True):
-    """Random per-GP inputs: F near I, Fp^-1 near I (det ~ 1), g around 100, rotations."""
-    ug = strain * rng.normal(size=(n, 3, 3))
-    fpi = np.eye(3) + (5e-3 * rng.normal(size=(n, 3, 3)) if plastic else 0.0)
-    g = rng.uniform(40.0, 160.0, size=(n, N))
+def random_gp_inputs(rng, n, N, strain=1e-3, plastic=True):
+    """Random per-GP inputs of one load increment: tension-like F near I with noise,
+    a mildly deformed Fp^-1, slip resistances around the flow stress, rotations."""
+    ug = np.zeros((n, 3, 3))
+    ug[:, 2, 2] = strain
+    ug[:, 0, 0] = ug[:, 1, 1] = -0.3 * strain
+    ug += 0.3 * strain * rng.normal(size=(n, 3, 3))
+    fpi = np.eye(3) + (2e-4 * rng.normal(size=(n, 3, 3)) if plastic else np.zeros((n, 3, 3)))
+    g = rng.uniform(60.0, 160.0, size=(n, N))
     slip = rng.normal(scale=1e-3, size=(n, N))
     q = rng.normal(size=(n, 4))
     q /= np.linalg.norm(q, axis=1)[:, None]

@@ -75,7 +75,10 @@ def test_assembly_residual_and_csr_match_oracle(pkg, gpu):
     prob = gpu_problem(pkg, problem_mod, spec, mesh, quat, ori)
     orc = oracle_problem(spec, mesh, quat, ori)
     prob.dt = orc.dt = 0.1
-    u = 2e-3 * np.random.default_rng(5).normal(size=3 * mesh.points.shape[0])
+    rng = np.random.default_rng(5)
+    u = 1e-4 * rng.normal(size=(mesh.points.shape[0], 3))
+    u[:, 2] += 1e-3 * mesh.points[:, 2]
+    u = u.reshape(-1)
     res_o, A_o = orc.newton_update(u)
     res = prob.newton_update([torch.tensor(u, device="cuda").reshape(-1, 3)])[0].reshape(-1)
     A = problem_mod.DeviceCSR(prob, prob.A_values).to_scipy()
