@@ -93,8 +93,10 @@ class Stepper:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms.  Started before the
+    warm-up (its start-up stalls the driver for a moment), and summarised over the samples
+    whose timestamps fall inside the timed region."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -102,8 +104,9 @@ class ClockSampler:
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.dev = device_index
         self.proc = None
+        self.window = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -112,29 +115,42 @@ class ClockSampler:
             self.proc = None
         return self
 
-    def __exit__(self, *exc):
+    def stop(self):
         if self.proc is not None:
             self.proc.terminate()
             self.proc.wait(timeout=10)
-        return False
+            self.proc = None
 
-    def summary(self):
+    def summary(self, t0, t1):
+        import datetime
+        self.stop()
         self.f.flush()
         self.f.seek(0)
-        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        rows = [[c.strip() for c in r.split(",")] for r in self.f.read().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
-        if not rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
-        smax = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        sel = []
+        for r in rows:
+            try:
+                ts = datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except (ValueError, IndexError):
+                continue
+            if t0 - 0.25 <= ts <= t1 + 0.25:
+                sel.append(r)
+        if not sel:
+            sel = rows[-3:]
+        if not sel:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        num = lambda v: float(v) if v.replace(".", "", 1).isdigit() else None
+        sm = [num(r[2]) for r in sel if len(r) > 3 and num(r[2]) is not None]
+        smax = [num(r[3]) for r in sel if len(r) > 3 and num(r[3]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
-        for r in rows:
+        for r in sel:
             for k, nm in enumerate(names):
-                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                if len(r) > 6 + k and r[6 + k].lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+                "reasons": sorted(reasons), "samples": len(sel)}
 
 
 def measured_peaks():
@@ -154,7 +170,7 @@ def fp64_peak(lib, torch):
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        rc = lib.cpfem_probe_dfma(4096, 8 * sms, out.data_ptr(), flops.ctypes.data,
+        rc = lib.cpfem_probe_dfma(1024, 8 * sms, out.data_ptr(), flops.ctypes.data,
                                   torch.cuda.current_stream().cuda_stream)
         e1.record()
         torch.cuda.synchronize()
@@ -164,11 +180,11 @@ def fp64_peak(lib, torch):
 
 
 def spmv_roofline(prob, torch, lib, reps=50):
-    """Average device time of one node-block SpMV on the final matrix (events)."""
+    """Average device time of one sliced-ELL SpMV on the final matrix (events)."""
     x = torch.randn(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
-    args = (prob.num_nodes, prob.node_rowptr.data_ptr(), prob.node_cols.data_ptr(), prob.A_values.data_ptr(),
-            x.data_ptr(), y.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    args = (prob.sell, prob.A_values.data_ptr(), x.data_ptr(), y.data_ptr(), 0,
+            torch.cuda.current_stream().cuda_stream)
     for _ in range(3):
         lib.cpfem_spmv(*args)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -179,7 +195,8 @@ def spmv_roofline(prob, torch, lib, reps=50):
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) * 1e-3 / reps
     nnz, nb, ndof = prob.nnz, prob.num_blocks, prob.num_total_dofs_all_vars
-    alg_bytes = 8 * nnz + 4 * nb + 4 * (prob.num_nodes + 1) + 8 * ndof + 8 * ndof
+    # values + one column index per 3x3 block + x once + y (algorithmic, no padding)
+    alg_bytes = 8 * nnz + 4 * nb + 8 * ndof + 8 * ndof
     return t, alg_bytes, 2.0 * nnz
 
 
@@ -277,6 +294,86 @@ def run_reference(args):
 REF_COUNTS = {"passes_per_step": 4, "krylov_iters_per_step": 1500}
 
 
+def run_adjoint_config(args, pkg, problem_mod, torch):
+    """configs[3]: gradient of the sigma_zz-curve misfit on the 32^3 / 64-grain RVE with
+    respect to (h0, g0, gs, a, m) and the 64x3 Euler angles; backward / forward time."""
+    from importlib import import_module
+    adjoint = import_module("jax-cpfem_gb300.adjoint")
+    n = args.edge
+    mesh, quat, ori = make_case(pkg, n)
+    spec = pkg.material.BENCH_STEEL
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=spec)
+    nsteps = args.load_steps or 20
+
+    def bc_fn(i, d):
+        nodes, comps, vals = roller_lists(pkg, mesh, d)
+        return nodes, comps, vals
+
+    disps = STRAIN_STEP * np.arange(nsteps + 1)
+    ts = DT * np.arange(nsteps + 1)
+    h = adjoint.LoadHistory(prob, disps, ts, bc_fn, quat)
+    theta = np.array([spec.h, spec.gss_initial, spec.t_sat, spec.gss_a, spec.xm])
+    euler = np.zeros((N_GRAINS, 3))
+    # synthetic target: h0, g0, gs scaled by 1.1 under the same seed
+    target = h.forward(theta * np.array([1.1, 1.1, 1.1, 1.0, 1.0]), euler, checkpoint=False).cpu().numpy()[:, 2, 2]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = h.forward(theta, euler).cpu().numpy()[:, 2, 2]
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    sbar = np.zeros((nsteps, 3, 3))
+    sbar[:, 2, 2] = 2.0 * (s - target) / nsteps
+    t0 = time.perf_counter()
+    tb, eb = h.backward(sbar)
+    torch.cuda.synchronize()
+    t_bwd = time.perf_counter() - t0
+    out = {"metric": METRIC, "value": t_bwd / t_fwd, "unit": "backward/forward time", "higher_is_better": False,
+           "n_gpus": 1, "steps": nsteps, "warmup": 0, "dtype": "f64", "data": "synthetic",
+           "config": dict(workload_config(n), workload=f"adjoint-fcc-polycrystal-{n}^3-{N_GRAINS}grains",
+                          load_steps=nsteps, params="h0,g0,gs,a,m + 64x3 Euler angles"),
+           "forward_s": t_fwd, "backward_s": t_bwd, "gradient_over_forward": (t_fwd + t_bwd) / t_fwd,
+           "objective": float(((s - target) ** 2).mean()), "theta_grad": tb.tolist(),
+           "euler_grad_norm": float(np.linalg.norm(eb)), "adjoint_krylov_iters": h.krylov_iters}
+    if args.fd_check:
+        rng = np.random.default_rng(1)
+        d_t = rng.normal(size=5) * theta * 1e-6
+        d_e = rng.normal(size=euler.shape) * 1e-4
+        f = lambda th, eu: float(((h.forward(th, eu, checkpoint=False).cpu().numpy()[:, 2, 2] - target) ** 2).mean())
+        fd = (f(theta + d_t, euler + d_e) - f(theta - d_t, euler - d_e)) / 2.0
+        ad = float(tb @ d_t + (eb * d_e).sum())
+        out["directional_fd_check"] = {"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd)}
+    print(json.dumps(out))
+
+
+def run_batch_config(args, pkg, torch):
+    """configs[4]: 256 RVEs (edges 8..24, 8-64 grains, parameters +-20 %) batched in one
+    ragged launch per Newton stage vs the same solves one at a time."""
+    from importlib import import_module
+    batch = import_module("jax-cpfem_gb300.batch")
+    inst = batch.sample_instances(args.instances, pkg.material.BENCH_STEEL, seed=SEED)
+    nsteps = args.load_steps or 2
+    disps = STRAIN_STEP * np.arange(1, nsteps + 1)
+    b = batch.Batch(inst)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    szz = np.stack([b.step(d, DT).cpu().numpy() for d in disps], axis=1)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ref = batch.run_serial(inst, disps, DT)
+    torch.cuda.synchronize()
+    t_serial = time.perf_counter() - t0
+    rel = float(np.abs(szz - ref).max() / np.abs(ref).max())
+    gps = sum(8 * it.edge ** 3 for it in inst)
+    print(json.dumps({"metric": METRIC, "value": t_serial / t_batch, "unit": "serial/batched time",
+                      "higher_is_better": True, "n_gpus": 1, "steps": nsteps, "warmup": 0, "dtype": "f64",
+                      "data": "synthetic",
+                      "config": {"workload": f"batch-{len(inst)}-rves-edges8-24", "instances": len(inst),
+                                 "gauss_points": gps, "load_steps": nsteps},
+                      "batched_s": t_batch, "serial_s": t_serial, "max_rel_diff_vs_serial": rel,
+                      "batched_gp_updates_per_s": gps * nsteps / t_batch}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -286,6 +383,12 @@ def main():
     ap.add_argument("--edge", type=int, default=N_EDGE, help="cube edge in cells (32 = the benchmark)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"],
+                    help="c1 (default): 32^3 FCC polycrystal; c0: 10^3 copper single crystal; "
+                         "c2: 64^3 BCC24 polycrystal; c3: adjoint on c1; c4: 256-RVE batch")
+    ap.add_argument("--load-steps", type=int, default=0)
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--fd-check", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -304,10 +407,30 @@ def main():
     from importlib import import_module
     lib = import_module("jax-cpfem_gb300._capi").load()
 
+    if args.config == "c3":
+        run_adjoint_config(args, pkg, problem_mod, torch)
+        return
+    if args.config == "c4":
+        run_batch_config(args, pkg, torch)
+        return
     n = args.edge
-    mesh, quat, ori = make_case(pkg, n)
-    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=pkg.material.BENCH_STEEL)
+    spec = pkg.material.BENCH_STEEL
+    if args.config == "c0":
+        n = 10
+        mesh, quat, ori = pkg.box_mesh(n, n, n), np.array([[1.0, 0.0, 0.0, 0.0]]), np.zeros(n ** 3, dtype=np.int64)
+        spec = pkg.material.BENCH_COPPER
+    elif args.config == "c2":
+        n = 64
+        mesh = pkg.box_mesh(n, n, n)
+        ori, rng = pkg.mesh.voronoi_grains(mesh, 512, SEED)
+        quat = pkg.material.random_quaternions(rng, 512)
+        spec = pkg.material.BENCH_TANTALUM
+    else:
+        mesh, quat, ori = make_case(pkg, n)
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=spec)
     st = Stepper(pkg, prob, solver_mod, mesh)
+    clk = ClockSampler(local).start()
+    time.sleep(1.0)
     for _ in range(args.warmup):
         st.step()
     torch.cuda.synchronize()
@@ -322,14 +445,15 @@ def main():
     newton = []
     barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.steps):
-            st.step()
-            newton.append(prob.stats["newton_iters"])
-        e1.record()
-        torch.cuda.synchronize()
+    wall0 = time.time()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        st.step()
+        newton.append(prob.stats["newton_iters"])
+    e1.record()
+    torch.cuda.synchronize()
+    wall1 = time.time()
     barrier()
     t = e0.elapsed_time(e1) * 1e-3
     if world > 1:
@@ -342,7 +466,7 @@ def main():
     passes = prob.stats["gp_passes"] - passes0
     G = prob.num_gp
     value = world * G * args.steps / t
-    clocks = clk.summary()
+    clocks = clk.summary(wall0, wall1)
 
     # end-to-end through the public API with pinned host buffers
     e2e = None

@@ -37,6 +37,7 @@ enum cpfem_status {
 /* Per-Gauss-point failure bits, OR-ed into cpfem_gp_args_t.status[0]. */
 #define CPFEM_GP_MAXITER   1   /* local Newton hit max_iter (the reference has no cap) */
 #define CPFEM_GP_NONFINITE 2   /* non-finite residual or stress */
+#define CPFEM_GP_BOUNDS    4   /* an index read from the inputs was out of range (skipped) */
 
 /*
  * Material constants shared by every Gauss point of a launch.
@@ -95,6 +96,48 @@ typedef struct {
   int32_t* status;            /* [1] OR of CPFEM_GP_* bits (caller zeroes it) */
 } cpfem_gp_args_t;
 
+/*
+ * Arguments of the per-Gauss-point backward pass of one load step (cpfem_gp_vjp).
+ * The converged local state is recomputed from the checkpoint (u, Fp^-1, g of the step's
+ * start).  Output cotangents: cell_sig_bar [num_cells*9] on the JxW-averaged cell
+ * Cauchy stress, fpi_bar [9*G] and g_bar [num_slip*G] on the committed state, and in
+ * mode 2 the equilibrium adjoint mu [3*num_nodes] (Dirichlet dofs zeroed), which enters
+ * as the P cotangent -JxW grad(mu).  Mode 1 returns the F cotangent f_bar [9*G] (to be
+ * gathered into the right-hand side of the transposed solve); mode 2 returns the
+ * cotangents of the step's inputs: fpi_bar_old, g_bar_old, theta_bar [5*G] (gss_a, h,
+ * t_sat, xm, r) and rot_bar [3*G] (spatial rotation increment, R -> (I + [w]x) R).
+ */
+typedef struct {
+  int64_t num_gp;
+  int32_t num_cells;
+  int32_t mode;
+  double dt;
+  int32_t num_nodes;          /* sizes of u/mu, the rotation and parameter tables: every */
+  int32_t num_rot;            /* gathered index is checked against them, and an index out */
+  int32_t num_param;          /* of range sets CPFEM_GP_BOUNDS instead of being read */
+  int32_t pad;
+  const double* u;
+  const int32_t* cells;
+  const double* shape_grads;
+  const double* jxw;
+  const double* fpi;
+  const double* g;
+  const double* rot_table;
+  const int32_t* rot_idx;
+  const double* param_table;
+  const int32_t* param_idx;
+  const double* cell_sig_bar;
+  const double* fpi_bar;
+  const double* g_bar;
+  const double* mu;
+  double* f_bar;
+  double* fpi_bar_old;
+  double* g_bar_old;
+  double* theta_bar;
+  double* rot_bar;
+  int32_t* status;
+} cpfem_vjp_args_t;
+
 /* Library identity and error text. */
 int cpfem_abi_version(void);
 const char* cpfem_last_error(void);
@@ -102,22 +145,49 @@ const char* cpfem_last_error(void);
 /*
  * Node-block sparsity of a HEX8 mesh (host memory, host work).
  * Replaces the scipy COO->CSR conversion of crystal_plasticity_OR_design/solver.py:279-282
- * (duplicates summed, column indices sorted).  The pattern is stored per node: node a's
- * sorted neighbour list is node_cols[node_rowptr[a] .. node_rowptr[a+1]).  The scalar CSR
- * value of row 3a+i, column 3b+k sits at 9*node_rowptr[a] + i*3*deg(a) + 3*pos(b) + k,
- * which is exactly the position scipy gives it.  elem_pos[e*64 + 8*a + b] = pos of
- * cells[e,b] in the list of cells[e,a].
+ * (duplicates summed, column indices sorted).  Node a's sorted neighbour list is
+ * node_cols[node_rowptr[a] .. node_rowptr[a+1]); the scalar CSR of the reference has row
+ * 3a+i, column 3b+k.  elem_pos[e*64 + 8*a + b] = position of cells[e,b] in the list of
+ * cells[e,a].  node_tpos (may be NULL): for list entry j of node a (neighbour b), the
+ * position of a in b's list.
  */
 int cpfem_pattern_count(int32_t num_cells, const int32_t* cells, int32_t num_nodes,
                         int64_t* num_blocks);
 int cpfem_pattern_build(int32_t num_cells, const int32_t* cells, int32_t num_nodes,
                         int32_t* node_rowptr, int32_t* node_cols, uint8_t* elem_pos,
                         int32_t* node_tpos);
-/* node_tpos (may be NULL): for the block of node a at list position j (neighbour b),
- * the position of a in b's list -- what the transposed SpMV of the adjoint needs. */
 /* Scalar CSR arrays (indptr [3n+1], indices [9*num_blocks]) of the pattern, host. */
 int cpfem_pattern_expand_csr(int32_t num_nodes, const int32_t* node_rowptr,
                              const int32_t* node_cols, int32_t* indptr, int32_t* indices);
+
+/*
+ * Sliced-ELL device layout of the matrix values (groups of 32 consecutive nodes, one
+ * thread per node, coalesced across the warp).  Group g holds group_width[g] neighbour
+ * slots; slot j of node a (lane a%32 of group a/32) has neighbour cols[group_off[g] + 32j
+ * + lane] and the 3x3 block value (row i, column k) at
+ *   values[9*group_off[g] + 32*(9j + 3i + k) + lane].
+ * Padding slots point at the node itself with zero values.  tpos is the slot of this node
+ * in the neighbour's list (the transposed product of the adjoint solve); diag_slot[a] is
+ * the slot of a itself.  The values array holds 9*group_off[num_groups] doubles.
+ */
+typedef struct {
+  int32_t num_nodes;
+  int32_t num_groups;
+  const int64_t* group_off;   /* [num_groups+1] */
+  const int32_t* group_width; /* [num_groups]   */
+  const int32_t* cols;        /* [group_off[num_groups]] */
+  const int32_t* tpos;        /* [group_off[num_groups]] */
+  const int32_t* diag_slot;   /* [num_nodes] */
+} cpfem_sell_t;
+
+/* Host builders: total slots (= group_off[num_groups]), the layout, and the map from the
+ * reference's scalar CSR value order to the sliced-ELL index (map [9*num_blocks]). */
+int cpfem_sell_count(int32_t num_nodes, const int32_t* node_rowptr, int64_t* total_slots);
+int cpfem_sell_build(int32_t num_nodes, const int32_t* node_rowptr, const int32_t* node_cols,
+                     const int32_t* node_tpos, int64_t* group_off, int32_t* group_width,
+                     int32_t* cols, int32_t* tpos, int32_t* diag_slot);
+int cpfem_sell_csr_map(int32_t num_nodes, const int32_t* node_rowptr, const int64_t* group_off,
+                       int64_t* map);
 
 /*
  * Constitutive pass: local Newton on S, stress, consistent tangent, trial state.
@@ -129,15 +199,25 @@ int cpfem_pattern_expand_csr(int32_t num_nodes, const int32_t* node_rowptr,
 int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void* stream);
 
 /*
+ * Backward of the converged local Newton at every GP for one load step: the
+ * implicit-function VJP (x_bar = (dy/dx)^T y_bar - (dr/dx)^T J^-T (dy/ds)^T y_bar) of the
+ * reference's newton_solver custom_jvp (singlecrystal_copper/models_copper.py:251-259)
+ * as jax.grad transposes it inside ad_wrapper/implicit_vjp
+ * (crystal_plasticity_OR_design/solver.py:801-874).
+ */
+int cpfem_gp_vjp(const cpfem_material_t* mat, const cpfem_vjp_args_t* args, void* stream);
+
+/*
  * Element residual and tangent scatter: R_ai += sum_q P_iJ dN_a/dX_J JxW and
  * K_(ai)(bk) += sum_q dN_a/dX_J dP_iJ/dF_kL dN_b/dX_L JxW into the node-block CSR values.
- * pk1_w / tangent_w are the JxW-weighted outputs of cpfem_gp_eval.  Replaces JAX-FEM's
+ * pk1_w / tangent_w are the JxW-weighted outputs of cpfem_gp_eval; values use the
+ * sliced-ELL layout of cpfem_sell_t.  Replaces JAX-FEM's
  * newton_update (called at crystal_plasticity_OR_design/solver.py:392): the
  * 'laplace'-kernel residual, its jax.jacfwd element tangent and the COO V array.
  * residual and values are accumulated into; zero them first.
  */
 int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* shape_grads,
-                        const int32_t* node_rowptr, const uint8_t* elem_pos,
+                        const cpfem_sell_t* sell, const uint8_t* elem_pos,
                         const double* pk1_w, const double* tangent_w,
                         double* residual, double* values, void* stream);
 
@@ -149,8 +229,7 @@ int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* s
  * (solver.py:127-129), and the host wrapper keeps that entry when it builds the list.
  */
 int cpfem_apply_dirichlet(int32_t num_bc, const int32_t* bc_dofs, const double* bc_vals,
-                          const double* u, double* residual, int32_t num_nodes,
-                          const int32_t* node_rowptr, const int32_t* node_cols,
+                          const double* u, double* residual, const cpfem_sell_t* sell,
                           double* values, void* stream);
 
 /*
@@ -167,38 +246,51 @@ int cpfem_cell_average(int32_t num_cells, const double* jxw, const double* field
 /* y = y + alpha * x (the Newton update dofs + inc, solver.py:234). */
 int cpfem_axpy(int64_t n, double alpha, const double* x, double* y, void* stream);
 
+/* Per-segment dot products out[i] = x[off[i]:off[i+1]] . y[off[i]:off[i+1]] (device),
+ * e.g. the per-instance residual norms of a ragged batch.  No reference counterpart. */
+int cpfem_segmented_dot(int32_t num_segments, const int64_t* offsets, const double* x,
+                        const double* y, double* out, void* stream);
+
 /* Device dot product x.y into *result (device), deterministic order. */
 size_t cpfem_dot_workspace_bytes(int64_t n);
 int cpfem_dot(int64_t n, const double* x, const double* y, double* result,
               void* workspace, void* stream);
 
-/*
- * y = A x with A in the node-block CSR layout (scalar CSR values as scipy orders them).
- */
-int cpfem_spmv(int32_t num_nodes, const int32_t* node_rowptr, const int32_t* node_cols,
-               const double* values, const double* x, double* y, void* stream);
-/* y = A^T x (gather form, needs node_tpos from cpfem_pattern_build). */
-int cpfem_spmv_t(int32_t num_nodes, const int32_t* node_rowptr, const int32_t* node_cols,
-                 const int32_t* node_tpos, const double* values, const double* x, double* y,
-                 void* stream);
+/* y = A x (transpose = 0) or y = A^T x (transpose != 0), values in the sliced-ELL layout. */
+int cpfem_spmv(const cpfem_sell_t* sell, const double* values, const double* x, double* y,
+               int32_t transpose, void* stream);
 
 /*
  * BiCGSTAB with Jacobi (precond=1), 3x3 block-Jacobi (precond=2) or no (0)
  * preconditioner.  Replaces jax_solve (crystal_plasticity_OR_design/solver.py:19-48):
- * same recurrences as jax.scipy.sparse.linalg.bicgstab, stop when
- * ||r||^2 <= max(tol^2 ||b||^2, atol^2).  transpose != 0 solves A^T x = b
- * (the adjoint solve of implicit_vjp, solver.py:844).
- * x holds x0 on entry and the solution on exit.  info[0] = iterations (or the
- * breakdown code -10/-11), info[1] = 1 if converged.  workspace: see
- * cpfem_bicgstab_workspace_bytes.  The call synchronises the stream to read the
- * convergence flag every check_every iterations.
+ * the recurrences of jax.scipy.sparse.linalg.bicgstab, stop when
+ * ||r||^2 <= max(tol^2 ||b||^2, atol^2), early exit on ||s||, breakdown codes -10/-11.
+ * transpose != 0 solves A^T x = b (the adjoint solve of implicit_vjp, solver.py:844).
+ * The whole solve is one persistent cooperative launch: every grid-wide wait is bounded
+ * and reports CPFEM_ERR_SOLVE instead of hanging.  x holds x0 on entry and the solution
+ * on exit; info[0] = iterations (or breakdown code), info[1] = 1 if converged.
+ * workspace: cpfem_bicgstab_workspace_bytes(num_nodes) bytes, 256-byte aligned.
+ * The call synchronises the stream to read info.
  */
 size_t cpfem_bicgstab_workspace_bytes(int32_t num_nodes);
-int cpfem_bicgstab(int32_t num_nodes, const int32_t* node_rowptr, const int32_t* node_cols,
-                   const int32_t* node_tpos, const double* values, const double* b, double* x,
-                   int32_t precond,
-                   int32_t transpose, double tol, double atol, int32_t maxiter,
-                   int32_t check_every, void* workspace, int32_t* info, void* stream);
+int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
+                   int32_t precond, int32_t transpose, double tol, double atol, int32_t maxiter,
+                   void* workspace, int32_t* info, void* stream);
+
+/*
+ * Ragged batch of independent systems (block-diagonal A over instances, instance i owning
+ * nodes [node_off[i], node_off[i+1])): BiCGSTAB per instance with its own scalars and
+ * its own stop test, one CTA per instance pulled from a work queue (list `active`, best
+ * ordered largest first).  Same recurrences and stop rule as cpfem_bicgstab.  info
+ * [2*num_instances] receives (iterations, converged) per listed instance; it stays on the
+ * device and the call does not synchronise.  No reference counterpart: the reference
+ * solves one RVE per jax_solve call (crystal_plasticity_OR_design/solver.py:19-48).
+ */
+size_t cpfem_bicgstab_batched_workspace_bytes(int32_t num_nodes);
+int cpfem_bicgstab_batched(const cpfem_sell_t* sell, const double* values, const double* b,
+                           double* x, int32_t precond, double tol, double atol, int32_t maxiter,
+                           int32_t num_active, const int32_t* active, const int32_t* node_off,
+                           void* workspace, int32_t* info, void* stream);
 
 /*
  * FP64 FMA throughput probe (measurement only, not on the solve path): launches `blocks`

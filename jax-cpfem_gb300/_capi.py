@@ -14,6 +14,7 @@ MAX_SLIP = 24
 
 CPFEM_GP_MAXITER = 1
 CPFEM_GP_NONFINITE = 2
+CPFEM_GP_BOUNDS = 4
 
 
 class CPFEMError(RuntimeError):
@@ -66,10 +67,41 @@ class GPArgs(ctypes.Structure):
     ]
 
 
+class VjpArgs(ctypes.Structure):
+    _fields_ = [
+        ("num_gp", ctypes.c_int64),
+        ("num_cells", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("dt", ctypes.c_double),
+        ("num_nodes", ctypes.c_int32),
+        ("num_rot", ctypes.c_int32),
+        ("num_param", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ] + [(name, ctypes.c_void_p) for name in (
+        "u", "cells", "shape_grads", "jxw", "fpi", "g", "rot_table", "rot_idx", "param_table", "param_idx",
+        "cell_sig_bar", "fpi_bar", "g_bar", "mu", "f_bar", "fpi_bar_old", "g_bar_old", "theta_bar", "rot_bar",
+        "status")]
+
+
+class Sell(ctypes.Structure):
+    _fields_ = [
+        ("num_nodes", ctypes.c_int32),
+        ("num_groups", ctypes.c_int32),
+        ("group_off", ctypes.c_void_p),
+        ("group_width", ctypes.c_void_p),
+        ("cols", ctypes.c_void_p),
+        ("tpos", ctypes.c_void_p),
+        ("diag_slot", ctypes.c_void_p),
+    ]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
 _D = ctypes.c_double
+
+# name -> (restype, argtypes); every symbol declared in include/cpfem_gb300.h
+_SP = ctypes.POINTER(Sell)
 
 # name -> (restype, argtypes); every symbol declared in include/cpfem_gb300.h
 SIGNATURES = {
@@ -78,20 +110,25 @@ SIGNATURES = {
     "cpfem_pattern_count": (ctypes.c_int, [_I32, _P, _I32, _P]),
     "cpfem_pattern_build": (ctypes.c_int, [_I32, _P, _I32, _P, _P, _P, _P]),
     "cpfem_pattern_expand_csr": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
+    "cpfem_sell_count": (ctypes.c_int, [_I32, _P, _P]),
+    "cpfem_sell_build": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "cpfem_sell_csr_map": (ctypes.c_int, [_I32, _P, _P, _P]),
     "cpfem_gp_eval": (ctypes.c_int, [ctypes.POINTER(Material), ctypes.POINTER(GPArgs), _P]),
-    "cpfem_elem_assemble": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
-    "cpfem_apply_dirichlet": (ctypes.c_int, [_I32, _P, _P, _P, _P, _I32, _P, _P, _P, _P]),
+    "cpfem_gp_vjp": (ctypes.c_int, [ctypes.POINTER(Material), ctypes.POINTER(VjpArgs), _P]),
+    "cpfem_elem_assemble": (ctypes.c_int, [_I32, _P, _P, _SP, _P, _P, _P, _P, _P, _P]),
+    "cpfem_apply_dirichlet": (ctypes.c_int, [_I32, _P, _P, _P, _P, _SP, _P, _P]),
     "cpfem_bc_initial_guess": (ctypes.c_int, [_I64, _I32, _P, _P, _P, _P, _P]),
     "cpfem_cell_average": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
     "cpfem_axpy": (ctypes.c_int, [_I64, _D, _P, _P, _P]),
+    "cpfem_segmented_dot": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P]),
     "cpfem_dot_workspace_bytes": (ctypes.c_size_t, [_I64]),
     "cpfem_dot": (ctypes.c_int, [_I64, _P, _P, _P, _P, _P]),
-    "cpfem_spmv": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P]),
-    "cpfem_spmv_t": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _P]),
+    "cpfem_spmv": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _P]),
     "cpfem_bicgstab_workspace_bytes": (ctypes.c_size_t, [_I32]),
+    "cpfem_bicgstab": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P, _P]),
+    "cpfem_bicgstab_batched_workspace_bytes": (ctypes.c_size_t, [_I32]),
+    "cpfem_bicgstab_batched": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _D, _D, _I32, _I32, _P, _P, _P, _P, _P]),
     "cpfem_probe_dfma": (ctypes.c_int, [_I64, _I32, _P, _P, _P]),
-    "cpfem_bicgstab": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P, _I32, _I32, _D, _D, _I32, _I32, _P,
-                                      _P, _P]),
 }
 
 _lib = None

@@ -1,0 +1,226 @@
+"""Hand-written discrete adjoint of the load-step sequence.
+
+Replaces the reference's differentiation path: ``ad_wrapper`` / ``implicit_vjp``
+(``crystal_plasticity_OR_design/solver.py:801-874``, driver copies in
+``calibration/calibration_case1_singleCrystalCopper_GB.py:73-94`` and
+``crystal_plasticity_OR_design/poly_sensitivity_rot_mesh2.py:70-92``) with ``jax.grad``
+running through every load step and through the local Newton's ``custom_jvp``.
+
+Forward: the plain load-step loop, checkpointing ``(u_n, Fp^-1_{n-1}, g_{n-1})`` per step.
+Backward, for n = N..1, with lambda_n the cotangent of the committed state z_n:
+  1. per GP (mode 1): F_bar from the stress cotangent and lambda_n, through the
+     implicit-function VJP of the converged local Newton (recomputed from the checkpoint);
+  2. f_u = gather of F_bar over the elements (assembly backward);
+  3. A_n^T mu = f_u with the step's row-eliminated tangent (transposed BiCGSTAB);
+  4. per GP (mode 2): lambda_{n-1} and the parameter / rotation cotangents from the stress
+     cotangent, lambda_n and the equilibrium term -mu^T dR/dp.
+Parameters: theta = (h0, g0, gs, a, m) and per-grain 'zyx' Euler angles in degrees
+composed as R = R_euler R_q (``poly_sensitivity_rot_mesh2.py:41-65,203``).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _capi
+from .material import euler_zyx_deg
+from .problem import _dev_ptr, _stream
+from . import solver as _solver
+
+THETA_NAMES = ("h0", "g0", "gs", "a", "m")
+
+
+def _euler_generators(angles_deg):
+    """Spatial angular-velocity vectors w_k (per degree) with [w_k]x = dR/dphi_k R^T for
+    R = Rx(c) Ry(b) Rz(a): w_a = Rx Ry e_z, w_b = Rx e_y, w_c = e_x."""
+    ang = np.deg2rad(np.asarray(angles_deg, dtype=np.float64))
+    b, c = ang[..., 1], ang[..., 2]
+    cb, sb, cc, sc = np.cos(b), np.sin(b), np.cos(c), np.sin(c)
+    out = np.zeros(ang.shape[:-1] + (3, 3))
+    # Ry e_z = (sb, 0, cb); Rx (x, y, z) = (x, cc y - sc z, sc y + cc z)
+    out[..., 0, 0] = sb
+    out[..., 0, 1] = -sc * cb
+    out[..., 0, 2] = cc * cb
+    out[..., 1, 1] = cc
+    out[..., 1, 2] = sc
+    out[..., 2, 0] = 1.0
+    return out * (np.pi / 180.0)
+
+
+class LoadHistory:
+    """A load-step sequence on a ``CrystalPlasticity`` problem with checkpoints.
+
+    ``bc_fn(i, disp) -> (node_lists, components, values)`` gives the Dirichlet lists of step
+    i.  ``grain_quat`` (n_grains, 4) and the problem's per-GP ``rot_idx`` (the cell's grain)
+    define the orientations; ``euler`` rotates them.
+    """
+
+    def __init__(self, problem, disps, ts, bc_fn, grain_quat, solver_options=None, adjoint_options=None):
+        self.p = problem
+        self.disps = np.asarray(disps, dtype=np.float64)
+        self.ts = np.asarray(ts, dtype=np.float64)
+        self.bc_fn = bc_fn
+        self.grain_quat = np.asarray(grain_quat, dtype=np.float64)
+        self.opts = dict(solver_options or {"jax_solver": {}})
+        self.adj_opts = dict(adjoint_options or {})
+        self.rot_idx0 = problem.rot_idx.clone()
+        self.n_steps = len(self.ts) - 1
+
+    # ------------------------------------------------------------------ set-up
+    def _set_theta(self, theta, euler):
+        p = self.p
+        h0, g0, gs, a, m = (float(v) for v in theta)
+        from .material import rot_mat
+        R = euler_zyx_deg(np.asarray(euler, dtype=np.float64)) @ rot_mat(self.grain_quat)
+        p.rot_table = torch.tensor(R.reshape(-1, 9), dtype=torch.float64, device=p.device)
+        p.rot_idx = self.rot_idx0.clone()
+        p.param_table = torch.tensor([[a, h0, gs, m, p.material.r]], dtype=torch.float64, device=p.device)
+        p.param_idx = None
+        G, N = p.num_gp, p.num_slip
+        p.fpi = torch.zeros((9, G), dtype=torch.float64, device=p.device)
+        p.fpi[0] = p.fpi[4] = p.fpi[8] = 1.0
+        p.g = torch.full((N, G), g0, dtype=torch.float64, device=p.device)
+        p.slip = torch.zeros((N, G), dtype=torch.float64, device=p.device)
+        p._views = None
+        p._post_cache = None
+
+    def _set_step(self, i):
+        p = self.p
+        p.dt = float(self.ts[i + 1] - self.ts[i])
+        nodes, comps, vals = self.bc_fn(i, float(self.disps[i + 1]))
+        p.fes[0].set_dirichlet_lists(nodes, comps, vals)
+
+    # ------------------------------------------------------------------ forward
+    def forward(self, theta, euler, checkpoint=True):
+        """Run the load steps; returns the mean cell Cauchy stress per step (n_steps, 3, 3)."""
+        p = self.p
+        self._set_theta(theta, euler)
+        self.theta = np.asarray(theta, dtype=np.float64)
+        self.euler = np.asarray(euler, dtype=np.float64)
+        sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
+        self.ckpt = []
+        out = []
+        params = p.internal_vars
+        for i in range(self.n_steps):
+            self._set_step(i)
+            p.set_params(params)
+            if checkpoint:
+                self.ckpt.append((p.fpi.clone(), p.g.clone()))
+            o = dict(self.opts)
+            o["initial_guess"] = [sol.reshape(-1, 3)]
+            sol = _solver.solver(p, o)[0].reshape(-1)
+            sig = p.compute_avg_stress(sol.reshape(-1, 3), params)
+            out.append(sig.mean(0))
+            params = p.update_int_vars_gp(sol.reshape(-1, 3), params)
+            if checkpoint:
+                self.ckpt[-1] = self.ckpt[-1] + (sol.clone(),)
+        p.set_params(params)
+        return torch.stack(out)
+
+    # ------------------------------------------------------------------ backward
+    def _vjp(self, mode, u, fpi, g, cell_sig_bar, lam_fp, lam_g, mu=None):
+        p = self.p
+        G, N = p.num_gp, p.num_slip
+        a = _capi.VjpArgs()
+        a.num_gp, a.num_cells, a.mode, a.dt = G, p.num_cells, mode, float(p.dt)
+        a.num_nodes, a.num_rot = p.num_nodes, int(p.rot_table.shape[0])
+        a.num_param = int(p.param_table.shape[0])
+        fe = p.fes[0]
+        a.u, a.cells, a.shape_grads, a.jxw = u.data_ptr(), fe.cells.data_ptr(), fe.shape_grads.data_ptr(), \
+            fe.JxW.data_ptr()
+        a.fpi, a.g = fpi.data_ptr(), g.data_ptr()
+        a.rot_table, a.rot_idx = p.rot_table.data_ptr(), p.rot_idx.data_ptr()
+        a.param_table = p.param_table.data_ptr()
+        a.param_idx = _dev_ptr(p.param_idx)
+        a.cell_sig_bar = _dev_ptr(cell_sig_bar)
+        a.fpi_bar, a.g_bar = _dev_ptr(lam_fp), _dev_ptr(lam_g)
+        a.mu = _dev_ptr(mu)
+        status = torch.zeros(1, dtype=torch.int32, device=p.device)
+        a.status = status.data_ptr()
+        outs = {}
+        if mode == 1:
+            outs["f_bar"] = torch.empty((9, G), dtype=torch.float64, device=p.device)
+            a.f_bar = outs["f_bar"].data_ptr()
+        else:
+            outs["fpi_bar_old"] = torch.empty((9, G), dtype=torch.float64, device=p.device)
+            outs["g_bar_old"] = torch.empty((N, G), dtype=torch.float64, device=p.device)
+            outs["theta_bar"] = torch.empty((5, G), dtype=torch.float64, device=p.device)
+            outs["rot_bar"] = torch.empty((3, G), dtype=torch.float64, device=p.device)
+            for k, v in outs.items():
+                setattr(a, k, v.data_ptr())
+        with p.region(f"gp_vjp{mode}"):
+            _capi.check(p.lib.cpfem_gp_vjp(p.mat_c, a, _stream()))
+        p._check_status(status)
+        return outs
+
+    def backward(self, stress_bar):
+        """stress_bar: (n_steps, 3, 3) cotangent of the per-step mean cell stress.
+        Returns (theta_bar (5,), euler_bar (n_grains, 3))."""
+        p = self.p
+        G, N, E = p.num_gp, p.num_slip, p.num_cells
+        stress_bar = torch.as_tensor(stress_bar, dtype=torch.float64, device=p.device).reshape(self.n_steps, 9)
+        lam_fp = torch.zeros((9, G), dtype=torch.float64, device=p.device)
+        lam_g = torch.zeros((N, G), dtype=torch.float64, device=p.device)
+        theta_acc = torch.zeros(5, dtype=torch.float64, device=p.device)
+        rot_acc = torch.zeros((p.rot_table.shape[0], 3), dtype=torch.float64, device=p.device)
+        ridx = p.rot_idx.long()
+        pc = self.adj_opts.get("precond", 1)
+        self.krylov_iters = []
+        for i in reversed(range(self.n_steps)):
+            fpi, g, u = self.ckpt[i]
+            self._set_step(i)
+            p.fpi, p.g = fpi, g
+            p._views = None
+            cell_bar = (stress_bar[i] / E).expand(E, 9).contiguous()
+            # 1. F cotangent and its gather into the right-hand side
+            fb = self._vjp(1, u, fpi, g, cell_bar, lam_fp, lam_g)["f_bar"]
+            f_u = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
+            fe = p.fes[0]
+            _capi.check(p.lib.cpfem_elem_assemble(p.num_cells, fe.cells.data_ptr(), fe.shape_grads.data_ptr(),
+                                                  p.sell, p.elem_pos.data_ptr(), fb.data_ptr(), None,
+                                                  f_u.data_ptr(), None, _stream()))
+            # 2. the step's tangent, row-eliminated, and the transposed solve
+            res, A = _solver.newton_update_helper(p, u)
+            mu0 = torch.zeros_like(f_u)
+            mu, k, ok = _solver.bicgstab(p, A.T, f_u, mu0, precond=pc, tol=self.adj_opts.get("tol", 1e-10),
+                                         atol=self.adj_opts.get("atol", 1e-14),
+                                         maxiter=self.adj_opts.get("maxiter", 10000))
+            self.krylov_iters.append(k)
+            if not ok:
+                raise RuntimeError(f"adjoint solve did not converge (iterations {k})")
+            mu[fe.bc_dofs.long()] = 0.0
+            # 3. cotangents of the step's inputs
+            o = self._vjp(2, u, fpi, g, cell_bar, lam_fp, lam_g, mu)
+            lam_fp, lam_g = o["fpi_bar_old"], o["g_bar_old"]
+            theta_acc += o["theta_bar"].sum(1)
+            rot_acc.index_add_(0, ridx, o["rot_bar"].t())
+        # parameters: (gss_a, h, t_sat, xm) -> (a, h0, gs, m); g0 through the initial state
+        th = theta_acc.cpu().numpy()
+        theta_bar = np.array([th[1], float(lam_g.sum()), th[2], th[0], th[3]])
+        gen = _euler_generators(self.euler)                       # (n_grains, 3 angles, 3)
+        euler_bar = np.einsum("gkj,gj->gk", gen, rot_acc.cpu().numpy())
+        return theta_bar, euler_bar
+
+
+class SimulationFunction(torch.autograd.Function):
+    """torch.autograd.Function over a LoadHistory: (theta (5,), euler (G,3)) -> the per-step
+    mean cell stress (n_steps, 3, 3); backward runs the hand-written adjoint."""
+
+    @staticmethod
+    def forward(ctx, theta, euler, history):
+        ctx.history = history
+        out = history.forward(theta.detach().cpu().numpy(), euler.detach().cpu().numpy())
+        ctx.save_for_backward(theta, euler)
+        return out.to(theta.device)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        theta, euler = ctx.saved_tensors
+        tb, eb = ctx.history.backward(grad_out)
+        return (torch.as_tensor(tb, dtype=theta.dtype, device=theta.device),
+                torch.as_tensor(eb, dtype=euler.dtype, device=euler.device), None)
+
+
+def simulate(history, theta, euler):
+    """Differentiable forward: ``SimulationFunction.apply``."""
+    return SimulationFunction.apply(theta, euler, history)

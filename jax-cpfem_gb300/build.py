@@ -17,9 +17,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcpfem_gb300.so")
 
-CUDA_SOURCES = ["assembly.cu", "krylov.cu", "probe.cu"]
+CUDA_SOURCES = ["assembly.cu", "krylov.cu", "adjoint.cu", "probe.cu"]
 CXX_SOURCES = ["pattern.cpp"]
-HEADERS = ["cpfem_common.cuh", "gp_update.cuh", "reduce.cuh"]
+HEADERS = ["cpfem_common.cuh", "gp_update.cuh", "gp_adjoint.cuh", "reduce.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

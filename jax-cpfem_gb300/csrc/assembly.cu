@@ -1,5 +1,6 @@
 // Constitutive pass, element assembly, Dirichlet row elimination and small vector
 // kernels of the cpfem_gb300 C ABI.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
 template <bool WITH_K>
 __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ cells,
                                                        const double* __restrict__ sg,
-                                                       const int32_t* __restrict__ nrp,
+                                                       const int64_t* __restrict__ goff,
                                                        const uint8_t* __restrict__ epos,
                                                        const double* __restrict__ Pw,
                                                        const double* __restrict__ Dw,
@@ -222,24 +223,22 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
 #pragma unroll
     for (int i = 0; i < 3; ++i) atomicAdd(&res[3 * na + i], Rr[i]);
   if (WITH_K) {
-    const int64_t r0 = nrp[na];
-    const int64_t deg = nrp[na + 1] - r0;
-    const int64_t base = 9 * r0;
+    // sliced-ELL slot of (node na, neighbour b): 9*goff[g] + 32*(9*pos + 3i + k) + lane
+    const int64_t base = 9 * goff[na >> 5] + (na & 31);
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
       const int64_t pos = epos[e * 64 + 8 * a + b];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) atomicAdd(&vals[base + i * 3 * deg + 3 * pos + k], K[i][3 * b + k]);
+        for (int k = 0; k < 3; ++k) atomicAdd(&vals[base + 32 * (9 * pos + 3 * i + k)], K[i][3 * b + k]);
     }
   }
 }
 
 // Row elimination for a list of unique Dirichlet dofs.
 __global__ void k_dirichlet(int32_t nbc, const int32_t* __restrict__ dofs, const double* __restrict__ bvals,
-                            const double* __restrict__ u, double* __restrict__ res,
-                            const int32_t* __restrict__ nrp, const int32_t* __restrict__ ncol,
+                            const double* __restrict__ u, double* __restrict__ res, const cpfem_sell_t L,
                             double* __restrict__ vals) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nbc) return;
@@ -251,12 +250,13 @@ __global__ void k_dirichlet(int32_t nbc, const int32_t* __restrict__ dofs, const
   if (vals != nullptr) {
     const int64_t na = d / 3;
     const int i = (int)(d % 3);
-    const int64_t r0 = nrp[na];
-    const int64_t deg = nrp[na + 1] - r0;
-    const int64_t base = 9 * r0 + i * 3 * deg;
-    for (int64_t v = 0; v < 3 * deg; ++v) vals[base + v] = 0.0;
-    for (int64_t j = 0; j < deg; ++j)
-      if (ncol[r0 + j] == na) vals[base + 3 * j + i] = 1.0;
+    const int64_t g = na >> 5;
+    const int64_t base = 9 * L.group_off[g] + (na & 31);
+    const int w = L.group_width[g];
+    for (int j = 0; j < w; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) vals[base + 32 * (9 * j + 3 * i + k)] = 0.0;
+    vals[base + 32 * (9 * L.diag_slot[na] + 3 * i + i)] = 1.0;
   }
 }
 
@@ -298,6 +298,20 @@ __global__ void __launch_bounds__(kVecThreads) k_dot(int64_t n, const double* __
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     v[0] = fma(x[i], y[i], v[0]);
   if (grid_sum<1>(v, partials, counter, smem) && threadIdx.x == 0) *result = v[0];
+}
+
+// out[i] = x.y over entries [off[i], off[i+1]) -- one block per segment, fixed order.
+__global__ void __launch_bounds__(256) k_segmented_dot(int32_t nseg, const int64_t* __restrict__ off,
+                                                       const double* __restrict__ x, const double* __restrict__ y,
+                                                       double* __restrict__ out) {
+  __shared__ double smem[32];
+  for (int seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
+    double v[1] = {0.0};
+    for (int64_t i = off[seg] + threadIdx.x; i < off[seg + 1]; i += blockDim.x) v[0] = fma(x[i], y[i], v[0]);
+    block_sum<1>(v, smem);
+    if (threadIdx.x == 0) out[seg] = v[0];
+    __syncthreads();
+  }
 }
 
 template <int NS>
@@ -345,33 +359,35 @@ int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void
 }
 
 int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* shape_grads,
-                        const int32_t* node_rowptr, const uint8_t* elem_pos, const double* pk1_w,
+                        const cpfem_sell_t* sell, const uint8_t* elem_pos, const double* pk1_w,
                         const double* tangent_w, double* residual, double* values, void* stream) {
   if (num_cells == 0) return CPFEM_OK;
   CPFEM_REQUIRE(num_cells > 0 && cells && shape_grads && pk1_w, "bad element arguments");
   CPFEM_REQUIRE((values == nullptr) == (tangent_w == nullptr), "values and tangent_w go together");
-  CPFEM_REQUIRE(values == nullptr || (node_rowptr && elem_pos), "values need the pattern");
+  CPFEM_REQUIRE(values == nullptr || (sell && sell->group_off && elem_pos), "values need the layout");
   const int threads = 128;
   const unsigned blocks = (unsigned)ceil_div((int64_t)num_cells * 8, threads);
   cudaStream_t s = (cudaStream_t)stream;
   if (values != nullptr)
-    k_elem_assemble<true><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, node_rowptr, elem_pos,
+    k_elem_assemble<true><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, sell->group_off, elem_pos,
                                                     pk1_w, tangent_w, residual, values);
   else
-    k_elem_assemble<false><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, node_rowptr, elem_pos,
+    k_elem_assemble<false><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, nullptr, elem_pos,
                                                      pk1_w, nullptr, residual, nullptr);
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;
 }
 
 int cpfem_apply_dirichlet(int32_t num_bc, const int32_t* bc_dofs, const double* bc_vals, const double* u,
-                          double* residual, int32_t num_nodes, const int32_t* node_rowptr,
-                          const int32_t* node_cols, double* values, void* stream) {
+                          double* residual, const cpfem_sell_t* sell, double* values, void* stream) {
   if (num_bc == 0) return CPFEM_OK;
   CPFEM_REQUIRE(num_bc > 0 && bc_dofs && bc_vals, "bad Dirichlet arguments");
-  CPFEM_REQUIRE(values == nullptr || (node_rowptr && node_cols && num_nodes > 0), "values need the pattern");
-  k_dirichlet<<<(unsigned)ceil_div(num_bc, 128), 128, 0, (cudaStream_t)stream>>>(
-      num_bc, bc_dofs, bc_vals, u, residual, node_rowptr, node_cols, values);
+  CPFEM_REQUIRE(values == nullptr || (sell && sell->group_off && sell->group_width && sell->diag_slot),
+                "values need the layout");
+  cpfem_sell_t L{};
+  if (sell) L = *sell;
+  k_dirichlet<<<(unsigned)ceil_div(num_bc, 128), 128, 0, (cudaStream_t)stream>>>(num_bc, bc_dofs, bc_vals, u,
+                                                                                 residual, L, values);
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;
 }
@@ -404,6 +420,16 @@ int cpfem_axpy(int64_t n, double alpha, const double* x, double* y, void* stream
   CPFEM_REQUIRE(n > 0 && x && y, "bad axpy arguments");
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 4 * 152);
   k_axpy<<<blocks, 256, 0, (cudaStream_t)stream>>>(n, alpha, x, y);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+int cpfem_segmented_dot(int32_t num_segments, const int64_t* offsets, const double* x, const double* y,
+                        double* out, void* stream) {
+  if (num_segments == 0) return CPFEM_OK;
+  CPFEM_REQUIRE(num_segments > 0 && offsets && x && y && out, "bad segmented dot arguments");
+  const unsigned blocks = (unsigned)std::min<int64_t>(num_segments, 8 * 152);
+  k_segmented_dot<<<blocks, 256, 0, (cudaStream_t)stream>>>(num_segments, offsets, x, y, out);
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;
 }

@@ -16,6 +16,27 @@
 
 namespace cpfem {
 
+// x^e for x >= 0 and a non-negative integer e, by binary exponentiation.  The
+// Kalidindi exponents 1/m - 1 and a are integers for every shipped material (1/m = 10,
+// 20, 120; a = 2, 8), and this costs about 2 log2(e) FP64 multiplies against the ~100
+// FP64 operations of a general pow.
+CPFEM_HD double ipow(double x, int e) {
+  double r = 1.0;
+  while (e > 0) {
+    if (e & 1) r *= x;
+    x *= x;
+    e >>= 1;
+  }
+  return r;
+}
+
+// The integer exponent to use for x^p, or -1 when p is not a small non-negative integer.
+CPFEM_HD int int_exponent(double p) {
+  return (p >= 0.0 && p <= 1024.0 && p == floor(p)) ? (int)p : -1;
+}
+
+CPFEM_HD double powe(double x, double p, int ie) { return (ie >= 0) ? ipow(x, ie) : pow(x, p); }
+
 template <int NS>
 struct GPSolve {
   double s[6];      // converged lattice-frame S (tensor components)
@@ -30,7 +51,7 @@ struct GPSolve {
 // Residual at s.  Ct = (F Fp^-1_old R)^T (F Fp^-1_old R) (symmetric, full 3x3).
 template <int NS>
 CPFEM_HD void cp_residual(const MatDev& m, const double* Ct, const double* ig,
-                                            double cdt, double pexp, const double* s, double* r,
+                                            double cdt, double pexp, int ie1, const double* s, double* r,
                                             double& rn, double* dg, double* kk, double* B,
                                             double* M) {
   double L[9];
@@ -44,7 +65,7 @@ CPFEM_HD void cp_residual(const MatDev& m, const double* Ct, const double* ig,
     const double ax = fabs(x);
     // |x|^(p-1): dg = cdt |x|^(p-1) x = cdt |x|^p sign(tau) (g > 0), and the derivative
     // p cdt |x|^(p-1) / g uses the same power.
-    const double pw1 = (ax > 0.0) ? pow(ax, pexp - 1.0) : 0.0;
+    const double pw1 = (ax > 0.0) ? powe(ax, pexp - 1.0, ie1) : 0.0;
     const double d = cdt * pw1 * x;
     dg[a] = d;
     kk[a] = cdt * pexp * pw1 * ig[a];
@@ -108,10 +129,11 @@ CPFEM_HD void cp_jacobian(const MatDev& m, const double* kk, const double* M,
 template <int NS>
 CPFEM_HD void cp_local_newton(const MatDev& m, const double* Ct, const double* ig,
                                                 double cdt, double pexp, GPSolve<NS>& st) {
+  const int ie1 = int_exponent(pexp - 1.0);
   double r[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) st.s[k] = 0.0;
-  cp_residual<NS>(m, Ct, ig, cdt, pexp, st.s, r, st.rn, st.dg, st.kk, st.B, st.M);
+  cp_residual<NS>(m, Ct, ig, cdt, pexp, ie1, st.s, r, st.rn, st.dg, st.kk, st.B, st.M);
   int it = 0;
   while (st.rn > m.local_tol && it < m.max_iter) {
     double J[36];
@@ -130,7 +152,7 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const double* Ct, const double* i
     do {
 #pragma unroll
       for (int k = 0; k < 6; ++k) st_s[k] = fma(relax, ds[k], st.s[k]);
-      cp_residual<NS>(m, Ct, ig, cdt, pexp, st_s, r, st.rn, st.dg, st.kk, st.B, st.M);
+      cp_residual<NS>(m, Ct, ig, cdt, pexp, ie1, st_s, r, st.rn, st.dg, st.kk, st.B, st.M);
       relax *= 0.5;
       ++sub;
     } while (st.rn >= rn0 && sub < m.max_sub_step);
@@ -251,11 +273,12 @@ CPFEM_HD void cp_hardening(const MatDev& m, const double* g, const double* dg,
                                              double* g_new) {
   double tmp[NS];
   double total = 0.0;
+  const int ia = int_exponent(gss_a);
 #pragma unroll
   for (int b = 0; b < NS; ++b) {
     const double ratio = 1.0 - g[b] / t_sat;
     const double ar = fabs(ratio);
-    const double pw = (ar > 0.0) ? pow(ar, gss_a) : 0.0;
+    const double pw = (ar > 0.0) ? powe(ar, gss_a, ia) : 0.0;
     const double sg = (ratio > 0.0) ? 1.0 : ((ratio < 0.0) ? -1.0 : 0.0);
     tmp[b] = h * fabs(dg[b]) * pw * sg;
     total += tmp[b];

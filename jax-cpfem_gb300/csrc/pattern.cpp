@@ -122,3 +122,86 @@ int cpfem_pattern_expand_csr(int32_t num_nodes, const int32_t* node_rowptr, cons
 }
 
 }  // extern "C"
+
+// ---- sliced-ELL layout of the same pattern ------------------------------------------
+extern "C" {
+
+int cpfem_sell_count(int32_t num_nodes, const int32_t* node_rowptr, int64_t* total_slots) {
+  if (num_nodes < 0 || !node_rowptr || !total_slots) {
+    cpfem::set_error("bad sell arguments");
+    return CPFEM_ERR_ARG;
+  }
+  int64_t total = 0;
+  for (int32_t g0 = 0; g0 < num_nodes; g0 += 32) {
+    int32_t w = 0;
+    for (int32_t a = g0; a < std::min(num_nodes, g0 + 32); ++a) w = std::max(w, node_rowptr[a + 1] - node_rowptr[a]);
+    total += 32 * (int64_t)w;
+  }
+  if (9 * total > ((int64_t)1 << 40)) {
+    cpfem::set_error("sell layout too large");
+    return CPFEM_ERR_SIZE;
+  }
+  *total_slots = total;
+  return CPFEM_OK;
+}
+
+int cpfem_sell_build(int32_t num_nodes, const int32_t* node_rowptr, const int32_t* node_cols,
+                     const int32_t* node_tpos, int64_t* group_off, int32_t* group_width, int32_t* cols,
+                     int32_t* tpos, int32_t* diag_slot) {
+  if (num_nodes < 0 || !node_rowptr || !node_cols || !group_off || !group_width || !cols || !diag_slot) {
+    cpfem::set_error("bad sell arguments");
+    return CPFEM_ERR_ARG;
+  }
+  const int32_t ng = (num_nodes + 31) / 32;
+  group_off[0] = 0;
+  for (int32_t g = 0; g < ng; ++g) {
+    const int32_t a0 = 32 * g, a1 = std::min(num_nodes, a0 + 32);
+    int32_t w = 0;
+    for (int32_t a = a0; a < a1; ++a) w = std::max(w, node_rowptr[a + 1] - node_rowptr[a]);
+    group_width[g] = w;
+    group_off[g + 1] = group_off[g] + 32 * (int64_t)w;
+    for (int32_t lane = 0; lane < 32; ++lane) {
+      const int32_t a = a0 + lane;
+      for (int32_t j = 0; j < w; ++j) {
+        const int64_t s = group_off[g] + 32 * (int64_t)j + lane;
+        if (a < a1 && j < node_rowptr[a + 1] - node_rowptr[a]) {
+          cols[s] = node_cols[node_rowptr[a] + j];
+          if (tpos) tpos[s] = node_tpos ? node_tpos[node_rowptr[a] + j] : 0;
+        } else {
+          // padding: own node (or the group's first node past the end), zero values
+          cols[s] = (a < a1) ? a : a0;
+          if (tpos) tpos[s] = j;
+        }
+      }
+      if (a < a1) {
+        int32_t d = -1;
+        for (int32_t j = node_rowptr[a]; j < node_rowptr[a + 1]; ++j)
+          if (node_cols[j] == a) d = j - node_rowptr[a];
+        if (d < 0) {
+          cpfem::set_error("node missing from its own neighbour list");
+          return CPFEM_ERR_ARG;
+        }
+        diag_slot[a] = d;
+      }
+    }
+  }
+  return CPFEM_OK;
+}
+
+int cpfem_sell_csr_map(int32_t num_nodes, const int32_t* node_rowptr, const int64_t* group_off, int64_t* map) {
+  if (num_nodes < 0 || !node_rowptr || !group_off || !map) {
+    cpfem::set_error("bad sell map arguments");
+    return CPFEM_ERR_ARG;
+  }
+  int64_t w = 0;
+  for (int32_t a = 0; a < num_nodes; ++a) {
+    const int32_t g = a / 32, lane = a % 32;
+    const int32_t deg = node_rowptr[a + 1] - node_rowptr[a];
+    for (int i = 0; i < 3; ++i)
+      for (int32_t j = 0; j < deg; ++j)
+        for (int k = 0; k < 3; ++k) map[w++] = 9 * group_off[g] + 32 * (int64_t)(9 * j + 3 * i + k) + lane;
+  }
+  return CPFEM_OK;
+}
+
+}  // extern "C"

@@ -129,15 +129,10 @@ class DeviceCSR:
 
     def matvec(self, x):
         p = self.problem
+        x = x.contiguous()
         y = torch.empty_like(x)
-        lib = p.lib
-        if self.transposed:
-            _capi.check(lib.cpfem_spmv_t(p.num_nodes, _dev_ptr(p.node_rowptr), _dev_ptr(p.node_cols),
-                                         _dev_ptr(p.node_tpos), _dev_ptr(self.values), _dev_ptr(x), _dev_ptr(y),
-                                         _stream()))
-        else:
-            _capi.check(lib.cpfem_spmv(p.num_nodes, _dev_ptr(p.node_rowptr), _dev_ptr(p.node_cols),
-                                       _dev_ptr(self.values), _dev_ptr(x), _dev_ptr(y), _stream()))
+        _capi.check(p.lib.cpfem_spmv(p.sell, _dev_ptr(self.values), _dev_ptr(x), _dev_ptr(y),
+                                     1 if self.transposed else 0, _stream()))
         return y
 
     __matmul__ = matvec
@@ -147,7 +142,8 @@ class DeviceCSR:
         import scipy.sparse as sp
         p = self.problem
         indptr, indices = p.csr_arrays()
-        A = sp.csr_array((self.values.cpu().numpy(), indices, indptr), shape=self.shape)
+        data = self.values[p.csr_map()].cpu().numpy()
+        A = sp.csr_array((data, indices, indptr), shape=self.shape)
         return A.T.tocsr() if self.transposed else A
 
     def getValuesCSR(self):
@@ -220,10 +216,37 @@ class CrystalPlasticity:
         self.nnz = 9 * nb
         self._rowptr_np, self._cols_np = rowptr, cols
         dev = self.device
-        self.node_rowptr = torch.tensor(rowptr, device=dev)
-        self.node_cols = torch.tensor(cols, device=dev)
+        # sliced-ELL device layout of the values
+        slots = np.zeros(1, dtype=np.int64)
+        _capi.check(self.lib.cpfem_sell_count(self.num_nodes, rowptr.ctypes.data, slots.ctypes.data))
+        slots = int(slots[0])
+        ng = (self.num_nodes + 31) // 32
+        goff = np.zeros(ng + 1, dtype=np.int64)
+        gw = np.zeros(ng, dtype=np.int32)
+        scols = np.zeros(slots, dtype=np.int32)
+        stpos = np.zeros(slots, dtype=np.int32)
+        dslot = np.zeros(self.num_nodes, dtype=np.int32)
+        _capi.check(self.lib.cpfem_sell_build(self.num_nodes, rowptr.ctypes.data, cols.ctypes.data,
+                                              tpos.ctypes.data, goff.ctypes.data, gw.ctypes.data,
+                                              scols.ctypes.data, stpos.ctypes.data, dslot.ctypes.data))
+        self._goff_np = goff
+        self.num_values = 9 * slots
+        self.sell_arrays = {k: torch.tensor(v, device=dev) for k, v in
+                            (("group_off", goff), ("group_width", gw), ("cols", scols), ("tpos", stpos),
+                             ("diag_slot", dslot))}
+        self.sell = _capi.Sell(self.num_nodes, ng, *(self.sell_arrays[k].data_ptr() for k in
+                                                     ("group_off", "group_width", "cols", "tpos", "diag_slot")))
         self.elem_pos = torch.tensor(epos, device=dev)
-        self.node_tpos = torch.tensor(tpos, device=dev)
+        self._csr_map = None
+
+    def csr_map(self):
+        """Index of every scalar-CSR value (scipy's order) in the sliced-ELL values."""
+        if self._csr_map is None:
+            m = np.zeros(self.nnz, dtype=np.int64)
+            _capi.check(self.lib.cpfem_sell_csr_map(self.num_nodes, self._rowptr_np.ctypes.data,
+                                                    self._goff_np.ctypes.data, m.ctypes.data))
+            self._csr_map = torch.tensor(m, device=self.device)
+        return self._csr_map
 
     def csr_arrays(self):
         """Scalar CSR ``indptr``/``indices`` of the global matrix (host numpy)."""
@@ -381,6 +404,8 @@ class CrystalPlasticity:
 
     def _check_status(self, status):
         s = int(status.item())
+        if s & _capi.CPFEM_GP_BOUNDS:
+            raise IndexError("an index gathered by a Gauss-point kernel was out of range")
         if s & _capi.CPFEM_GP_NONFINITE:
             raise FloatingPointError("non-finite stress in the local Newton solve")
         if s & _capi.CPFEM_GP_MAXITER:
@@ -397,7 +422,7 @@ class CrystalPlasticity:
         status.zero_()
         values = dw = None
         if need_tangent:
-            values = self._buf("values", (self.nnz,))
+            values = self._buf("values", (self.num_values,))
             values.zero_()
             dw = self._buf("tangent_w", (81, G))
         its = self._buf("iters", (G,), torch.int32) if self.timing else None
@@ -411,7 +436,7 @@ class CrystalPlasticity:
         fe = self.fes[0]
         with self.region("elem_assemble"):
             _capi.check(self.lib.cpfem_elem_assemble(self.num_cells, _dev_ptr(fe.cells), _dev_ptr(fe.shape_grads),
-                                                 _dev_ptr(self.node_rowptr), _dev_ptr(self.elem_pos),
+                                                     self.sell, _dev_ptr(self.elem_pos),
                                                      _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res), _dev_ptr(values),
                                                      _stream()))
         return res, values, status
@@ -420,8 +445,7 @@ class CrystalPlasticity:
         fe = self.fes[0]
         n = int(fe.bc_dofs.numel())
         _capi.check(self.lib.cpfem_apply_dirichlet(n, _dev_ptr(fe.bc_dofs), _dev_ptr(fe.bc_vals), _dev_ptr(u),
-                                                   _dev_ptr(res), self.num_nodes, _dev_ptr(self.node_rowptr),
-                                                   _dev_ptr(self.node_cols), _dev_ptr(values), _stream()))
+                                                   _dev_ptr(res), self.sell, _dev_ptr(values), _stream()))
 
     def newton_update(self, sol_list):
         """JAX-FEM ``newton_update``: residual list; the tangent is kept on the device
@@ -432,10 +456,14 @@ class CrystalPlasticity:
         self.A_values = values
         return [res.reshape(self.num_nodes, 3)]
 
-    def compute_residual(self, sol_list):
+    def compute_residual(self, sol_list, check=True):
+        """Residual only.  ``check=False`` lets non-finite or unconverged local solves
+        through as values (the global line search compares their norms the way the
+        reference does, ``solver.py:258-272``)."""
         u = _flat(sol_list, self.device)
         res, _, status = self.assemble(u, need_tangent=False)
-        self._check_status(status)
+        if check:
+            self._check_status(status)
         return [res.reshape(self.num_nodes, 3)]
 
     def get_tensor_map(self):

@@ -35,20 +35,19 @@ def norm(problem, x):
     return math.sqrt(_dot(problem, x, x))
 
 
-def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, check_every=32):
-    """``jax.scipy.sparse.linalg.bicgstab`` on the device CSR (``solver.py:34-40``).
-    precond: 0 none, 1 Jacobi 1/diag(A) (the reference), 2 3x3 block-Jacobi.
-    Returns (x, iterations or breakdown code, converged)."""
+def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000):
+    """``jax.scipy.sparse.linalg.bicgstab`` on the device matrix (``solver.py:34-40``), one
+    persistent cooperative launch.  precond: 0 none, 1 Jacobi 1/diag(A) (the
+    reference), 2 3x3 block-Jacobi.  Returns (x, iterations or breakdown code, converged)."""
     lib = problem.lib
     x = x0.clone()
     nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
     with problem.region("bicgstab"):
-        _capi.check(lib.cpfem_bicgstab(problem.num_nodes, _dev_ptr(problem.node_rowptr), _dev_ptr(problem.node_cols),
-                                       _dev_ptr(problem.node_tpos), _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
+        _capi.check(lib.cpfem_bicgstab(problem.sell, _dev_ptr(A.values), _dev_ptr(b.contiguous()), _dev_ptr(x),
                                        int(precond), 1 if A.transposed else 0, float(tol), float(atol),
-                                       int(maxiter), int(check_every), _dev_ptr(ws), info.ctypes.data, _stream()))
+                                       int(maxiter), _dev_ptr(ws), info.ctypes.data, _stream()))
     return x, int(info[0]), bool(info[1])
 
 
@@ -59,8 +58,7 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
     pc = opts.get("precond", precond)
     pc = {True: 1, False: 0, "jacobi": 1, "block3": 2, "block_jacobi": 2}.get(pc, pc)
     x, k, ok = bicgstab(problem, A, b, x0, precond=pc, tol=opts.get("tol", 1e-10),
-                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000),
-                        check_every=opts.get("check_every", 32))
+                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000))
     problem.stats["krylov_iters"].append(k)
     r = A.matvec(x)
     r.sub_(b)
@@ -91,8 +89,8 @@ def newton_update_helper(problem, dofs):
     return res, DeviceCSR(problem, problem.A_values)
 
 
-def residual_bc(problem, dofs):
-    res = problem.compute_residual(problem.unflatten_fn_sol_list(dofs))[0].reshape(-1)
+def residual_bc(problem, dofs, check=True):
+    res = problem.compute_residual(problem.unflatten_fn_sol_list(dofs), check=check)[0].reshape(-1)
     problem.apply_dirichlet(res, dofs, None)
     return res
 
@@ -111,7 +109,9 @@ def line_search(problem, dofs, inc):
     def res_norm(alpha):
         d = dofs.clone()
         _capi.check(problem.lib.cpfem_axpy(d.numel(), float(alpha), _dev_ptr(inc), _dev_ptr(d), _stream()))
-        return norm(problem, residual_bc(problem, d))
+        # a trial step may drive local solves non-finite; its norm then compares false,
+        # exactly as NaN does in the reference's loop
+        return norm(problem, residual_bc(problem, d, check=False))
     alpha = 1.0
     rn = res_norm(alpha)
     for _ in range(3):

@@ -147,3 +147,51 @@ def test_product_code_never_imports_the_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".cpp")):
                 src = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in src.replace("oracle/_ref", ""), f
+
+
+def _sell(lib, rp, cols, tpos, n):
+    slots = np.zeros(1, np.int64)
+    assert lib.cpfem_sell_count(n, rp.ctypes.data, slots.ctypes.data) == 0
+    S = int(slots[0])
+    ng = (n + 31) // 32
+    goff = np.zeros(ng + 1, np.int64)
+    gw = np.zeros(ng, np.int32)
+    sc = np.zeros(S, np.int32)
+    st = np.zeros(S, np.int32)
+    ds = np.zeros(n, np.int32)
+    assert lib.cpfem_sell_build(n, rp.ctypes.data, cols.ctypes.data, tpos.ctypes.data, goff.ctypes.data,
+                                gw.ctypes.data, sc.ctypes.data, st.ctypes.data, ds.ctypes.data) == 0
+    m = np.zeros(9 * cols.size, np.int64)
+    assert lib.cpfem_sell_csr_map(n, rp.ctypes.data, goff.ctypes.data, m.ctypes.data) == 0
+    return goff, gw, sc, st, ds, m
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (5, 4, 3)])
+def test_sell_layout_reproduces_csr_products(lib, pkg, shape):
+    """The sliced-ELL indexing the kernels use, replayed in numpy: A x, A^T x, the
+    diagonal blocks and a Dirichlet row all agree with scipy on the scalar CSR."""
+    m = pkg.box_mesh(*shape)
+    n = m.points.shape[0]
+    rp, cols, epos, tpos, indptr, indices = _pattern(lib, m.cells, n)
+    goff, gw, sc, st, ds, cmap = _sell(lib, rp, cols, tpos, n)
+    rng = np.random.default_rng(1)
+    data = rng.normal(size=indices.size)
+    A = sp.csr_array((data, indices, indptr), shape=(3 * n, 3 * n))
+    vals = np.zeros(9 * goff[-1])
+    vals[cmap] = data
+    assert np.unique(cmap).size == cmap.size
+    x = rng.normal(size=3 * n)
+    y, yt = np.zeros(3 * n), np.zeros(3 * n)
+    for a in range(n):
+        g, lane = a >> 5, a & 31
+        for j in range(gw[g]):
+            b = sc[goff[g] + 32 * j + lane]
+            for i in range(3):
+                for k in range(3):
+                    y[3 * a + i] += vals[9 * goff[g] + 32 * (9 * j + 3 * i + k) + lane] * x[3 * b + k]
+                    tp = st[goff[g] + 32 * j + lane]
+                    yt[3 * a + i] += vals[9 * goff[b >> 5] + 32 * (9 * tp + 3 * k + i) + (b & 31)] * x[3 * b + k]
+        for i in range(3):
+            assert vals[9 * goff[g] + 32 * (9 * ds[a] + 4 * i) + lane] == A[3 * a + i, 3 * a + i]
+    assert np.allclose(y, A @ x, rtol=1e-13, atol=1e-12)
+    assert np.allclose(yt, A.T @ x, rtol=1e-13, atol=1e-12)

@@ -131,3 +131,21 @@ def test_box_mesh_matches_package(pkg):
     sg2, jxw2 = pkg.mesh.shape_grads_jxw(m)
     assert np.abs(sg - sg2).max() < 1e-14 and np.abs(jxw - jxw2).max() < 1e-15
     assert abs(jxw.sum() - 6.0) < 1e-12
+
+
+def test_euler_generators_match_finite_differences(pkg):
+    from importlib import import_module
+    adj = import_module("jax-cpfem_gb300.adjoint")
+    ang = np.random.default_rng(9).uniform(-90, 90, size=(4, 3))
+    W = adj._euler_generators(ang)
+    R0 = pkg.material.euler_zyx_deg(ang)
+    for k in range(3):
+        d = np.zeros(3)
+        d[k] = 1e-5
+        dR = (pkg.material.euler_zyx_deg(ang + d) - pkg.material.euler_zyx_deg(ang - d)) / 2e-5
+        Wfd = dR @ np.swapaxes(R0, -1, -2)
+        w = W[:, k]
+        skew = np.zeros((4, 3, 3))
+        skew[:, 0, 1], skew[:, 0, 2], skew[:, 1, 2] = -w[:, 2], w[:, 1], -w[:, 0]
+        skew = skew - np.swapaxes(skew, -1, -2)
+        assert np.abs(skew - Wfd).max() < 1e-8
