@@ -278,6 +278,24 @@ int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double*
                    void* workspace, int32_t* info, void* stream);
 
 /*
+ * Allocation-free BiCGSTAB.  No reference counterpart: the reference's jax_solve
+ * (crystal_plasticity_OR_design/solver.py:19-48) lets JAX allocate.  Same solver and
+ * arguments as cpfem_bicgstab, but the scratch is a fixed device array inside the library
+ * (every GPU that loads it keeps CPFEM_NOALLOC_SCRATCH_BYTES until the process exits), for
+ * callers that cannot allocate device memory -- host codes that own all device memory
+ * through their own pool, or loops that must not allocate.  Limit: num_nodes <=
+ * CPFEM_NOALLOC_MAX_NODES, else CPFEM_ERR_SIZE with a message.  The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Every call shares the one array, so calls that overlap on
+ * the GPU (other streams or threads) race; serialise them.  Calls no cudaMalloc/cudaFree.
+ */
+#define CPFEM_NOALLOC_MAX_NODES 65536
+#define CPFEM_NOALLOC_SCRATCH_BYTES (20u * 1024u * 1024u)
+int cpfem_bicgstab_noalloc(const cpfem_sell_t* sell, const double* values, const double* b,
+                           double* x, int32_t precond, int32_t transpose, double tol, double atol,
+                           int32_t maxiter, int32_t* info, void* stream);
+
+/*
  * Ragged batch of independent systems (block-diagonal A over instances, instance i owning
  * nodes [node_off[i], node_off[i+1])): BiCGSTAB per instance with its own scalars and
  * its own stop test, one CTA per instance pulled from a work queue (list `active`, best

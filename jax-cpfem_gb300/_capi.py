@@ -126,6 +126,7 @@ SIGNATURES = {
     "cpfem_spmv": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _P]),
     "cpfem_bicgstab_workspace_bytes": (ctypes.c_size_t, [_I32]),
     "cpfem_bicgstab": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P, _P]),
+    "cpfem_bicgstab_noalloc": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P]),
     "cpfem_bicgstab_batched_workspace_bytes": (ctypes.c_size_t, [_I32]),
     "cpfem_bicgstab_batched": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _D, _D, _I32, _I32, _P, _P, _P, _P, _P]),
     "cpfem_probe_dfma": (ctypes.c_int, [_I64, _I32, _P, _P, _P]),

@@ -12,6 +12,7 @@
 // and take the same branch.  Barrier waits are bounded: a block that waits too long sets
 // an error flag and the solve returns CPFEM_ERR_SOLVE.
 #include <algorithm>
+#include <string>
 
 #include "cpfem_common.cuh"
 #include "reduce.cuh"
@@ -663,3 +664,65 @@ int cpfem_bicgstab_batched(const cpfem_sell_t* sell, const double* values, const
 }
 
 }  // extern "C"
+
+// ---- allocation-free variant ---------------------------------------------------------
+// Some callers cannot allocate device memory at all: a host code that owns every device
+// byte through its own pool, or a caller that must not grow its footprint inside a
+// real-time loop.  cpfem_bicgstab_noalloc gives them the same solver with its scratch
+// (Krylov vectors, preconditioner, reduction partials, barrier words) in a fixed
+// file-scope device array, sized for CPFEM_NOALLOC_MAX_NODES nodes.  The array lives in
+// every GPU that loads the library until the process exits.
+#include <mutex>
+
+namespace cpfem {
+
+constexpr int64_t kNoAllocMaxNodes = CPFEM_NOALLOC_MAX_NODES;
+
+static size_t noalloc_bytes_needed() { return carve(nullptr, kNoAllocMaxNodes, nullptr); }
+
+// 256-byte aligned scratch; its size is fixed at compile time from the carve layout of
+// kNoAllocMaxNodes nodes (checked again at run time).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[CPFEM_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[256] = {nullptr};
+
+// Device address of the scratch on the current device.  Host code must not use the
+// symbol's name as an address: it is a host-side stand-in.  Resolved once per device.
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  CPFEM_CUDA_TRY(cudaGetDevice(&dev));
+  CPFEM_REQUIRE(dev >= 0 && dev < 256, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* ptr = nullptr;
+    CPFEM_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+    CPFEM_REQUIRE(ptr != nullptr && ((uintptr_t)ptr & 255) == 0, "scratch address is not 256-byte aligned");
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CPFEM_OK;
+}
+
+}  // namespace cpfem
+
+extern "C" int cpfem_bicgstab_noalloc(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
+                                      int32_t precond, int32_t transpose, double tol, double atol,
+                                      int32_t maxiter, int32_t* info, void* stream) {
+  using namespace cpfem;
+  CPFEM_REQUIRE(info != nullptr, "info is null");
+  info[0] = 0;
+  info[1] = 1;
+  CPFEM_REQUIRE(sell_ok(sell), "bad layout");
+  if (sell->num_nodes > kNoAllocMaxNodes) {
+    set_error("cpfem_bicgstab_noalloc: " + std::to_string(sell->num_nodes) + " nodes exceed the fixed scratch of " +
+              std::to_string((long long)kNoAllocMaxNodes) + " nodes; use cpfem_bicgstab with a caller workspace");
+    return CPFEM_ERR_SIZE;
+  }
+  CPFEM_REQUIRE(noalloc_bytes_needed() <= sizeof(g_noalloc_scratch), "scratch smaller than its layout");
+  void* ws = nullptr;
+  int rc = noalloc_scratch(&ws);
+  if (rc != CPFEM_OK) return rc;
+  // run_bicgstab clears the barrier words and writes every vector before reading it
+  return cpfem_bicgstab(sell, values, b, x, precond, transpose, tol, atol, maxiter, ws, info, stream);
+}
