@@ -34,11 +34,15 @@ N_EDGE, N_GRAINS, SEED = 32, 64, 0
 STRAIN_STEP, DT = 1e-3, 0.1
 
 
-def workload_config(n=N_EDGE):
-    return {"workload": f"fcc-polycrystal-{n}^3-{N_GRAINS}grains-304steel-tension",
-            "cells": n ** 3, "gauss_points": 8 * n ** 3, "dofs": 3 * (n + 1) ** 3, "grains": N_GRAINS,
+def workload_config(n=N_EDGE, config="c1"):
+    name = {"c0": f"fcc-single-crystal-{n}^3-copper-tension",
+            "c2": f"bcc24-polycrystal-{n}^3-512grains-tantalum-tension"}.get(
+        config, f"fcc-polycrystal-{n}^3-{N_GRAINS}grains-304steel-tension")
+    grains = {"c0": 1, "c2": 512}.get(config, N_GRAINS)
+    return {"workload": name,
+            "cells": n ** 3, "gauss_points": 8 * n ** 3, "dofs": 3 * (n + 1) ** 3, "grains": grains,
             "strain_per_step": STRAIN_STEP, "dt_s": DT, "bcs": "rollers x=0,y=0,z=0; u_z(top)",
-            "linear_solver": "BiCGSTAB+Jacobi tol=atol=1e-10", "newton": "tol 1e-6 / rel_tol 1e-8",
+            "linear_solver": "BiCGSTAB tol=atol=1e-10", "newton": "tol 1e-6 / rel_tol 1e-8",
             "l2": "working set > L2 (state+tangent+CSR ~0.4 GB per step)"}
 
 
@@ -66,6 +70,7 @@ class Stepper:
     def __init__(self, pkg, prob, solver_mod, mesh):
         self.pkg, self.prob, self.solver, self.mesh = pkg, prob, solver_mod, mesh
         self.i = 0
+        self.precond = 1
         self.params = prob.internal_vars
         import torch
         self.sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
@@ -82,7 +87,8 @@ class Stepper:
             guess = sol_h.to("cuda", non_blocking=True)
         else:
             guess = self.sol
-        sol = self.solver.solver(prob, {"jax_solver": {}, "initial_guess": [guess.reshape(-1, 3)]})[0]
+        sol = self.solver.solver(prob, {"jax_solver": {"precond": self.precond},
+                                        "initial_guess": [guess.reshape(-1, 3)]})[0]
         sig = prob.compute_avg_stress(sol, self.params)
         self.params = prob.update_int_vars_gp(sol, self.params)
         self.sol = sol.reshape(-1)
@@ -389,6 +395,8 @@ def main():
     ap.add_argument("--load-steps", type=int, default=0)
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--fd-check", action="store_true")
+    ap.add_argument("--precond", type=int, default=1, choices=[0, 1, 2],
+                    help="BiCGSTAB preconditioner: 1 Jacobi (the reference), 2 3x3 block-Jacobi")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -429,6 +437,7 @@ def main():
         mesh, quat, ori = make_case(pkg, n)
     prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=spec)
     st = Stepper(pkg, prob, solver_mod, mesh)
+    st.precond = args.precond
     clk = ClockSampler(local).start()
     time.sleep(1.0)
     for _ in range(args.warmup):
@@ -506,14 +515,15 @@ def main():
     dominant = spmv_roof if kr_share >= gp_share else gp_roof
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.config == "c1":
         kps = sum(max(k, 0) for k in krylov) / args.steps
         cpu = cpu_baseline_sample(pkg, mesh, quat, ori, passes / args.steps, kps)
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": dict(workload_config(n), parallelism="replicas" if world > 1 else "single-gpu"),
+           "config": dict(workload_config(n, args.config), parallelism="replicas" if world > 1 else "single-gpu",
+                          precond={0: "none", 1: "jacobi", 2: "block-jacobi-3x3"}[args.precond]),
            "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
            "roofline": dominant, "roofline_kernels": {"spmv": spmv_roof, "gp_eval": gp_roof},
            "cpu_baseline": cpu,

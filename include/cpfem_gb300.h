@@ -218,8 +218,17 @@ int cpfem_gp_vjp(const cpfem_material_t* mat, const cpfem_vjp_args_t* args, void
  */
 int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* shape_grads,
                         const cpfem_sell_t* sell, const uint8_t* elem_pos,
+                        const int32_t* cell_list, int32_t num_listed,
                         const double* pk1_w, const double* tangent_w,
                         double* residual, double* values, void* stream);
+/* With cell_list == NULL every cell is scattered with FP64 atomics (summation order not
+ * fixed).  With a list of cells that share no node (one colour of cpfem_color_cells) the
+ * listed cells add without atomics; calling the colours in order gives a bitwise
+ * reproducible assembly. */
+
+/* Greedy cell colouring (host): cells of one colour share no node.  color [num_cells]. */
+int cpfem_color_cells(int32_t num_cells, const int32_t* cells, int32_t num_nodes, int32_t* color,
+                      int32_t* num_colors);
 
 /*
  * Row elimination: residual[d] = u[d] - val for every Dirichlet dof d, and (values != NULL)

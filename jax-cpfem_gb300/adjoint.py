@@ -176,9 +176,7 @@ class LoadHistory:
             fb = self._vjp(1, u, fpi, g, cell_bar, lam_fp, lam_g)["f_bar"]
             f_u = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
             fe = p.fes[0]
-            _capi.check(p.lib.cpfem_elem_assemble(p.num_cells, fe.cells.data_ptr(), fe.shape_grads.data_ptr(),
-                                                  p.sell, p.elem_pos.data_ptr(), fb.data_ptr(), None,
-                                                  f_u.data_ptr(), None, _stream()))
+            p.scatter(fb, None, f_u, None)
             # 2. the step's tangent, row-eliminated, and the transposed solve
             res, A = _solver.newton_update_helper(p, u)
             mu0 = torch.zeros_like(f_u)

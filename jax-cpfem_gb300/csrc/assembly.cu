@@ -167,8 +167,9 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
 // ------------------------------------------------------------------------------------
 // Element residual / tangent: one thread per (cell, node a) owns rows (a, 0..2).
 // ------------------------------------------------------------------------------------
-template <bool WITH_K>
-__global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ cells,
+template <bool WITH_K, bool ATOMIC>
+__global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ clist,
+                                                       int32_t ncl, const int32_t* __restrict__ cells,
                                                        const double* __restrict__ sg,
                                                        const int64_t* __restrict__ goff,
                                                        const uint8_t* __restrict__ epos,
@@ -177,9 +178,10 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
                                                        double* __restrict__ res,
                                                        double* __restrict__ vals) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t e = tid >> 3;
+  const int64_t li = tid >> 3;
   const int a = (int)(tid & 7);
-  if (e >= E) return;
+  if (li >= ncl) return;
+  const int64_t e = (clist != nullptr) ? clist[li] : li;
   const int64_t G = (int64_t)E * 8;
   double K[3][24];
   double Rr[3] = {0.0, 0.0, 0.0};
@@ -219,9 +221,13 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
     }
   }
   const int64_t na = cells[e * 8 + a];
+  // a conflict-free cell list (one colour) adds without atomics, in a fixed order
   if (res != nullptr)
 #pragma unroll
-    for (int i = 0; i < 3; ++i) atomicAdd(&res[3 * na + i], Rr[i]);
+    for (int i = 0; i < 3; ++i) {
+      if (ATOMIC) atomicAdd(&res[3 * na + i], Rr[i]);
+      else res[3 * na + i] += Rr[i];
+    }
   if (WITH_K) {
     // sliced-ELL slot of (node na, neighbour b): 9*goff[g] + 32*(9*pos + 3i + k) + lane
     const int64_t base = 9 * goff[na >> 5] + (na & 31);
@@ -231,7 +237,11 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) atomicAdd(&vals[base + 32 * (9 * pos + 3 * i + k)], K[i][3 * b + k]);
+        for (int k = 0; k < 3; ++k) {
+          double* v = &vals[base + 32 * (9 * pos + 3 * i + k)];
+          if (ATOMIC) atomicAdd(v, K[i][3 * b + k]);
+          else *v += K[i][3 * b + k];
+        }
     }
   }
 }
@@ -359,21 +369,35 @@ int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void
 }
 
 int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* shape_grads,
-                        const cpfem_sell_t* sell, const uint8_t* elem_pos, const double* pk1_w,
-                        const double* tangent_w, double* residual, double* values, void* stream) {
+                        const cpfem_sell_t* sell, const uint8_t* elem_pos, const int32_t* cell_list,
+                        int32_t num_listed, const double* pk1_w, const double* tangent_w, double* residual,
+                        double* values, void* stream) {
   if (num_cells == 0) return CPFEM_OK;
   CPFEM_REQUIRE(num_cells > 0 && cells && shape_grads && pk1_w, "bad element arguments");
   CPFEM_REQUIRE((values == nullptr) == (tangent_w == nullptr), "values and tangent_w go together");
   CPFEM_REQUIRE(values == nullptr || (sell && sell->group_off && elem_pos), "values need the layout");
+  CPFEM_REQUIRE(cell_list == nullptr || (num_listed >= 0 && num_listed <= num_cells), "bad cell list");
+  const int32_t ncl = (cell_list != nullptr) ? num_listed : num_cells;
+  if (ncl == 0) return CPFEM_OK;
   const int threads = 128;
-  const unsigned blocks = (unsigned)ceil_div((int64_t)num_cells * 8, threads);
+  const unsigned blocks = (unsigned)ceil_div((int64_t)ncl * 8, threads);
   cudaStream_t s = (cudaStream_t)stream;
-  if (values != nullptr)
-    k_elem_assemble<true><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, sell->group_off, elem_pos,
-                                                    pk1_w, tangent_w, residual, values);
-  else
-    k_elem_assemble<false><<<blocks, threads, 0, s>>>(num_cells, cells, shape_grads, nullptr, elem_pos,
-                                                     pk1_w, nullptr, residual, nullptr);
+  const int64_t* goff = (values != nullptr) ? sell->group_off : nullptr;
+  if (cell_list != nullptr) {
+    if (values != nullptr)
+      k_elem_assemble<true, false><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads, goff,
+                                                             elem_pos, pk1_w, tangent_w, residual, values);
+    else
+      k_elem_assemble<false, false><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads,
+                                                              nullptr, elem_pos, pk1_w, nullptr, residual, nullptr);
+  } else {
+    if (values != nullptr)
+      k_elem_assemble<true, true><<<blocks, threads, 0, s>>>(num_cells, nullptr, ncl, cells, shape_grads, goff,
+                                                            elem_pos, pk1_w, tangent_w, residual, values);
+    else
+      k_elem_assemble<false, true><<<blocks, threads, 0, s>>>(num_cells, nullptr, ncl, cells, shape_grads, nullptr,
+                                                             elem_pos, pk1_w, nullptr, residual, nullptr);
+  }
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;
 }

@@ -205,3 +205,32 @@ int cpfem_sell_csr_map(int32_t num_nodes, const int32_t* node_rowptr, const int6
 }
 
 }  // extern "C"
+
+// ---- element colouring for a deterministic, atomic-free scatter -----------------------
+extern "C" int cpfem_color_cells(int32_t num_cells, const int32_t* cells, int32_t num_nodes, int32_t* color,
+                                 int32_t* num_colors) {
+  int rc = check_cells(num_cells, cells, num_nodes);
+  if (rc) return rc;
+  if (!color || !num_colors) {
+    cpfem::set_error("bad colouring arguments");
+    return CPFEM_ERR_ARG;
+  }
+  // greedy in cell order: the smallest colour not held by a cell sharing a node
+  std::vector<uint64_t> node_mask((size_t)num_nodes, 0);
+  int32_t nc = 0;
+  for (int32_t e = 0; e < num_cells; ++e) {
+    uint64_t used = 0;
+    for (int k = 0; k < 8; ++k) used |= node_mask[cells[8 * (int64_t)e + k]];
+    int c = 0;
+    while (c < 64 && (used >> c) & 1u) ++c;
+    if (c >= 64) {
+      cpfem::set_error("more than 64 colours needed");
+      return CPFEM_ERR_SIZE;
+    }
+    color[e] = c;
+    nc = std::max(nc, c + 1);
+    for (int k = 0; k < 8; ++k) node_mask[cells[8 * (int64_t)e + k]] |= (uint64_t)1 << c;
+  }
+  *num_colors = nc;
+  return CPFEM_OK;
+}

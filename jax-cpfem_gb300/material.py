@@ -111,6 +111,8 @@ CALIB_CASE4 = MaterialSpec(  # calibration/case4.py (304 steel, FCC)
     gss_a=8.0, xm=1.0 / 120.0, r=1.0, slip="fcc12", coplanar_q=False, per_gp_params=True,
     local_tol=1e-8, max_sub_step=8)
 SENS_ROT = COPPER.replace(coplanar_q=False, per_gp_params=True, local_tol=1e-6, max_sub_step=10)
+STEEL304 = CALIB_CASE4.replace(coplanar_q=True, per_gp_params=False)   # polycrystal_304steel/models_304steel.py
+TANTALUM = CALIB_CASE2.replace(coplanar_q=True, per_gp_params=False)   # singlecrystal_tantalum/models_tantalum.py
 
 # The benchmark configurations (GPa in the specification, MPa here).
 BENCH_COPPER = MaterialSpec(
@@ -177,4 +179,4 @@ def check_orthonormal(R, tol=1e-10):
 
 __all__ = ["MaterialSpec", "FCC12", "BCC12", "BCC24", "SLIP_SYSTEMS", "rot_mat", "euler_zyx_deg",
            "random_quaternions", "check_orthonormal", "COPPER", "CALIB_CASE1", "CALIB_CASE2",
-           "CALIB_CASE4", "SENS_ROT", "BENCH_COPPER", "BENCH_STEEL", "BENCH_TANTALUM"]
+           "CALIB_CASE4", "SENS_ROT", "STEEL304", "TANTALUM", "BENCH_COPPER", "BENCH_STEEL", "BENCH_TANTALUM"]

@@ -72,6 +72,7 @@ class FiniteElement:
         self.node_inds_list, self.vec_inds_list, self.vals_list = [], [], []
         self.bc_dofs = torch.zeros(0, dtype=torch.int32, device=device)
         self.bc_vals = torch.zeros(0, dtype=torch.float64, device=device)
+        self.bc_token = 0
         if dirichlet_bc_info is not None:
             self.update_Dirichlet_boundary_conditions(dirichlet_bc_info)
 
@@ -108,6 +109,7 @@ class FiniteElement:
             dofs, vals = np.zeros(0, np.int64), np.zeros(0)
         self.bc_dofs = torch.tensor(dofs, dtype=torch.int32, device=self.device)
         self.bc_vals = torch.tensor(vals, dtype=torch.float64, device=self.device)
+        self.bc_token = getattr(self, "bc_token", 0) + 1
 
 
 class DeviceCSR:
@@ -194,6 +196,8 @@ class CrystalPlasticity:
         self._build_pattern()
         self._bufs = {}
         self._post_cache = None
+        self._trial = None
+        self._state_token = 0
         self.stats = {"gp_passes": 0, "krylov_iters": [], "local_iters_max": 0}
         self.timing = False
         self.timers = {}
@@ -238,6 +242,15 @@ class CrystalPlasticity:
                                                      ("group_off", "group_width", "cols", "tpos", "diag_slot")))
         self.elem_pos = torch.tensor(epos, device=dev)
         self._csr_map = None
+        # colours of a deterministic scatter (cells of one colour share no node)
+        color = np.zeros(self.num_cells, dtype=np.int32)
+        nc = np.zeros(1, dtype=np.int32)
+        _capi.check(self.lib.cpfem_color_cells(self.num_cells, cells.ctypes.data, self.num_nodes,
+                                               color.ctypes.data, nc.ctypes.data))
+        order = np.argsort(color, kind="stable").astype(np.int32)
+        counts = np.bincount(color, minlength=int(nc[0]))
+        self.color_cells = torch.tensor(order, device=dev)
+        self.color_ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
 
     def csr_map(self):
         """Index of every scalar-CSR value (scipy's order) in the sliced-ELL values."""
@@ -287,6 +300,8 @@ class CrystalPlasticity:
         self.slip = torch.zeros((N, G), dtype=torch.float64, device=dev)
         self._views = None
         self._post_cache = None
+        self._trial = None
+        self._state_token = getattr(self, "_state_token", 0) + 1
 
     # ------------------------------------------------------------------ state views
     def _make_views(self):
@@ -312,7 +327,18 @@ class CrystalPlasticity:
 
     def set_params(self, params):
         """Adopt a reference-shaped internal-variable list (``models_copper.py:284-285``)."""
-        self._adopt(params)
+        if not self._is_adopted(params):
+            self._adopt(params)
+
+    def _is_adopted(self, params):
+        """True when ``params`` are the very objects (unchanged) last adopted or handed out."""
+        key = (tuple(id(p) for p in params), tuple(getattr(p, "_version", 0) for p in params))
+        if key == getattr(self, "_adopted_key", None):
+            return True
+        if self._views is not None and len(params) == len(self._views) and \
+                all(p is q for p, q in zip(params, self._views)):
+            return True
+        return False
 
     def _soa(self, t, width):
         t = torch.as_tensor(t, dtype=torch.float64, device=self.device)
@@ -348,7 +374,11 @@ class CrystalPlasticity:
         # keep the caller's objects for the entries adopted as they are
         self._views = [params[k] if (k >= 3 and old is not None and params[k] is old[k]) else new_views[k]
                        for k in range(len(params))]
+        self._adopted_key = (tuple(id(p) for p in params), tuple(getattr(p, "_version", 0) for p in params))
+        self._adopted_ref = list(params)   # keeps the ids valid while the key is held
         self._post_cache = None
+        self._trial = None
+        self._state_token = getattr(self, "_state_token", 0) + 1
 
     def set_initial_guess(self, initial_sol):
         """``models_sens_rot.py:287-288``."""
@@ -426,20 +456,38 @@ class CrystalPlasticity:
             values.zero_()
             dw = self._buf("tangent_w", (81, G))
         its = self._buf("iters", (G,), torch.int32) if self.timing else None
+        trial = {}
+        if need_tangent:
+            # the trial state and stress of this pass are the post-processing of the step if
+            # it turns out to be the converged one (models_copper.py:273-282,297-319 re-solve)
+            N = self.num_slip
+            trial = {"stress": torch.empty((9, G), dtype=torch.float64, device=self.device),
+                     "fpi_new": torch.empty((9, G), dtype=torch.float64, device=self.device),
+                     "g_new": torch.empty((N, G), dtype=torch.float64, device=self.device),
+                     "slip_new": torch.empty((N, G), dtype=torch.float64, device=self.device)}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its)
+                             iters=its, **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
         if its is not None and need_tangent:
             acc = self._bufs.setdefault("iters_acc", torch.zeros(2, dtype=torch.float64, device=self.device))
             acc[0] += its.sum()
             acc[1] += G
-        fe = self.fes[0]
-        with self.region("elem_assemble"):
-            _capi.check(self.lib.cpfem_elem_assemble(self.num_cells, _dev_ptr(fe.cells), _dev_ptr(fe.shape_grads),
-                                                     self.sell, _dev_ptr(self.elem_pos),
-                                                     _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res), _dev_ptr(values),
-                                                     _stream()))
+        self.scatter(pw, dw, res, values)
+        if trial:
+            self._trial = (self._trial_key(u), u, trial, status)
         return res, values, status
+
+    def scatter(self, pw, dw, res, values):
+        """Element residual / tangent scatter, colour by colour (no atomics, fixed order)."""
+        fe = self.fes[0]
+        base = self.color_cells.data_ptr()
+        with self.region("elem_assemble"):
+            for c in range(len(self.color_ptr) - 1):
+                c0, c1 = int(self.color_ptr[c]), int(self.color_ptr[c + 1])
+                _capi.check(self.lib.cpfem_elem_assemble(self.num_cells, _dev_ptr(fe.cells), _dev_ptr(fe.shape_grads),
+                                                         self.sell, _dev_ptr(self.elem_pos), base + 4 * c0, c1 - c0,
+                                                         _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res),
+                                                         _dev_ptr(values), _stream()))
 
     def apply_dirichlet(self, res, u, values=None):
         fe = self.fes[0]
@@ -512,19 +560,34 @@ class CrystalPlasticity:
         state = [fn.t().reshape(*lead, 3, 3), gn.t().reshape(*lead, N), sn.t().reshape(*lead, N)]
         return out_P, out_D, state, its.reshape(lead)
 
+    def _trial_key(self, u):
+        return (u.data_ptr(), u._version, self._state_token, float(self.dt),
+                tuple(id(t) for t in self._state()), self.fes[0].bc_token)
+
     def _post_pass(self, sol, params):
         """One constitutive pass at the converged solution giving both the per-cell
         Cauchy stress and the new internal variables (the reference runs the local
-        solve once for each, ``models_copper.py:273-282,297-319``)."""
+        solve once for each, ``models_copper.py:273-282,297-319``).  When the last
+        tangent assembly ran at this very solution and state, its trial outputs are used
+        and no constitutive pass is needed."""
         u = _flat([sol], self.device)
-        key = (u.data_ptr(), u._version, tuple(id(p) for p in params),
-               tuple(getattr(p, "_version", 0) for p in params), float(self.dt))
+        if not self._is_adopted(params):
+            self._adopt(params)
+        key = self._trial_key(u)
         if self._post_cache is not None and self._post_cache[0] == key:
             return self._post_cache[1]
-        if self._views is None or len(params) != len(self._views) or \
-                any(p is not q for p, q in zip(params, self._views)):
-            self._adopt(params)
         G, N = self.num_gp, self.num_slip
+        if self._trial is not None and self._trial[0] == key:
+            _, _, tr, status = self._trial
+            sig = torch.empty((self.num_cells, 3, 3), dtype=torch.float64, device=self.device)
+            _capi.check(self.lib.cpfem_cell_average(self.num_cells, _dev_ptr(self.fes[0].JxW),
+                                                    _dev_ptr(tr["stress"]), _dev_ptr(sig), _stream()))
+            self._check_status(status)
+            E = self.num_cells
+            new = [tr["fpi_new"].t().reshape(E, 8, 3, 3), tr["g_new"].t().reshape(E, 8, N),
+                   tr["slip_new"].t().reshape(E, 8, N)] + list(params[3:])
+            self._post_cache = (key, (sig, new))
+            return sig, new
         sw = self._buf("stress_w", (9, G))
         fn = torch.empty((9, G), dtype=torch.float64, device=self.device)
         gn = torch.empty((N, G), dtype=torch.float64, device=self.device)

@@ -7,8 +7,12 @@ Reads (paths relative to the reference project root):
   calibration/data/csv/calibration_case4/UQ/stress_xx_curve_scenario1.txt  mean sigma_xx, x-loaded twin
   calibration/data/csv/calibration_case4/quat.txt                         orientations (rows 0..49)
   calibration/data/neper/calibration_case4/UQ/n50-id0.msh                 grain of every voxel cell
-and writes ``golden.npz``.  The 20^3 Neper mesh is checked to be the structured box of
-side 0.0295 with x-fastest node numbering, so only its per-cell grain ids are stored.
+  polycrystal_304steel/data/vtk/polycrystal_304steel/u_000..015.vtu     per-cell stresses, 16^3, 8 grains
+  polycrystal_304steel/data/csv/polycrystal_304steel/quat.txt            its orientations
+  singlecrystal_tantalum/data/vtk/singlecrystal_tantalum/u_000..049.vtu  per-cell stresses, 10^3 single crystal
+and writes ``golden.npz``.  The Neper meshes (20^3 of case 4, 16^3 of the 304-steel VTUs,
+10^3 of the tantalum VTUs) are checked to be structured boxes with x-fastest node
+numbering, so only per-cell grain ids are stored.  The VTU fields are float32 (meshio).
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -50,9 +54,25 @@ def main():
     bp, bc = box_mesh(20, 20, 20, 0.0295, 0.0295, 0.0295)
     assert np.abs(bp - pts).max() < 1e-9, "case4 mesh is not the structured box"
     assert (bc == cells).all(), "case4 connectivity differs from the structured box"
+    import importlib
+    vtu = importlib.import_module("jax-cpfem_gb300.vtu")
+    vdir = os.path.join(REF, "polycrystal_304steel/data/vtk/polycrystal_304steel")
+    st = [vtu.read_vtu(os.path.join(vdir, f"u_{i:03d}.vtu")) for i in range(16)]
+    bp, bc = box_mesh(16, 16, 16, 0.016, 0.016, 0.016)
+    assert np.abs(bp - st[0]["points"]).max() < 1e-12 and (bc == st[0]["cells"]).all()
+    steel_sig = np.stack([np.stack([r["cell_data"][f"sigma_{c}"] for c in ("xx", "yy", "zz")]) for r in st])
+    steel_ori = st[0]["cell_data"]["cell_ori_inds"].astype(np.int16)
+    steel_quat = np.loadtxt(os.path.join(REF, "polycrystal_304steel/data/csv/polycrystal_304steel/quat.txt"))[:8, 1:]
+    tdir = os.path.join(REF, "singlecrystal_tantalum/data/vtk/singlecrystal_tantalum")
+    ta = [vtu.read_vtu(os.path.join(tdir, f"u_{i:03d}.vtu")) for i in range(50)]
+    L = ta[0]["points"].max()
+    bp, bc = box_mesh(10, 10, 10, L, L, L)
+    assert np.abs(bp - ta[0]["points"]).max() < 1e-12 and (bc == ta[0]["cells"]).all()
+    ta_szz = np.stack([r["cell_data"]["sigma_zz"] for r in ta])
     np.savez_compressed(os.path.join(HERE, "golden.npz"), case1_szz=case1, case2_szz=case2,
                         case4_szz=c4zz, case4_sxx=c4xx, case4_quat=quat,
-                        case4_grain=grains.astype(np.int16))
+                        case4_grain=grains.astype(np.int16), steel_sig=steel_sig, steel_ori=steel_ori,
+                        steel_quat=steel_quat, ta_szz=ta_szz, ta_L=np.array(L))
     print("wrote golden.npz", case1.shape, case2.shape, c4zz.shape, c4xx.shape, quat.shape, grains.shape)
 
 

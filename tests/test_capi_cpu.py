@@ -195,3 +195,17 @@ def test_sell_layout_reproduces_csr_products(lib, pkg, shape):
             assert vals[9 * goff[g] + 32 * (9 * ds[a] + 4 * i) + lane] == A[3 * a + i, 3 * a + i]
     assert np.allclose(y, A @ x, rtol=1e-13, atol=1e-12)
     assert np.allclose(yt, A.T @ x, rtol=1e-13, atol=1e-12)
+
+
+@pytest.mark.parametrize("shape", [(4, 3, 2), (6, 6, 6)])
+def test_cell_colouring_is_conflict_free(lib, pkg, shape):
+    m = pkg.box_mesh(*shape)
+    cells = np.ascontiguousarray(m.cells, dtype=np.int32)
+    color = np.zeros(cells.shape[0], np.int32)
+    nc = np.zeros(1, np.int32)
+    assert lib.cpfem_color_cells(cells.shape[0], cells.ctypes.data, m.points.shape[0], color.ctypes.data,
+                                 nc.ctypes.data) == 0
+    assert nc[0] == 8
+    for c in range(nc[0]):
+        nodes = cells[color == c].ravel()
+        assert np.unique(nodes).size == nodes.size

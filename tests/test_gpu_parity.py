@@ -226,3 +226,44 @@ def test_nonfinite_state_is_reported(pkg, gpu):
     g[1, 3] = np.nan
     with pytest.raises((FloatingPointError, RuntimeError)):
         prob.gp_map(ug, fpi, g, slip, R)
+
+
+def test_golden_304steel_cell_stresses_on_gpu(pkg, gpu):
+    """polycrystal_304steel: 16^3 voxels, 8 grains, the reference's per-cell sigma_xx/yy/zz
+    of its first 16 VTU steps (float32 files; Newton tolerance 1e-6 in the reference)."""
+    problem_mod, solver_mod = gpu
+    L = 0.016
+    mesh = pkg.box_mesh(16, 16, 16, L, L, L)
+    prob = gpu_problem(pkg, problem_mod, pkg.material.STEEL304, mesh, GOLD["steel_quat"],
+                       GOLD["steel_ori"].astype(np.int64))
+    c = pkg.mesh.corner_nodes(mesh.points, (0.0, 0.0, L))
+    bcf = lambda d: [(c, 0, 0.0), (c, 1, 0.0), (pkg.mesh.face_nodes(mesh.points, 2, 0.0), 2, 0.0),
+                     (pkg.mesh.face_nodes(mesh.points, 2, L), 2, d)]
+    s, _ = _run_steps(prob, solver_mod, np.linspace(0, 0.01 * L, 51)[:17], np.linspace(0, 0.1, 51)[:17], bcf,
+                      {"jax_solver": {}}, lambda sg: np.stack([sg[:, 0, 0], sg[:, 1, 1], sg[:, 2, 2]]))
+    # The reference's BiCGSTAB stops at an absolute 1e-10 residual (solver.py:34-40); on this
+    # 0.016 mm mesh that is ~2e-6 of the right-hand side, so its per-cell fields carry
+    # ~1e-4 solver noise (the CPU oracle differs from the files by the same amount) while
+    # the volume averages agree closely.
+    gold = GOLD["steel_sig"]
+    for i in range(16):
+        scale = np.abs(gold[i][2]).max()
+        assert np.abs(s[i] - gold[i]).max() / scale < 2e-3, i
+        assert abs(s[i][2].mean() - gold[i][2].mean()) / abs(gold[i][2].mean()) < 1e-6, i
+
+
+def test_golden_tantalum_single_crystal_on_gpu(pkg, gpu):
+    """singlecrystal_tantalum: 10^3 cells, BCC12, compression to 1.25 % in 50 steps."""
+    problem_mod, solver_mod = gpu
+    L = float(GOLD["ta_L"])
+    mesh = pkg.box_mesh(10, 10, 10, L, L, L)
+    prob = gpu_problem(pkg, problem_mod, pkg.material.TANTALUM, mesh, [[1.0, 0.0, 0.0, 0.0]],
+                       np.zeros(1000, dtype=np.int64))
+    c = pkg.mesh.corner_nodes(mesh.points, (0.0, 0.0, L))
+    bcf = lambda d: [(c, 0, 0.0), (c, 1, 0.0), (pkg.mesh.face_nodes(mesh.points, 2, 0.0), 2, 0.0),
+                     (pkg.mesh.face_nodes(mesh.points, 2, L), 2, d)]
+    s, _ = _run_steps(prob, solver_mod, np.linspace(0, -0.0125 * L, 51), np.linspace(0, 12.5, 51), bcf,
+                      {"jax_solver": {}}, lambda sg: sg[:, 2, 2])
+    gold = GOLD["ta_szz"]
+    rel = np.abs(s - gold).max(1) / np.abs(gold).max(1)
+    assert rel.max() < 2e-6, rel
