@@ -85,6 +85,9 @@ typedef struct {
   const int32_t* rot_idx;     /* [num_gp] */
   const double* param_table;  /* [5*n_param] */
   const int32_t* param_idx;   /* [num_gp] or NULL (row 0 for every GP) */
+  const double* elastic_table; /* [3*n_param] (C11, C12, C44) per parameter row, or NULL for
+                                  the material's constants (per-phase stiffness,
+                                  polycrystal_DPsteel/models_DPsteel_inhomo.py:184-186) */
   double* pk1;                /* [9*num_gp]  first Piola-Kirchhoff stress P */
   double* tangent;            /* [81*num_gp] dP/dF */
   double* stress;             /* [9*num_gp]  Cauchy stress */
@@ -126,6 +129,7 @@ typedef struct {
   const int32_t* rot_idx;
   const double* param_table;
   const int32_t* param_idx;
+  const double* elastic_table;
   const double* cell_sig_bar;
   const double* fpi_bar;
   const double* g_bar;

@@ -55,6 +55,7 @@ class GPArgs(ctypes.Structure):
         ("rot_idx", ctypes.c_void_p),
         ("param_table", ctypes.c_void_p),
         ("param_idx", ctypes.c_void_p),
+        ("elastic_table", ctypes.c_void_p),
         ("pk1", ctypes.c_void_p),
         ("tangent", ctypes.c_void_p),
         ("stress", ctypes.c_void_p),
@@ -79,7 +80,7 @@ class VjpArgs(ctypes.Structure):
         ("pad", ctypes.c_int32),
     ] + [(name, ctypes.c_void_p) for name in (
         "u", "cells", "shape_grads", "jxw", "fpi", "g", "rot_table", "rot_idx", "param_table", "param_idx",
-        "cell_sig_bar", "fpi_bar", "g_bar", "mu", "f_bar", "fpi_bar_old", "g_bar_old", "theta_bar", "rot_bar",
+        "elastic_table", "cell_sig_bar", "fpi_bar", "g_bar", "mu", "f_bar", "fpi_bar_old", "g_bar_old", "theta_bar", "rot_bar",
         "status")]
 
 

@@ -132,6 +132,7 @@ class LoadHistory:
         a.rot_table, a.rot_idx = p.rot_table.data_ptr(), p.rot_idx.data_ptr()
         a.param_table = p.param_table.data_ptr()
         a.param_idx = _dev_ptr(p.param_idx)
+        a.elastic_table = _dev_ptr(p.elastic_table)
         a.cell_sig_bar = _dev_ptr(cell_sig_bar)
         a.fpi_bar, a.g_bar = _dev_ptr(lam_fp), _dev_ptr(lam_g)
         a.mu = _dev_ptr(mu)

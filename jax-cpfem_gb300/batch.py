@@ -11,8 +11,10 @@ semantics (``crystal_plasticity_OR_design/solver.py:407``): it stops iterating w
 """
 from __future__ import annotations
 
+import contextlib
 import dataclasses
 import math
+import time
 
 import numpy as np
 import torch
@@ -107,6 +109,19 @@ class Batch:
         self.sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=dev)
         self.params = p.internal_vars
         self.stats = {"newton_iters": [], "krylov_iters": []}
+        self.host_s = {}
+
+    @contextlib.contextmanager
+    def _phase(self, name):
+        """Wall-clock time of a solve phase (synchronised) when the problem is timing."""
+        if not self.problem.timing:
+            yield
+            return
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        yield
+        torch.cuda.synchronize()
+        self.host_s[name] = self.host_s.get(name, 0.0) + time.perf_counter() - t0
 
     def set_bcs(self, disp):
         nodes, comps, vals = [], [], []
@@ -128,8 +143,9 @@ class Batch:
         p = self.problem
         lib = p.lib
         dofs = self.sol.clone()
-        res, A = _solver.newton_update_helper(p, dofs)
-        r0 = self._norms(res)
+        with self._phase("assemble"):
+            res, A = _solver.newton_update_helper(p, dofs)
+            r0 = self._norms(res)
         rn = r0.copy()
         with np.errstate(invalid="ignore", divide="ignore"):
             active = (rn / r0 > rel_tol) & (rn > tol)
@@ -145,7 +161,7 @@ class Batch:
             act_dev = torch.tensor(act, device=p.device)
             b = torch.neg(res)
             x = _solver.initial_increment(p, dofs).clone()
-            with p.region("bicgstab_batched"):
+            with self._phase("krylov"), p.region("bicgstab_batched"):
                 _capi.check(lib.cpfem_bicgstab_batched(p.sell, A.values.data_ptr(), b.data_ptr(), x.data_ptr(),
                                                        int(precond), float(ktol), float(katol), int(maxiter),
                                                        int(act.size), act_dev.data_ptr(), self.node_off.data_ptr(),
@@ -156,8 +172,9 @@ class Batch:
             self.stats["krylov_iters"].append(inf[act, 0].copy())
             _capi.check(lib.cpfem_axpy(dofs.numel(), 1.0, x.data_ptr(), dofs.data_ptr(), _stream()))
             newton_count[act] += 1
-            res, A = _solver.newton_update_helper(p, dofs)
-            rn = self._norms(res)
+            with self._phase("assemble"):
+                res, A = _solver.newton_update_helper(p, dofs)
+                rn = self._norms(res)
             if not np.isfinite(rn).all():
                 raise FloatingPointError("non-finite residual in the batch")
             active = active & (rn / r0 > rel_tol) & (rn > tol)
@@ -169,25 +186,36 @@ class Batch:
         """One load step of every instance; returns the per-instance mean cell sigma_zz."""
         p = self.problem
         p.dt = float(dt)
-        self.set_bcs(disp)
-        p.set_params(self.params)
+        with self._phase("bcs"):
+            self.set_bcs(disp)
+            p.set_params(self.params)
         sol = self.solve()
-        sig = p.compute_avg_stress(sol.reshape(-1, 3), self.params)
-        self.params = p.update_int_vars_gp(sol.reshape(-1, 3), self.params)
+        with self._phase("post"):
+            sig = p.compute_avg_stress(sol.reshape(-1, 3), self.params)
+            self.params = p.update_int_vars_gp(sol.reshape(-1, 3), self.params)
         self.sol = sol
         szz = torch.zeros(self.n, dtype=torch.float64, device=p.device)
         szz.index_add_(0, self.inst_of_cell, sig[:, 2, 2])
         return szz / self.cells_per_inst
 
 
-def run_serial(instances, disps, dt, device=None):
-    """The same RVEs one at a time through the plain drop-in path."""
-    out = np.zeros((len(instances), len(disps)))
-    for k, it in enumerate(instances):
+def build_serial(instances, device=None):
+    """One plain drop-in problem per RVE (the set-up half of ``run_serial``)."""
+    out = []
+    for it in instances:
         mesh, quat, ori = build_instance(it)
         p = CrystalPlasticity(mesh, additional_info=(quat, ori), material=it.material, device=device)
         P = mesh.points
-        nodes = [face_nodes(P, 0, 0.0), face_nodes(P, 1, 0.0), face_nodes(P, 2, 0.0), face_nodes(P, 2, 1.0)]
+        out.append((p, [face_nodes(P, 0, 0.0), face_nodes(P, 1, 0.0), face_nodes(P, 2, 0.0), face_nodes(P, 2, 1.0)]))
+    return out
+
+
+def run_serial(instances, disps, dt, device=None, prepared=None):
+    """The same RVEs one at a time through the plain drop-in path (``prepared`` from
+    ``build_serial`` keeps the problem set-up out of a timed region)."""
+    prepared = prepared if prepared is not None else build_serial(instances, device)
+    out = np.zeros((len(prepared), len(disps)))
+    for k, (p, nodes) in enumerate(prepared):
         params = p.internal_vars
         sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
         for i, d in enumerate(disps):

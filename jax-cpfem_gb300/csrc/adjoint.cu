@@ -46,6 +46,12 @@ __global__ void __launch_bounds__(64) k_gp_vjp(const MatDev m, const cpfem_vjp_a
   for (int k = 0; k < 9; ++k) R[k] = a.rot_table[9 * ri + k];
 #pragma unroll
   for (int k = 0; k < 5; ++k) th[k] = a.param_table[5 * pi + k];
+  Cub cc{m.C11, m.C12, m.C44};
+  if (a.elastic_table != nullptr) {
+    cc.C11 = a.elastic_table[3 * pi];
+    cc.C12 = a.elastic_table[3 * pi + 1];
+    cc.C44 = a.elastic_table[3 * pi + 2];
+  }
 #pragma unroll
   for (int s = 0; s < NS; ++s) {
     g[s] = a.g[s * G + gp];
@@ -58,7 +64,7 @@ __global__ void __launch_bounds__(64) k_gp_vjp(const MatDev m, const cpfem_vjp_a
   mm3_at(AR, AR, Ct);
   const double cdt = m.ao * a.dt;
   GPSolve<NS> st;
-  cp_local_newton<NS>(m, Ct, ig, cdt, 1.0 / th[3], st);
+  cp_local_newton<NS>(m, cc, Ct, ig, cdt, 1.0 / th[3], st);
   // output cotangents
   constexpr int NY = YOut<NS>::kN;
   double ybar[NY];
@@ -101,7 +107,7 @@ __global__ void __launch_bounds__(64) k_gp_vjp(const MatDev m, const cpfem_vjp_a
   } else {
     for (int k = XIn<NS>::kFp; k < NX; ++k) dirs[ndir++] = k;
   }
-  const bool ok = cp_vjp<NS, kVjpK>(m, cdt, st.s, F, Fpi, g, R, th, ybar, dirs, ndir, xbar);
+  const bool ok = cp_vjp<NS, kVjpK>(m, cc, cdt, st.s, F, Fpi, g, R, th, ybar, dirs, ndir, xbar);
   if (a.status != nullptr) {
     int bits = 0;
     if (!(st.rn <= m.local_tol)) bits |= CPFEM_GP_MAXITER;

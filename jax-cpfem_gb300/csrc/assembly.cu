@@ -90,6 +90,12 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
   const double t_sat = a.param_table[5 * pi + 2];
   const double xm = a.param_table[5 * pi + 3];
   const double rq = a.param_table[5 * pi + 4];
+  Cub cc{m.C11, m.C12, m.C44};
+  if (a.elastic_table != nullptr) {
+    cc.C11 = a.elastic_table[3 * pi];
+    cc.C12 = a.elastic_table[3 * pi + 1];
+    cc.C44 = a.elastic_table[3 * pi + 2];
+  }
 
   double g[NS], ig[NS];
 #pragma unroll
@@ -103,7 +109,7 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
   mm3_at(AR, AR, Ct);
 
   GPSolve<NS> st;
-  cp_local_newton<NS>(m, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
+  cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
   if (a.status != nullptr) {
     int bits = 0;
     if (!(st.rn <= m.local_tol)) bits |= CPFEM_GP_MAXITER;
@@ -120,9 +126,9 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
     for (int c = 0; c < 9; ++c) tan[(int64_t)(9 * c + kl) * G + gp] = col[c] * w;
   };
   if (TANGENT && tan != nullptr)
-    cp_outputs<NS, true>(m, F, Gm, st, H, P, store);
+    cp_outputs<NS, true>(m, cc, F, Gm, st, H, P, store);
   else
-    cp_outputs<NS, false>(m, F, Gm, st, H, P, store);
+    cp_outputs<NS, false>(m, cc, F, Gm, st, H, P, store);
 
   if (a.pk1 != nullptr)
 #pragma unroll

@@ -107,9 +107,14 @@ CPFEM_HD void inv3(const double* A, double* Ai) {
   Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
 }
 
+// Cubic elastic constants of one Gauss point (the material's, or its phase's row).
+struct Cub {
+  double C11, C12, C44;
+};
+
 // Cubic stiffness applied to a symmetric tensor in 6-component form
 // (11,22,33,23,13,12), tensor components (not engineering shears).
-CPFEM_HD void cubic_apply(const MatDev& m, const double* e, double* t) {
+CPFEM_HD void cubic_apply(const Cub& m, const double* e, double* t) {
   t[0] = fma(m.C11, e[0], m.C12 * (e[1] + e[2]));
   t[1] = fma(m.C11, e[1], m.C12 * (e[0] + e[2]));
   t[2] = fma(m.C11, e[2], m.C12 * (e[0] + e[1]));

@@ -141,7 +141,7 @@ CPFEM_HD Dual<K> ddet3(const Dual<K>* A) {
 }
 
 template <int K>
-CPFEM_HD void dcubic(const MatDev& m, const Dual<K>* e, Dual<K>* t) {
+CPFEM_HD void dcubic(const Cub& m, const Dual<K>* e, Dual<K>* t) {
   t[0] = m.C11 * e[0] + m.C12 * (e[1] + e[2]);
   t[1] = m.C11 * e[1] + m.C12 * (e[0] + e[2]);
   t[2] = m.C11 * e[2] + m.C12 * (e[0] + e[1]);
@@ -178,7 +178,8 @@ CPFEM_HD Dual<K> seeded(const signed char* slot, int idx, double v) {
 // Returns the residual r (6 duals) and yb = sum_o ybar[o] y[o] over the output slots, so
 // the outputs never have to be live at once.
 template <int NS, int K>
-CPFEM_HD void cp_eval_dual(const MatDev& m, double cdt, const double* s0, const double* F0, const double* Fp0,
+CPFEM_HD void cp_eval_dual(const MatDev& m, const Cub& cc, double cdt, const double* s0, const double* F0,
+                           const double* Fp0,
                            const double* g0, const double* R0, const double* th0, const signed char* slot,
                            const double* ybar, Dual<K>* r6, Dual<K>& yb) {
 #define mk(idx, v) seeded<K>(slot, (idx), (v))
@@ -246,7 +247,7 @@ CPFEM_HD void cp_eval_dual(const MatDev& m, double cdt, const double* s0, const 
   e[3] = 0.5 * dfma(B[1], M[2], dfma(B[4], M[5], B[7] * M[8]));
   e[4] = 0.5 * dfma(B[0], M[2], dfma(B[3], M[5], B[6] * M[8]));
   e[5] = 0.5 * dfma(B[0], M[1], dfma(B[3], M[4], B[6] * M[7]));
-  dcubic<K>(m, e, t);
+  dcubic<K>(cc, e, t);
 #pragma unroll
   for (int i = 0; i < 6; ++i) r6[i] = s[i] - t[i];
   yb = dconst<K>(0.0);
@@ -297,7 +298,8 @@ CPFEM_HD void cp_eval_dual(const MatDev& m, double cdt, const double* s0, const 
 // slots are ignored); xbar receives the XIn<NS>::kN input cotangents for the directions
 // listed in dirs[0..ndir) (others untouched).  Returns false if J is singular.
 template <int NS, int K>
-CPFEM_HD bool cp_vjp(const MatDev& m, double cdt, const double* s0, const double* F0, const double* Fp0,
+CPFEM_HD bool cp_vjp(const MatDev& m, const Cub& cc, double cdt, const double* s0, const double* F0,
+                     const double* Fp0,
                      const double* g0, const double* R0, const double* th0, const double* ybar,
                      const int* dirs, int ndir, double* xbar) {
   // sweep 1: d/ds -> J (6x6) and sbar = (dy/ds)^T ybar
@@ -307,7 +309,7 @@ CPFEM_HD bool cp_vjp(const MatDev& m, double cdt, const double* s0, const double
   for (int c0 = 0; c0 < 6; c0 += K) {
     for (int i = 0; i < NX; ++i) slot[i] = (i >= c0 && i < c0 + K && i < 6) ? (signed char)(i - c0) : (signed char)-1;
     Dual<K> r6[6], yb;
-    cp_eval_dual<NS, K>(m, cdt, s0, F0, Fp0, g0, R0, th0, slot, ybar, r6, yb);
+    cp_eval_dual<NS, K>(m, cc, cdt, s0, F0, Fp0, g0, R0, th0, slot, ybar, r6, yb);
     for (int k = 0; k < K && c0 + k < 6; ++k) {
       for (int i = 0; i < 6; ++i) J[6 * i + c0 + k] = r6[i].d[k];
       sbar[c0 + k] = yb.d[k];
@@ -328,7 +330,7 @@ CPFEM_HD bool cp_vjp(const MatDev& m, double cdt, const double* s0, const double
     for (int i = 0; i < NX; ++i) slot[i] = -1;
     for (int k = 0; k < K && c0 + k < ndir; ++k) slot[dirs[c0 + k]] = (signed char)k;
     Dual<K> r6[6], yb;
-    cp_eval_dual<NS, K>(m, cdt, s0, F0, Fp0, g0, R0, th0, slot, ybar, r6, yb);
+    cp_eval_dual<NS, K>(m, cc, cdt, s0, F0, Fp0, g0, R0, th0, slot, ybar, r6, yb);
     for (int k = 0; k < K && c0 + k < ndir; ++k) {
       double acc = yb.d[k];
       for (int i = 0; i < 6; ++i) acc = fma(-sbar[i], r6[i].d[k], acc);

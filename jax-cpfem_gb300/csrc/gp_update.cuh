@@ -50,7 +50,7 @@ struct GPSolve {
 
 // Residual at s.  Ct = (F Fp^-1_old R)^T (F Fp^-1_old R) (symmetric, full 3x3).
 template <int NS>
-CPFEM_HD void cp_residual(const MatDev& m, const double* Ct, const double* ig,
+CPFEM_HD void cp_residual(const MatDev& m, const Cub& cc, const double* Ct, const double* ig,
                                             double cdt, double pexp, int ie1, const double* s, double* r,
                                             double& rn, double* dg, double* kk, double* B,
                                             double* M) {
@@ -84,7 +84,7 @@ CPFEM_HD void cp_residual(const MatDev& m, const double* Ct, const double* ig,
   e[4] = 0.5 * fma(B[0], M[2], fma(B[3], M[5], B[6] * M[8]));
   e[5] = 0.5 * fma(B[0], M[1], fma(B[3], M[4], B[6] * M[7]));
   double t[6];
-  cubic_apply(m, e, t);
+  cubic_apply(cc, e, t);
 #pragma unroll
   for (int k = 0; k < 6; ++k) r[k] = s[k] - t[k];
   const double n2 = fma(r[0], r[0], fma(r[1], r[1], r[2] * r[2])) +
@@ -94,7 +94,7 @@ CPFEM_HD void cp_residual(const MatDev& m, const double* Ct, const double* ig,
 
 // J = dr/ds = I + sum_a kk_a (C : sym(M^T d_a (x) n_a)) (x) pv_a
 template <int NS>
-CPFEM_HD void cp_jacobian(const MatDev& m, const double* kk, const double* M,
+CPFEM_HD void cp_jacobian(const MatDev& m, const Cub& cc, const double* kk, const double* M,
                                             double* J) {
 #pragma unroll
   for (int i = 0; i < 36; ++i) J[i] = (i % 7 == 0) ? 1.0 : 0.0;
@@ -113,7 +113,7 @@ CPFEM_HD void cp_jacobian(const MatDev& m, const double* kk, const double* M,
     q[4] = 0.5 * fma(w[0], n[2], w[2] * n[0]);
     q[5] = 0.5 * fma(w[0], n[1], w[1] * n[0]);
     double t[6];
-    cubic_apply(m, q, t);
+    cubic_apply(cc, q, t);
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
       const double ti = kk[a] * t[i];
@@ -127,19 +127,19 @@ CPFEM_HD void cp_jacobian(const MatDev& m, const double* kk, const double* M,
 // trial residuals at s + relax ds, relax = 1, 1/2, ..., until the norm drops below the
 // current one or max_sub_step trials were made; the last trial is taken.
 template <int NS>
-CPFEM_HD void cp_local_newton(const MatDev& m, const double* Ct, const double* ig,
+CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, const double* ig,
                                                 double cdt, double pexp, GPSolve<NS>& st) {
   const int ie1 = int_exponent(pexp - 1.0);
   double r[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) st.s[k] = 0.0;
-  cp_residual<NS>(m, Ct, ig, cdt, pexp, ie1, st.s, r, st.rn, st.dg, st.kk, st.B, st.M);
+  cp_residual<NS>(m, cc, Ct, ig, cdt, pexp, ie1, st.s, r, st.rn, st.dg, st.kk, st.B, st.M);
   int it = 0;
   while (st.rn > m.local_tol && it < m.max_iter) {
     double J[36];
     int perm[6];
     double dinv[6];
-    cp_jacobian<NS>(m, st.kk, st.M, J);
+    cp_jacobian<NS>(m, cc, st.kk, st.M, J);
     lu_factor<6>(J, perm, dinv);
     double ds[6];
 #pragma unroll
@@ -152,7 +152,7 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const double* Ct, const double* i
     do {
 #pragma unroll
       for (int k = 0; k < 6; ++k) st_s[k] = fma(relax, ds[k], st.s[k]);
-      cp_residual<NS>(m, Ct, ig, cdt, pexp, ie1, st_s, r, st.rn, st.dg, st.kk, st.B, st.M);
+      cp_residual<NS>(m, cc, Ct, ig, cdt, pexp, ie1, st_s, r, st.rn, st.dg, st.kk, st.B, st.M);
       relax *= 0.5;
       ++sub;
     } while (st.rn >= rn0 && sub < m.max_sub_step);
@@ -171,7 +171,7 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const double* Ct, const double* i
 // The tangent column for F_kl is handed to store_col(kl, col[9]) as soon as it is
 // known, so the 81 entries never need to be live at once.
 template <int NS, bool WITH_TANGENT, class StoreCol>
-CPFEM_HD void cp_outputs(const MatDev& m, const double* F, const double* G /*Fp^-1_old R*/,
+CPFEM_HD void cp_outputs(const MatDev& m, const Cub& cc, const double* F, const double* G /*Fp^-1_old R*/,
                                            const GPSolve<NS>& st, double* H, double* P,
                                            StoreCol store_col) {
   double S[9], W[9], Y[9];
@@ -229,7 +229,7 @@ CPFEM_HD void cp_outputs(const MatDev& m, const double* F, const double* G /*Fp^
   double J[36];
   int perm[6];
   double dinv[6];
-  cp_jacobian<NS>(m, st.kk, st.M, J);
+  cp_jacobian<NS>(m, cc, st.kk, st.M, J);
   lu_factor<6>(J, perm, dinv);
   double Fe[9];
   mm3(F, H, Fe);
@@ -249,7 +249,7 @@ CPFEM_HD void cp_outputs(const MatDev& m, const double* F, const double* G /*Fp^
     q[3] = 0.5 * fma(a[1], b[2], a[2] * b[1]);
     q[4] = 0.5 * fma(a[0], b[2], a[2] * b[0]);
     q[5] = 0.5 * fma(a[0], b[1], a[1] * b[0]);
-    cubic_apply(m, q, x);
+    cubic_apply(cc, q, x);
     lu_solve<6>(J, perm, dinv, x);
     double col[9];
 #pragma unroll

@@ -198,6 +198,7 @@ class CrystalPlasticity:
         self._post_cache = None
         self._trial = None
         self._state_token = 0
+        self.elastic_table = None
         self.stats = {"gp_passes": 0, "krylov_iters": [], "local_iters_max": 0}
         self.timing = False
         self.timers = {}
@@ -292,6 +293,7 @@ class CrystalPlasticity:
         self.rot_idx = torch.tensor(np.repeat(idx, Q), dtype=torch.int32, device=dev)
         self.param_table = torch.tensor(spec.param_row()[None, :], dtype=torch.float64, device=dev)
         self.param_idx = None
+        self.elastic_table = None
         self.fpi = torch.zeros((9, G), dtype=torch.float64, device=dev)
         self.fpi[0] = 1.0
         self.fpi[4] = 1.0
@@ -402,6 +404,7 @@ class CrystalPlasticity:
         a.fpi, a.g, a.slip = _dev_ptr(fpi), _dev_ptr(g), _dev_ptr(slip)
         a.rot_table, a.rot_idx = _dev_ptr(rot_table), _dev_ptr(rot_idx)
         a.param_table, a.param_idx = _dev_ptr(param_table), _dev_ptr(param_idx)
+        a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
         a.weight_jxw = 1 if outs.pop("weight_jxw", False) else 0
         for k, v in outs.items():
             setattr(a, k, _dev_ptr(v))
