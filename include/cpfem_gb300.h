@@ -97,6 +97,11 @@ typedef struct {
   double* s_out;              /* [9*num_gp] converged second Piola-Kirchhoff S (global frame) */
   int32_t* iters;             /* [num_gp] local Newton iterations */
   int32_t* status;            /* [1] OR of CPFEM_GP_* bits (caller zeroes it) */
+  const int32_t* cell_list;   /* [num_listed] or NULL: with nodal u, evaluate only the 8 GPs
+                                 of each listed cell; every output of other GPs is left
+                                 untouched (a ragged batch skips its converged instances) */
+  int32_t num_listed;
+  int32_t pad;
 } cpfem_gp_args_t;
 
 /*
@@ -291,6 +296,26 @@ int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double*
                    void* workspace, int32_t* info, void* stream);
 
 /*
+ * Options of cpfem_bicgstab_ex.  max_restarts = 0 keeps jax's semantics exactly (a
+ * breakdown, rho = 0 or alpha/omega = 0, ends the solve with code -10/-11 and the current
+ * x).  max_restarts > 0 instead restarts at a breakdown that is not yet converged, from the
+ * current x with the true residual as the new shadow vector (rhat = p = r = b - A x), at
+ * most that many times; info[0] then counts every iteration.  Near-singular systems (a
+ * free rigid rotation under BiCGSTAB, which the reference avoids by switching to UMFPACK,
+ * calibration/case4.py) stagnate into exact rho = 0 in FP64; restarting lets the solve
+ * reach its tolerance instead of returning an unconverged increment.
+ */
+typedef struct {
+  int32_t precond;        /* 0 none, 1 Jacobi (the reference), 2 3x3 block-Jacobi */
+  int32_t transpose;      /* solve A^T x = b */
+  int32_t maxiter;
+  int32_t max_restarts;
+  double tol, atol;
+} cpfem_krylov_opts_t;
+int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
+                      const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream);
+
+/*
  * Allocation-free BiCGSTAB.  No reference counterpart: the reference's jax_solve
  * (crystal_plasticity_OR_design/solver.py:19-48) lets JAX allocate.  Same solver and
  * arguments as cpfem_bicgstab, but the scratch is a fixed device array inside the library
@@ -309,19 +334,36 @@ int cpfem_bicgstab_noalloc(const cpfem_sell_t* sell, const double* values, const
                            int32_t maxiter, int32_t* info, void* stream);
 
 /*
+ * Scalars of the last cpfem_bicgstab / _ex / _noalloc call made by this host thread:
+ * out[7] = (iterations or breakdown code, final ||r||^2, stop threshold
+ * max(tol^2 ||b||^2, atol^2), rho, alpha and omega of the last iteration, restarts).  For logging
+ * a solve the way jax's BiCGSTAB state would be inspected (solver.py:34-40 keeps only x).
+ */
+int cpfem_bicgstab_last_stats(double* out);
+
+/*
  * Ragged batch of independent systems (block-diagonal A over instances, instance i owning
  * nodes [node_off[i], node_off[i+1])): BiCGSTAB per instance with its own scalars and
- * its own stop test, one CTA per instance pulled from a work queue (list `active`, best
- * ordered largest first).  Same recurrences and stop rule as cpfem_bicgstab.  info
- * [2*num_instances] receives (iterations, converged) per listed instance; it stays on the
- * device and the call does not synchronise.  No reference counterpart: the reference
- * solves one RVE per jax_solve call (crystal_plasticity_OR_design/solver.py:19-48).
+ * its own stop test.  Same recurrences and stop rule as cpfem_bicgstab.
+ *   node_off [num_instances+1]  HOST array, non-decreasing, within the system;
+ *   active   [num_active]       HOST array of distinct instance ids to solve;
+ *   weights  [num_active]       HOST work estimate per listed instance (e.g. nodes x the
+ *                               previous solve's iterations), or NULL for nodes^(4/3);
+ *   info     [2*num_instances]  HOST output, (iterations or breakdown code, converged) of
+ *                               every listed instance; other entries are left untouched.
+ * One cooperative launch: with no more instances than co-resident blocks, each instance
+ * gets a team of blocks sized by its weight (team barriers bounded like the grid barrier);
+ * otherwise every block solves whole instances from a queue, heaviest first.  The call
+ * synchronises the stream.  CPFEM_ERR_SOLVE if a team barrier timed out.  No reference
+ * counterpart: the reference solves one RVE per jax_solve call
+ * (crystal_plasticity_OR_design/solver.py:19-48).
  */
 size_t cpfem_bicgstab_batched_workspace_bytes(int32_t num_nodes);
 int cpfem_bicgstab_batched(const cpfem_sell_t* sell, const double* values, const double* b,
                            double* x, int32_t precond, double tol, double atol, int32_t maxiter,
-                           int32_t num_active, const int32_t* active, const int32_t* node_off,
-                           void* workspace, int32_t* info, void* stream);
+                           int32_t num_instances, const int32_t* node_off, int32_t num_active,
+                           const int32_t* active, const double* weights, void* workspace,
+                           int32_t* info, void* stream);
 
 /*
  * FP64 FMA throughput probe (measurement only, not on the solve path): launches `blocks`

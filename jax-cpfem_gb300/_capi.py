@@ -65,6 +65,9 @@ class GPArgs(ctypes.Structure):
         ("s_out", ctypes.c_void_p),
         ("iters", ctypes.c_void_p),
         ("status", ctypes.c_void_p),
+        ("cell_list", ctypes.c_void_p),
+        ("num_listed", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
     ]
 
 
@@ -82,6 +85,17 @@ class VjpArgs(ctypes.Structure):
         "u", "cells", "shape_grads", "jxw", "fpi", "g", "rot_table", "rot_idx", "param_table", "param_idx",
         "elastic_table", "cell_sig_bar", "fpi_bar", "g_bar", "mu", "f_bar", "fpi_bar_old", "g_bar_old", "theta_bar", "rot_bar",
         "status")]
+
+
+class KrylovOpts(ctypes.Structure):
+    _fields_ = [
+        ("precond", ctypes.c_int32),
+        ("transpose", ctypes.c_int32),
+        ("maxiter", ctypes.c_int32),
+        ("max_restarts", ctypes.c_int32),
+        ("tol", ctypes.c_double),
+        ("atol", ctypes.c_double),
+    ]
 
 
 class Sell(ctypes.Structure):
@@ -129,8 +143,10 @@ SIGNATURES = {
     "cpfem_bicgstab_workspace_bytes": (ctypes.c_size_t, [_I32]),
     "cpfem_bicgstab": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P, _P]),
     "cpfem_bicgstab_noalloc": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P]),
+    "cpfem_bicgstab_last_stats": (ctypes.c_int, [_P]),
+    "cpfem_bicgstab_ex": (ctypes.c_int, [_SP, _P, _P, _P, ctypes.POINTER(KrylovOpts), _P, _P, _P]),
     "cpfem_bicgstab_batched_workspace_bytes": (ctypes.c_size_t, [_I32]),
-    "cpfem_bicgstab_batched": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _D, _D, _I32, _I32, _P, _P, _P, _P, _P]),
+    "cpfem_bicgstab_batched": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _D, _D, _I32, _I32, _P, _I32, _P, _P, _P, _P, _P]),
     "cpfem_probe_dfma": (ctypes.c_int, [_I64, _I32, _P, _P, _P]),
 }
 

@@ -4,8 +4,8 @@ Many RVEs (a UQ or calibration sweep: different sizes, grain maps and Kalidindi
 parameters) run as one problem on the concatenated mesh: one constitutive launch over
 every Gauss point of every instance (per-instance parameters through the parameter-index
 table), one element-assembly launch, a block-diagonal matrix, and a batched BiCGSTAB that
-gives every instance its own scalars and stop test (one CTA per instance from a work
-queue, largest instances first).  Each instance keeps the reference's global-Newton
+gives every instance its own scalars and stop test (a team of blocks per instance, sized
+by the instance's nodes times its last Krylov count).  Each instance keeps the reference's global-Newton
 semantics (``crystal_plasticity_OR_design/solver.py:407``): it stops iterating when its own
 ``rel_res <= rel_tol or res <= tol``; converged instances get a zero increment.
 """
@@ -22,7 +22,7 @@ import torch
 from . import _capi
 from .material import MaterialSpec, random_quaternions
 from .mesh import Mesh, box_mesh, face_nodes, voronoi_grains
-from .problem import CrystalPlasticity, _stream
+from .problem import CrystalPlasticity, DeviceCSR, _stream
 from . import solver as _solver
 
 
@@ -110,6 +110,7 @@ class Batch:
         self.params = p.internal_vars
         self.stats = {"newton_iters": [], "krylov_iters": []}
         self.host_s = {}
+        self._last_iters = np.zeros(self.n, dtype=np.float64)
 
     @contextlib.contextmanager
     def _phase(self, name):
@@ -131,6 +132,22 @@ class Batch:
             vals += [0.0, 0.0, 0.0, disp]
         self.problem.fes[0].set_dirichlet_lists(nodes, comps, vals)
 
+    def _assemble(self, dofs, trial, cells=None):
+        """Residual and BC-eliminated tangent at dofs; with ``cells`` only those cells'
+        GPs are re-evaluated (the others keep their outputs in the persistent buffers)."""
+        p = self.problem
+        res, values, status = p.assemble(dofs, need_tangent=True, cell_list=cells, trial=trial)
+        p._check_status(status)
+        p.A_values = values
+        res = res.reshape(-1)
+        p.apply_dirichlet(res, dofs, values)
+        return res, DeviceCSR(p, values)
+
+    def _cells_of(self, inst):
+        c = np.concatenate([np.arange(self.cell_off_np[i], self.cell_off_np[i + 1], dtype=np.int32)
+                            for i in np.sort(inst)])
+        return torch.from_numpy(c).to(self.problem.device)
+
     def _norms(self, res):
         p = self.problem
         out = torch.empty(self.n, dtype=torch.float64, device=p.device)
@@ -143,39 +160,47 @@ class Batch:
         p = self.problem
         lib = p.lib
         dofs = self.sol.clone()
+        trial = p.new_trial()
         with self._phase("assemble"):
-            res, A = _solver.newton_update_helper(p, dofs)
+            res, A = self._assemble(dofs, trial)
             r0 = self._norms(res)
         rn = r0.copy()
         with np.errstate(invalid="ignore", divide="ignore"):
             active = (rn / r0 > rel_tol) & (rn > tol)
         nws = int(lib.cpfem_bicgstab_batched_workspace_bytes(p.num_nodes))
         ws = p._buf("batched_ws", (nws // 8 + 64,))
-        info = torch.zeros(2 * self.n, dtype=torch.int32, device=p.device)
+        info = np.zeros(2 * self.n, dtype=np.int32)
+        node_off = np.ascontiguousarray(self.node_off_np, dtype=np.int32)
+        nodes = np.diff(self.node_off_np).astype(np.float64)
         its = 0
         newton_count = np.zeros(self.n, dtype=np.int64)
         while active.any():
             if its >= max_newton:
                 raise RuntimeError("batched global Newton did not converge")
-            act = self.order[active[self.order]].astype(np.int32)
-            act_dev = torch.tensor(act, device=p.device)
+            act = np.ascontiguousarray(self.order[active[self.order]], dtype=np.int32)
+            # work estimate per instance: nodes x its last Krylov count (nodes^(4/3) before any)
+            wts = np.ascontiguousarray(nodes[act] * np.where(self._last_iters[act] > 0, self._last_iters[act],
+                                                             nodes[act] ** (1.0 / 3.0)))
             b = torch.neg(res)
             x = _solver.initial_increment(p, dofs).clone()
             with self._phase("krylov"), p.region("bicgstab_batched"):
                 _capi.check(lib.cpfem_bicgstab_batched(p.sell, A.values.data_ptr(), b.data_ptr(), x.data_ptr(),
                                                        int(precond), float(ktol), float(katol), int(maxiter),
-                                                       int(act.size), act_dev.data_ptr(), self.node_off.data_ptr(),
-                                                       ws.data_ptr(), info.data_ptr(), _stream()))
-            inf = info.cpu().numpy().reshape(self.n, 2)
+                                                       self.n, node_off.ctypes.data, int(act.size), act.ctypes.data,
+                                                       wts.ctypes.data, ws.data_ptr(), info.ctypes.data, _stream()))
+            inf = info.reshape(self.n, 2)
+            self._last_iters[act] = np.maximum(inf[act, 0], 1)
             if not inf[act, 1].all():
                 raise RuntimeError("a batched linear solve did not converge")
             self.stats["krylov_iters"].append(inf[act, 0].copy())
             _capi.check(lib.cpfem_axpy(dofs.numel(), 1.0, x.data_ptr(), dofs.data_ptr(), _stream()))
             newton_count[act] += 1
             with self._phase("assemble"):
-                res, A = _solver.newton_update_helper(p, dofs)
+                # converged instances keep their state: only the active ones are re-evaluated
+                cells = None if act.size == self.n else self._cells_of(act)
+                res, A = self._assemble(dofs, trial, cells)
                 rn = self._norms(res)
-            if not np.isfinite(rn).all():
+            if not np.isfinite(rn[active]).all():
                 raise FloatingPointError("non-finite residual in the batch")
             active = active & (rn / r0 > rel_tol) & (rn > tol)
             its += 1

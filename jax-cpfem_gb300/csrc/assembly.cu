@@ -53,8 +53,18 @@ int make_matdev(const cpfem_material_t* m, MatDev* o) {
 // ------------------------------------------------------------------------------------
 template <int NS, bool TANGENT>
 __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_args_t a) {
-  const int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t G = a.num_gp;
+  int64_t gp = tid;
+  if (a.cell_list != nullptr) {
+    if (tid >= 8 * (int64_t)a.num_listed) return;
+    const int64_t c = a.cell_list[tid >> 3];
+    if (c < 0 || c >= a.num_cells) {
+      atomicOr(a.status, CPFEM_GP_BOUNDS);
+      return;
+    }
+    gp = 8 * c + (tid & 7);
+  }
   if (gp >= G) return;
 
   double F[9];
@@ -333,7 +343,9 @@ __global__ void __launch_bounds__(256) k_segmented_dot(int32_t nseg, const int64
 template <int NS>
 static int launch_gp(const MatDev& md, const cpfem_gp_args_t& a, cudaStream_t s) {
   const int threads = 128;
-  const unsigned blocks = (unsigned)ceil_div(a.num_gp, threads);
+  const int64_t work = a.cell_list != nullptr ? 8 * (int64_t)a.num_listed : a.num_gp;
+  if (work == 0) return CPFEM_OK;
+  const unsigned blocks = (unsigned)ceil_div(work, threads);
   if (a.tangent != nullptr)
     k_gp_eval<NS, true><<<blocks, threads, 0, s>>>(md, a);
   else
@@ -367,6 +379,9 @@ int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void
     CPFEM_REQUIRE(a.num_gp == (int64_t)a.num_cells * 8, "num_gp must be 8*num_cells with nodal u");
   }
   CPFEM_REQUIRE(!(a.weight_jxw && a.jxw == nullptr), "weight_jxw without jxw");
+  CPFEM_REQUIRE(a.cell_list == nullptr || (a.u != nullptr && a.status != nullptr && a.num_listed >= 0 &&
+                                           a.num_listed <= a.num_cells),
+                "a cell list needs nodal u, a status word and 0 <= num_listed <= num_cells");
   CPFEM_REQUIRE(a.slip_new == nullptr || a.slip != nullptr, "slip_new needs slip");
   CPFEM_REQUIRE(md.qmode == 0 || md.num_slip % 3 == 0, "qmode 1 needs num_slip % 3 == 0");
   cudaStream_t s = (cudaStream_t)stream;

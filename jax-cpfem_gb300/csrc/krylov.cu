@@ -12,6 +12,8 @@
 // and take the same branch.  Barrier waits are bounded: a block that waits too long sets
 // an error flag and the solve returns CPFEM_ERR_SOLVE.
 #include <algorithm>
+#include <cmath>
+#include <vector>
 #include <string>
 
 #include "cpfem_common.cuh"
@@ -35,7 +37,12 @@ struct SolveOut {
   int error;
   double rs;
   double atol2;
+  double rho, alpha, omega;   // scalars of the last iteration (rho: the one it started with)
+  int restarts;
+  int pad;
 };
+
+static thread_local SolveOut g_last_solve = {0, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 0, 0};
 
 struct KWork {
   GridSync* sync;
@@ -224,7 +231,7 @@ template <bool TRANS>
 __global__ void __launch_bounds__(kPThreads) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
                                                         const double* __restrict__ b, double* __restrict__ x,
                                                         KWork w, int precond, double tol, double atol,
-                                                        int maxiter) {
+                                                        int maxiter, int max_restarts) {
   __shared__ double smem[4 * 32];
   __shared__ double bcast[4];
   const int64_t n = L.num_nodes;
@@ -257,7 +264,7 @@ __global__ void __launch_bounds__(kPThreads) k_bicgstab(const cpfem_sell_t L, co
   ok = grid_reduce<2>(v2, parts(), w.sync, gen, smem, bcast) && ok;
   const double atol2 = fmax(tol * tol * v2[0], atol * atol);
   double rs = v2[1], rho_new = v2[1], rho = 1.0, alpha = 1.0, omega = 1.0;
-  int k = 0;
+  int k = 0, restarts = 0;
 
   while (ok && rs > atol2 && k < maxiter && k >= 0) {
     const double beta = rho_new / rho * alpha / omega;
@@ -343,16 +350,43 @@ __global__ void __launch_bounds__(kPThreads) k_bicgstab(const cpfem_sell_t L, co
     ok = grid_reduce<2>(vr, parts(), w.sync, gen, smem, bcast) && ok;
     int kn = (omega == 0.0 || alpha == 0.0) ? -11 : k + 1;
     if (rho_new == 0.0) kn = -10;
-    k = kn;
     rho = rho_new;
     rho_new = vr[1];
     rs = vr[0];
+    if (kn < 0 && restarts < max_restarts && ok && rs > atol2) {
+      // restart at the current x: rhat = p = q = r = b - A x (x is complete: the last
+      // reduction crossed the grid barrier after every block wrote its part)
+      ++restarts;
+      double v3[1] = {0.0};
+      for (int64_t a = t0; a < n; a += stride) {
+        double acc[3];
+        sell_rows<TRANS, true>(L, vals, x, a, acc);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const int64_t d = 3 * a + i;
+          const double rv = b[d] - acc[i];
+          w.r[d] = rv; w.rhat[d] = rv; w.p[d] = rv; w.q[d] = rv;
+          v3[0] = fma(rv, rv, v3[0]);
+        }
+      }
+      ok = grid_reduce<1>(v3, parts(), w.sync, gen, smem, bcast) && ok;
+      rs = v3[0];
+      rho_new = v3[0];
+      rho = alpha = omega = 1.0;
+      k = k + 1;
+    } else {
+      k = kn;
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.out->restarts = restarts;
     w.out->k = k;
     w.out->error = ok ? 0 : 1;
     w.out->rs = rs;
     w.out->atol2 = atol2;
+    w.out->rho = rho;
+    w.out->alpha = alpha;
+    w.out->omega = omega;
   }
 }
 
@@ -366,7 +400,8 @@ static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms) {
 
 template <bool TRANS>
 static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double* b, double* x, int precond,
-                        double tol, double atol, int32_t maxiter, void* workspace, int32_t* info, cudaStream_t s) {
+                        double tol, double atol, int32_t maxiter, void* workspace, int32_t* info, cudaStream_t s,
+                        int max_restarts = 0) {
   KWork w;
   carve(workspace, L.num_nodes, &w);
   CPFEM_CUDA_TRY(cudaMemsetAsync(w.sync, 0, sizeof(GridSync), s));
@@ -388,8 +423,8 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   double* xx = x;
   int pc = precond;
   double tl = tol, at = atol;
-  int mi = maxiter;
-  void* args[] = {&Lc, &vals, &bb, &xx, &w, &pc, &tl, &at, &mi};
+  int mi = maxiter, mr = max_restarts;
+  void* args[] = {&Lc, &vals, &bb, &xx, &w, &pc, &tl, &at, &mi, &mr};
   CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_bicgstab<TRANS>, dim3((unsigned)blocks),
                                              dim3(kPThreads), args, 0, s));
   SolveOut out;
@@ -397,6 +432,7 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   CPFEM_CUDA_TRY(cudaStreamSynchronize(s));
   info[0] = out.k;
   info[1] = (out.rs <= out.atol2) ? 1 : 0;
+  g_last_solve = out;
   if (out.error) {
     set_error("BiCGSTAB grid barrier timed out");
     return CPFEM_ERR_SOLVE;
@@ -431,38 +467,89 @@ int cpfem_spmv(const cpfem_sell_t* sell, const double* values, const double* x, 
 
 size_t cpfem_bicgstab_workspace_bytes(int32_t num_nodes) { return carve(nullptr, num_nodes, nullptr); }
 
-int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x, int32_t precond,
-                   int32_t transpose, double tol, double atol, int32_t maxiter, void* workspace, int32_t* info,
-                   void* stream) {
+int cpfem_bicgstab_last_stats(double* out) {
+  CPFEM_REQUIRE(out != nullptr, "out is null");
+  out[0] = (double)g_last_solve.k;
+  out[1] = g_last_solve.rs;
+  out[2] = g_last_solve.atol2;
+  out[3] = g_last_solve.rho;
+  out[4] = g_last_solve.alpha;
+  out[5] = g_last_solve.omega;
+  out[6] = (double)g_last_solve.restarts;
+  return CPFEM_OK;
+}
+
+int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
+                      const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream) {
   CPFEM_REQUIRE(info != nullptr, "info is null");
   info[0] = 0;
   info[1] = 1;
+  CPFEM_REQUIRE(opts != nullptr, "opts is null");
   CPFEM_REQUIRE(sell_ok(sell), "bad layout");
   if (sell->num_nodes == 0) return CPFEM_OK;
   CPFEM_REQUIRE(values && b && x && workspace, "bad bicgstab arguments");
   CPFEM_REQUIRE(((uintptr_t)workspace & 255) == 0, "workspace must be 256-byte aligned");
-  CPFEM_REQUIRE(precond >= 0 && precond <= 2, "precond must be 0, 1 or 2");
-  CPFEM_REQUIRE(maxiter >= 0, "maxiter must be >= 0");
-  CPFEM_REQUIRE(!transpose || sell->tpos != nullptr, "transpose needs tpos");
+  CPFEM_REQUIRE(opts->precond >= 0 && opts->precond <= 2, "precond must be 0, 1 or 2");
+  CPFEM_REQUIRE(opts->maxiter >= 0, "maxiter must be >= 0");
+  CPFEM_REQUIRE(opts->max_restarts >= 0, "max_restarts must be >= 0");
+  CPFEM_REQUIRE(!opts->transpose || sell->tpos != nullptr, "transpose needs tpos");
   cudaStream_t s = (cudaStream_t)stream;
-  if (transpose) return run_bicgstab<true>(*sell, values, b, x, precond, tol, atol, maxiter, workspace, info, s);
-  return run_bicgstab<false>(*sell, values, b, x, precond, tol, atol, maxiter, workspace, info, s);
+  if (opts->transpose)
+    return run_bicgstab<true>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
+                              info, s, opts->max_restarts);
+  return run_bicgstab<false>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
+                             info, s, opts->max_restarts);
+}
+
+int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x, int32_t precond,
+                   int32_t transpose, double tol, double atol, int32_t maxiter, void* workspace, int32_t* info,
+                   void* stream) {
+  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol};
+  return cpfem_bicgstab_ex(sell, values, b, x, &o, workspace, info, stream);
 }
 
 }  // extern "C"
 
-// ---- batched BiCGSTAB: one CTA per instance, ragged instances from a work queue ------
+// ---- ragged batch: teams of blocks, one instance per team --------------------------------
+// A ragged batch (instances of very different sizes and iteration counts) is split over the
+// co-resident blocks of one cooperative launch.  When the batch has no more instances than
+// blocks, every instance gets a team of consecutive blocks sized by its estimated work
+// (nodes x expected iterations), so a 24^3 RVE and an 8^3 RVE finish at about the same
+// time; a team crosses its dependencies with its own bounded barrier and reduces its dot
+// products in a fixed block order.  With more instances than blocks, every block is a team
+// of one that pulls instances from a queue, largest first.
 namespace cpfem {
 
-constexpr int kBThreads = 1024;
+constexpr int kMinNodesPerBlock = 256;
 
-struct BWork {
-  double *r, *rhat, *p, *q, *s, *t, *phat, *shat, *minv;
-  unsigned int* queue;   // next entry of the active list
+struct RTeam {
+  int first;   // first block of the team
+  int nb;      // blocks in the team
+  int job;     // the team's job, or -1: pull jobs from the queue (nb == 1)
+  int pad;
 };
 
-static size_t carve_batched(void* base, int64_t n_nodes, BWork* w) {
+struct RJob {
+  int inst;
+  int pad;
+  int64_t n0, n1;
+};
+
+struct RWork {
+  double *r, *rhat, *p, *q, *s, *t, *phat, *shat, *minv;
+  double* partials;      // 2 buffers x 4 values x kMaxBlocks, by block id
+  int* team_of_block;    // kMaxBlocks
+  RTeam* teams;          // kMaxBlocks
+  GridSync* tsync;       // one barrier per team
+  RJob* jobs;            // at most num_nodes (every listed instance owns a node)
+  int32_t* info;         // 2 per job
+  unsigned int* queue;
+  int* error;
+};
+
+static size_t carve_ragged(void* base, int64_t n_nodes, RWork* w) {
   const int64_t n = 3 * n_nodes;
+  const int64_t nj = std::max<int64_t>(n_nodes, 1);
   char* p = (char*)base;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -470,49 +557,130 @@ static size_t carve_batched(void* base, int64_t n_nodes, BWork* w) {
     off += align256(bytes);
     return q;
   };
-  BWork tmp;
-  tmp.queue = (unsigned int*)take(sizeof(unsigned int));
+  RWork tmp;
   double** vecs[] = {&tmp.r, &tmp.rhat, &tmp.p, &tmp.q, &tmp.s, &tmp.t, &tmp.phat, &tmp.shat};
   for (double** v : vecs) *v = (double*)take(sizeof(double) * n);
   tmp.minv = (double*)take(sizeof(double) * 9 * n_nodes);
+  tmp.partials = (double*)take(sizeof(double) * 2 * 4 * kMaxBlocks);
+  tmp.team_of_block = (int*)take(sizeof(int) * kMaxBlocks);
+  tmp.teams = (RTeam*)take(sizeof(RTeam) * kMaxBlocks);
+  tmp.tsync = (GridSync*)take(sizeof(GridSync) * kMaxBlocks);
+  tmp.jobs = (RJob*)take(sizeof(RJob) * nj);
+  tmp.info = (int32_t*)take(sizeof(int32_t) * 2 * nj);
+  tmp.queue = (unsigned int*)take(sizeof(unsigned int));
+  tmp.error = (int*)take(sizeof(int));
   if (w) *w = tmp;
   return off;
 }
 
-template <int NV>
-__device__ __forceinline__ void cta_sum(double (&v)[NV], double* smem) {
-  block_sum<NV>(v, smem);
-  __shared__ double bc[4];
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int k = 0; k < NV; ++k) bc[k] = v[k];
+// Barrier over the nb blocks of a team (bounded wait, as grid_barrier).
+__device__ __forceinline__ bool team_barrier(GridSync* gs, unsigned int nb, unsigned int& gen, int* gerr) {
+  __shared__ int s_ok;
+  __threadfence();
   __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = bc[k];
+  if (threadIdx.x == 0) {
+    const unsigned int my = gen;
+    int ok = 1;
+    const unsigned int arrived = atomicAdd(&gs->count, 1u);
+    if (arrived == nb - 1) {
+      atomicExch(&gs->count, 0u);
+      __threadfence();
+      atomicExch(&gs->gen, my + 1u);
+    } else {
+      volatile unsigned int* vg = &gs->gen;
+      long long spins = 0;
+      while (*vg == my) {
+        if (++spins > kSpinLimit) {
+          ok = 0;
+          atomicExch(&gs->error, 1);
+          atomicExch(gerr, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_ok = ok && (*(volatile int*)&gs->error == 0);
+  }
   __syncthreads();
+  gen += 1u;
+  return s_ok != 0;
 }
 
-// Each CTA takes instances from the queue; instance `inst` owns nodes
-// [node_off[inst], node_off[inst+1]).  Threads walk the instance's nodes group-aligned so
-// a warp reads one sliced-ELL group.
-__global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
+// Team-wide sums of NV values: block sum, then (teams of several blocks) publish, barrier
+// and add the team's partials in block order.  Every block of the team gets the same bits.
+template <int NV>
+__device__ __forceinline__ bool team_reduce(double (&v)[NV], double* partials, int first, int nb, GridSync* gs,
+                                            unsigned int& gen, int* gerr, double* smem, double* bcast) {
+  block_sum<NV>(v, smem);
+  bool ok = true;
+  if (nb == 1) {
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) bcast[k] = v[k];
+  } else {
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) partials[k * kMaxBlocks + blockIdx.x] = v[k];
+    ok = team_barrier(gs, (unsigned)nb, gen, gerr);
+    if (threadIdx.x < 32) {
+      double acc[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+      for (int b = first + (int)threadIdx.x; b < first + nb; b += 32)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += __ldcg(&partials[k * kMaxBlocks + b]);
+      warp_sum<NV>(acc);
+      if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) bcast[k] = acc[k];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = bcast[k];
+  __syncthreads();
+  return ok;
+}
+
+__global__ void __launch_bounds__(kPThreads) k_bicgstab_ragged(
     const cpfem_sell_t L, const double* __restrict__ vals, const double* __restrict__ b, double* __restrict__ x,
-    BWork w, int precond, double tol, double atol, int maxiter, int n_active, const int32_t* __restrict__ active,
-    const int32_t* __restrict__ node_off, int32_t* __restrict__ info) {
+    RWork w, int precond, double tol, double atol, int maxiter, int n_jobs) {
   __shared__ double smem[4 * 32];
+  __shared__ double bcast[4];
   __shared__ int s_job;
-  for (;;) {
-    if (threadIdx.x == 0) s_job = (int)atomicAdd(w.queue, 1u);
-    __syncthreads();
-    const int job = s_job;
-    __syncthreads();
-    if (job >= n_active) break;
-    const int inst = active[job];
-    const int64_t n0 = node_off[inst], n1 = node_off[inst + 1];
-    const int64_t a0 = (n0 >> 5) << 5;
-    // r = b - A x0 ; rhat = p = q = r
+  const int team = w.team_of_block[blockIdx.x];
+  const RTeam tm = w.teams[team];
+  GridSync* gs = w.tsync + team;
+  const int nb = tm.nb, first = tm.first;
+  const int64_t tid = (int64_t)(blockIdx.x - first) * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)nb * blockDim.x;
+  unsigned int gen = 0u;
+  int buf = 0;
+  auto parts = [&]() {
+    double* p = w.partials + (size_t)buf * 4 * kMaxBlocks;
+    buf ^= 1;
+    return p;
+  };
+  bool ok = true;
+  for (int pass = 0; ok; ++pass) {
+    int job;
+    if (tm.job >= 0) {
+      if (pass > 0) break;
+      job = tm.job;
+    } else {
+      if (threadIdx.x == 0) s_job = (int)atomicAdd(w.queue, 1u);
+      __syncthreads();
+      job = s_job;
+      __syncthreads();
+    }
+    if (job >= n_jobs) break;
+    const RJob jb = w.jobs[job];
+    const int64_t n0 = jb.n0, n1 = jb.n1;
+    const int64_t a0 = ((n0 >> 5) << 5) + tid;   // group-aligned: a warp reads one sliced-ELL group
+
     double v2[2] = {0.0, 0.0};
-    for (int64_t a = a0 + threadIdx.x; a < n1; a += blockDim.x) {
+    for (int64_t a = a0; a < n1; a += stride) {
       if (a < n0) continue;
       double acc[3];
       sell_rows<false, true>(L, vals, x, a, acc);
@@ -526,13 +694,13 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
         v2[1] = fma(rv, rv, v2[1]);
       }
     }
-    cta_sum<2>(v2, smem);
+    ok = team_reduce<2>(v2, parts(), first, nb, gs, gen, w.error, smem, bcast) && ok;
     const double atol2 = fmax(tol * tol * v2[0], atol * atol);
     double rs = v2[1], rho_new = v2[1], rho = 1.0, alpha = 1.0, omega = 1.0;
     int k = 0;
-    while (rs > atol2 && k < maxiter && k >= 0) {
+    while (ok && rs > atol2 && k < maxiter && k >= 0) {
       const double beta = rho_new / rho * alpha / omega;
-      for (int64_t a = a0 + threadIdx.x; a < n1; a += blockDim.x) {
+      for (int64_t a = a0; a < n1; a += stride) {
         if (a < n0) continue;
         double pv[3], ph[3];
 #pragma unroll
@@ -545,9 +713,10 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
 #pragma unroll
         for (int i = 0; i < 3; ++i) w.phat[3 * a + i] = ph[i];
       }
-      __syncthreads();
+      if (nb > 1) ok = team_barrier(gs, (unsigned)nb, gen, w.error) && ok;
+      else __syncthreads();
       double v1[1] = {0.0};
-      for (int64_t a = a0 + threadIdx.x; a < n1; a += blockDim.x) {
+      for (int64_t a = a0; a < n1; a += stride) {
         if (a < n0) continue;
         double acc[3];
         sell_rows<false, true>(L, vals, w.phat, a, acc);
@@ -558,10 +727,10 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
           v1[0] = fma(w.rhat[d], acc[i], v1[0]);
         }
       }
-      cta_sum<1>(v1, smem);
+      ok = team_reduce<1>(v1, parts(), first, nb, gs, gen, w.error, smem, bcast) && ok;
       alpha = rho_new / v1[0];
       double vs[1] = {0.0};
-      for (int64_t a = a0 + threadIdx.x; a < n1; a += blockDim.x) {
+      for (int64_t a = a0; a < n1; a += stride) {
         if (a < n0) continue;
         double sv[3], sh[3];
 #pragma unroll
@@ -575,10 +744,10 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
 #pragma unroll
         for (int i = 0; i < 3; ++i) w.shat[3 * a + i] = sh[i];
       }
-      cta_sum<1>(vs, smem);
+      ok = team_reduce<1>(vs, parts(), first, nb, gs, gen, w.error, smem, bcast) && ok;
       const bool early = vs[0] < atol2;
       double vt[2] = {0.0, 0.0};
-      for (int64_t a = a0 + threadIdx.x; a < n1; a += blockDim.x) {
+      for (int64_t a = a0; a < n1; a += stride) {
         if (a < n0) continue;
         double acc[3];
         sell_rows<false, true>(L, vals, w.shat, a, acc);
@@ -590,10 +759,10 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
           vt[1] = fma(acc[i], acc[i], vt[1]);
         }
       }
-      cta_sum<2>(vt, smem);
+      ok = team_reduce<2>(vt, parts(), first, nb, gs, gen, w.error, smem, bcast) && ok;
       omega = vt[0] / vt[1];
       double vr[2] = {0.0, 0.0};
-      for (int64_t a = a0 + threadIdx.x; a < n1; a += blockDim.x) {
+      for (int64_t a = a0; a < n1; a += stride) {
         if (a < n0) continue;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -611,7 +780,7 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
           vr[1] = fma(w.rhat[d], rv, vr[1]);
         }
       }
-      cta_sum<2>(vr, smem);
+      ok = team_reduce<2>(vr, parts(), first, nb, gs, gen, w.error, smem, bcast) && ok;
       int kn = (omega == 0.0 || alpha == 0.0) ? -11 : k + 1;
       if (rho_new == 0.0) kn = -10;
       k = kn;
@@ -619,11 +788,10 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
       rho_new = vr[1];
       rs = vr[0];
     }
-    if (threadIdx.x == 0) {
-      info[2 * inst] = k;
-      info[2 * inst + 1] = (rs <= atol2) ? 1 : 0;
+    if ((int)blockIdx.x == first && threadIdx.x == 0) {
+      w.info[2 * job] = k;
+      w.info[2 * job + 1] = (rs <= atol2) ? 1 : 0;
     }
-    __syncthreads();
   }
 }
 
@@ -632,34 +800,123 @@ __global__ void __launch_bounds__(kBThreads) k_bicgstab_batched(
 extern "C" {
 
 size_t cpfem_bicgstab_batched_workspace_bytes(int32_t num_nodes) {
-  return cpfem::carve_batched(nullptr, num_nodes, nullptr);
+  return cpfem::carve_ragged(nullptr, num_nodes, nullptr);
 }
 
 int cpfem_bicgstab_batched(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
-                           int32_t precond, double tol, double atol, int32_t maxiter, int32_t num_active,
-                           const int32_t* active, const int32_t* node_off, void* workspace, int32_t* info,
-                           void* stream) {
+                           int32_t precond, double tol, double atol, int32_t maxiter, int32_t num_instances,
+                           const int32_t* node_off, int32_t num_active, const int32_t* active,
+                           const double* weights, void* workspace, int32_t* info, void* stream) {
   using namespace cpfem;
   CPFEM_REQUIRE(sell_ok(sell), "bad layout");
+  CPFEM_REQUIRE(num_instances >= 0 && num_active >= 0 && num_active <= num_instances, "bad instance counts");
   if (num_active == 0 || sell->num_nodes == 0) return CPFEM_OK;
   CPFEM_REQUIRE(values && b && x && active && node_off && workspace && info, "bad batched bicgstab arguments");
   CPFEM_REQUIRE(((uintptr_t)workspace & 255) == 0, "workspace must be 256-byte aligned");
-  CPFEM_REQUIRE(precond >= 0 && precond <= 2 && maxiter >= 0 && num_active > 0, "bad solver settings");
+  CPFEM_REQUIRE(precond >= 0 && precond <= 2 && maxiter >= 0, "bad solver settings");
+  CPFEM_REQUIRE(node_off[0] >= 0 && node_off[num_instances] <= sell->num_nodes, "node_off outside the system");
+  for (int32_t i = 0; i < num_instances; ++i)
+    CPFEM_REQUIRE(node_off[i + 1] >= node_off[i], "node_off must be non-decreasing");
+  // jobs: listed instances that own nodes, heaviest first
+  std::vector<char> seen((size_t)num_instances, 0);
+  std::vector<RJob> jobs;
+  std::vector<double> wts;
+  jobs.reserve((size_t)num_active);
+  for (int32_t j = 0; j < num_active; ++j) {
+    const int32_t inst = active[j];
+    CPFEM_REQUIRE(inst >= 0 && inst < num_instances, "active instance out of range");
+    CPFEM_REQUIRE(!seen[(size_t)inst], "an instance is listed twice");
+    seen[(size_t)inst] = 1;
+    const int64_t n0 = node_off[inst], n1 = node_off[inst + 1];
+    if (n1 == n0) {
+      info[2 * inst] = 0;
+      info[2 * inst + 1] = 1;
+      continue;
+    }
+    const double wt = weights ? weights[j] : std::pow((double)(n1 - n0), 4.0 / 3.0);
+    CPFEM_REQUIRE(wt > 0.0 && std::isfinite(wt), "weights must be positive");
+    jobs.push_back(RJob{inst, 0, n0, n1});
+    wts.push_back(wt);
+  }
+  if (jobs.empty()) return CPFEM_OK;
+  {
+    std::vector<size_t> order(jobs.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) { return wts[a] > wts[c]; });
+    std::vector<RJob> j2(jobs.size());
+    std::vector<double> w2(jobs.size());
+    for (size_t i = 0; i < order.size(); ++i) { j2[i] = jobs[order[i]]; w2[i] = wts[order[i]]; }
+    jobs.swap(j2);
+    wts.swap(w2);
+  }
+  const int nj = (int)jobs.size();
   cudaStream_t s = (cudaStream_t)stream;
-  BWork w;
-  carve_batched(workspace, sell->num_nodes, &w);
+  RWork w;
+  carve_ragged(workspace, sell->num_nodes, &w);
+  int dev = 0, sms = 0, per_sm = 0;
+  CPFEM_CUDA_TRY(cudaGetDevice(&dev));
+  CPFEM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CPFEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_bicgstab_ragged, kPThreads, 0));
+  if (per_sm < 1) {
+    set_error("ragged BiCGSTAB kernel cannot be resident");
+    return CPFEM_ERR_CUDA;
+  }
+  const int bmax = (int)std::min<int64_t>((int64_t)per_sm * sms, kMaxBlocks);
+  std::vector<RTeam> teams;
+  std::vector<int> team_of_block;
+  if (nj <= bmax) {
+    // static plan: one team per job, 1 block plus a share of the spare blocks by weight
+    double wsum = 0.0;
+    for (double v : wts) wsum += v;
+    const int spare = bmax - nj;
+    int next = 0;
+    for (int j = 0; j < nj; ++j) {
+      const int64_t cap = std::max<int64_t>(1, ceil_div(jobs[(size_t)j].n1 - jobs[(size_t)j].n0, kMinNodesPerBlock));
+      int64_t k = 1 + (int64_t)std::floor((double)spare * wts[(size_t)j] / wsum);
+      k = std::min<int64_t>(k, cap);
+      teams.push_back(RTeam{next, (int)k, j, 0});
+      for (int64_t c = 0; c < k; ++c) team_of_block.push_back(j);
+      next += (int)k;
+    }
+  } else {
+    for (int blk = 0; blk < bmax; ++blk) {
+      teams.push_back(RTeam{blk, 1, -1, 0});
+      team_of_block.push_back(blk);
+    }
+  }
+  const int blocks = (int)team_of_block.size();
+  CPFEM_CUDA_TRY(cudaMemcpyAsync(w.teams, teams.data(), sizeof(RTeam) * teams.size(), cudaMemcpyHostToDevice, s));
+  CPFEM_CUDA_TRY(cudaMemcpyAsync(w.team_of_block, team_of_block.data(), sizeof(int) * (size_t)blocks,
+                                 cudaMemcpyHostToDevice, s));
+  CPFEM_CUDA_TRY(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(RJob) * (size_t)nj, cudaMemcpyHostToDevice, s));
+  CPFEM_CUDA_TRY(cudaMemsetAsync(w.tsync, 0, sizeof(GridSync) * teams.size(), s));
   CPFEM_CUDA_TRY(cudaMemsetAsync(w.queue, 0, sizeof(unsigned int), s));
+  CPFEM_CUDA_TRY(cudaMemsetAsync(w.error, 0, sizeof(int), s));
   if (precond != 0) {
     k_precond_setup<false><<<(unsigned)ceil_div(sell->num_nodes, 128), 128, 0, s>>>(*sell, values, precond, w.minv);
     CPFEM_CUDA_TRY(cudaGetLastError());
   }
-  int dev = 0, sms = 0;
-  CPFEM_CUDA_TRY(cudaGetDevice(&dev));
-  CPFEM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const unsigned blocks = (unsigned)std::min<int64_t>(num_active, (int64_t)sms);
-  k_bicgstab_batched<<<blocks, kBThreads, 0, s>>>(*sell, values, b, x, w, precond, tol, atol, maxiter, num_active,
-                                                 active, node_off, info);
-  CPFEM_CUDA_TRY(cudaGetLastError());
+  cpfem_sell_t Lc = *sell;
+  const double* bb = b;
+  double* xx = x;
+  int pc = precond, mi = maxiter, njobs = nj;
+  double tl = tol, at = atol;
+  void* args[] = {&Lc, &values, &bb, &xx, &w, &pc, &tl, &at, &mi, &njobs};
+  CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_bicgstab_ragged, dim3((unsigned)blocks), dim3(kPThreads),
+                                             args, 0, s));
+  std::vector<int32_t> out((size_t)(2 * nj));
+  int err = 0;
+  CPFEM_CUDA_TRY(cudaMemcpyAsync(out.data(), w.info, sizeof(int32_t) * out.size(), cudaMemcpyDeviceToHost, s));
+  CPFEM_CUDA_TRY(cudaMemcpyAsync(&err, w.error, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CPFEM_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int j = 0; j < nj; ++j) {
+    info[2 * jobs[(size_t)j].inst] = out[(size_t)(2 * j)];
+    info[2 * jobs[(size_t)j].inst + 1] = out[(size_t)(2 * j + 1)];
+  }
+  if (err) {
+    set_error("ragged BiCGSTAB team barrier timed out");
+    return CPFEM_ERR_SOLVE;
+  }
   return CPFEM_OK;
 }
 

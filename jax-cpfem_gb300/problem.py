@@ -406,6 +406,9 @@ class CrystalPlasticity:
         a.param_table, a.param_idx = _dev_ptr(param_table), _dev_ptr(param_idx)
         a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
         a.weight_jxw = 1 if outs.pop("weight_jxw", False) else 0
+        cl = outs.pop("cell_list", None)
+        if cl is not None:
+            a.cell_list, a.num_listed = _dev_ptr(cl), int(cl.numel())
         for k, v in outs.items():
             setattr(a, k, _dev_ptr(v))
         return a
@@ -444,8 +447,11 @@ class CrystalPlasticity:
         if s & _capi.CPFEM_GP_MAXITER:
             raise RuntimeError(f"local Newton did not converge within max_iter={self.material.max_iter}")
 
-    def assemble(self, u, need_tangent=True):
+    def assemble(self, u, need_tangent=True, cell_list=None, trial=None):
         """Residual int P:grad(v) (ndof) and, if asked, the CSR tangent values, before BCs.
+        ``cell_list`` (device int32) restricts the constitutive pass to those cells: the
+        other GPs keep their P, dP/dF and trial outputs from an earlier pass (``trial``, a
+        dict of persistent trial buffers, keeps them across passes).
         Returns (res, values or None, status tensor)."""
         G = self.num_gp
         res = self._buf("res", (self.num_total_dofs_all_vars,))
@@ -459,19 +465,13 @@ class CrystalPlasticity:
             values.zero_()
             dw = self._buf("tangent_w", (81, G))
         its = self._buf("iters", (G,), torch.int32) if self.timing else None
-        trial = {}
-        if need_tangent:
-            # the trial state and stress of this pass are the post-processing of the step if
-            # it turns out to be the converged one (models_copper.py:273-282,297-319 re-solve)
-            N = self.num_slip
-            trial = {"stress": torch.empty((9, G), dtype=torch.float64, device=self.device),
-                     "fpi_new": torch.empty((9, G), dtype=torch.float64, device=self.device),
-                     "g_new": torch.empty((N, G), dtype=torch.float64, device=self.device),
-                     "slip_new": torch.empty((N, G), dtype=torch.float64, device=self.device)}
+        if need_tangent and trial is None:
+            trial = self.new_trial()
+        trial = trial if need_tangent else {}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its, **trial)
+                             iters=its, cell_list=cell_list, **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
-        if its is not None and need_tangent:
+        if its is not None and need_tangent and cell_list is None:
             acc = self._bufs.setdefault("iters_acc", torch.zeros(2, dtype=torch.float64, device=self.device))
             acc[0] += its.sum()
             acc[1] += G
@@ -479,6 +479,16 @@ class CrystalPlasticity:
         if trial:
             self._trial = (self._trial_key(u), u, trial, status)
         return res, values, status
+
+    def new_trial(self):
+        """Fresh trial-output buffers of a tangent pass: the trial state and stress of the
+        pass are the post-processing of the step if it turns out to be the converged one
+        (the reference re-solves for them, models_copper.py:273-282,297-319)."""
+        G, N = self.num_gp, self.num_slip
+        return {"stress": torch.empty((9, G), dtype=torch.float64, device=self.device),
+                "fpi_new": torch.empty((9, G), dtype=torch.float64, device=self.device),
+                "g_new": torch.empty((N, G), dtype=torch.float64, device=self.device),
+                "slip_new": torch.empty((N, G), dtype=torch.float64, device=self.device)}
 
     def scatter(self, pw, dw, res, values):
         """Element residual / tangent scatter, colour by colour (no atomics, fixed order)."""

@@ -12,6 +12,7 @@ pattern fixed at set-up, and the Dirichlet rows are eliminated in place.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import time
 
@@ -35,19 +36,21 @@ def norm(problem, x):
     return math.sqrt(_dot(problem, x, x))
 
 
-def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000):
+def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, restarts=0):
     """``jax.scipy.sparse.linalg.bicgstab`` on the device matrix (``solver.py:34-40``), one
     persistent cooperative launch.  precond: 0 none, 1 Jacobi 1/diag(A) (the
-    reference), 2 3x3 block-Jacobi.  Returns (x, iterations or breakdown code, converged)."""
+    reference), 2 3x3 block-Jacobi.  restarts > 0 restarts at a breakdown instead of
+    stopping there (jax stops).  Returns (x, iterations or breakdown code, converged)."""
     lib = problem.lib
     x = x0.clone()
     nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
+    opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
+                            float(tol), float(atol))
     with problem.region("bicgstab"):
-        _capi.check(lib.cpfem_bicgstab(problem.sell, _dev_ptr(A.values), _dev_ptr(b.contiguous()), _dev_ptr(x),
-                                       int(precond), 1 if A.transposed else 0, float(tol), float(atol),
-                                       int(maxiter), _dev_ptr(ws), info.ctypes.data, _stream()))
+        _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b.contiguous()), _dev_ptr(x),
+                                          ctypes.byref(opts), _dev_ptr(ws), info.ctypes.data, _stream()))
     return x, int(info[0]), bool(info[1])
 
 
@@ -57,8 +60,10 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
     opts = opts or {}
     pc = opts.get("precond", precond)
     pc = {True: 1, False: 0, "jacobi": 1, "block3": 2, "block_jacobi": 2}.get(pc, pc)
+    rs = opts.get("restart_on_breakdown", 0)
+    rs = 20 if rs is True else int(rs or 0)
     x, k, ok = bicgstab(problem, A, b, x0, precond=pc, tol=opts.get("tol", 1e-10),
-                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000))
+                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000), restarts=rs)
     problem.stats["krylov_iters"].append(k)
     r = A.matvec(x)
     r.sub_(b)

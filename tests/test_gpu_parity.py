@@ -190,8 +190,12 @@ def test_golden_case2_tantalum_on_gpu(pkg, gpu):
 
 def test_golden_case4_polycrystal_on_gpu(pkg, gpu):
     """calibration_case4 scenario 0: 20^3 voxels, 50 grains (Neper n50-id0), 304 steel,
-    80 steps to 2.5 %, mean sigma_zz over cells.  The reference solved with UMFPACK; the
-    free rigid rotation about z of its corner BCs does not change sigma_zz."""
+    80 steps to 2.5 %, mean sigma_zz over cells.  The reference solved with UMFPACK: the
+    corner BCs leave the rigid rotation about z free, and on that near-singular matrix
+    jax's BiCGSTAB stagnates into an exact rho = 0 breakdown in FP64 and hands Newton an
+    unconverged increment.  A direct solve has no such failure, so the linear solve here
+    restarts at breakdowns and runs to its tolerance; the free rotation does not change
+    sigma_zz."""
     problem_mod, solver_mod = gpu
     L = 0.0295
     mesh = pkg.box_mesh(20, 20, 20, L, L, L)
@@ -203,7 +207,8 @@ def test_golden_case4_polycrystal_on_gpu(pkg, gpu):
     nsteps = 80
     s, _ = _run_steps(prob, solver_mod, np.linspace(0, 0.025 * L, 81)[:nsteps + 1],
                       np.linspace(0, 2.5, 81)[:nsteps + 1], bcf,
-                      {"jax_solver": {}, "tol": 1e-7, "line_search_flag": True}, lambda sg: sg[:, 2, 2].mean())
+                      {"jax_solver": {"restart_on_breakdown": True}, "tol": 1e-7, "line_search_flag": True},
+                      lambda sg: sg[:, 2, 2].mean())
     gold = GOLD["case4_szz"][:nsteps]
     rel = np.abs((s - gold) / gold)
     assert rel.max() < 1e-5, rel
