@@ -206,6 +206,23 @@ def spmv_roofline(prob, torch, lib, reps=50):
     return t, alg_bytes, 2.0 * nnz
 
 
+# DRAM bytes (read + write) per launch from the ncu capture summarised in
+# profiles/dram_fcc32_loadstep.md, on the 32^3 benchmark matrix: the standalone SpMV and
+# the persistent BiCGSTAB (the matrix is read from HBM once per solve, then from L2).
+SPMV_DRAM_BYTES = {"c1": 72.4e6}
+KRYLOV_DRAM_BYTES_PER_LAUNCH = {"c1": 75.7e6}
+
+
+def krylov_iteration_cost(prob):
+    """Algorithmic bytes and FP64 flops of one BiCGSTAB iteration: two SpMVs (values, one
+    column index per 3x3 block, x and y once) and the vector phases as written (p/phat 5,
+    q 2, s/shat 4, t 2, x/r 8 vector reads+writes of 8*ndof bytes); flops 2 per stored
+    value per SpMV plus ~30 per dof (updates, Jacobi, six dot products)."""
+    nnz, nb, ndof = prob.nnz, prob.num_blocks, prob.num_total_dofs_all_vars
+    spmv = 8 * nnz + 4 * nb + 16 * ndof
+    return 2 * spmv + 21 * 8 * ndof, 4.0 * nnz + 30.0 * ndof
+
+
 def gp_flops_per_eval(num_slip, iters_mean, tangent=True):
     """Algorithmic FP64 flops of one GP update (FMA = 2; pow, div, sqrt = 1 each):
     per local iteration one residual (tau 12N, power/slip 6N, L_p 18N, 3x3 products and
@@ -221,48 +238,86 @@ def gp_flops_per_eval(num_slip, iters_mean, tangent=True):
     return setup + iters_mean * per_iter + tan + 60
 
 
-def cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters, budget_s=20.0):
-    """Oracle (numpy/scipy, 1 host thread) on a bounded sample of the workload, scaled
-    to s per load step: constitutive+tangent+assembly on a subset of cells x passes,
-    BiCGSTAB iterations on a matrix with the full 32^3 pattern."""
+def _oracle_pass_worker(job):
+    """One host process: the oracle's constitutive + tangent + element pass on a chunk of
+    cells, started at a common wall-clock instant; returns (start, end)."""
+    points, cells, quat, ori, spec, start_at = job
     from oracle import cpfem_oracle as O
-    import scipy.sparse as sp
-    spec = pkg.material.BENCH_STEEL
-    E = mesh.cells.shape[0]
-    sub = 2048
-    cells = mesh.cells[:sub]
     used, inv = np.unique(cells, return_inverse=True)
-    orc = O.OracleProblem(mesh.points[used], inv.reshape(cells.shape), O.FCC12, spec.C11, spec.C12, spec.C44,
-                          quat, ori[:sub], gss_initial=spec.gss_initial, h=spec.h, t_sat=spec.t_sat,
-                          gss_a=spec.gss_a, xm=spec.xm, r=spec.r, coplanar=True)
+    orc = O.OracleProblem(points[used], inv.reshape(cells.shape), O.FCC12, spec["C11"], spec["C12"], spec["C44"],
+                          quat, ori, gss_initial=spec["gss_initial"], h=spec["h"], t_sat=spec["t_sat"],
+                          gss_a=spec["gss_a"], xm=spec["xm"], r=spec["r"], coplanar=True)
     orc.dt = DT
     u = np.zeros(orc.ndof)
     u[2::3] = STRAIN_STEP * orc.points[:, 2]
-    t0 = time.perf_counter()
+    while time.time() < start_at:
+        time.sleep(0.001)
+    t0 = time.time()
     orc.newton_update(u)
-    t_asm = (time.perf_counter() - t0) * E / sub
-    # Krylov: iterations of the restated BiCGSTAB on the full pattern
-    dof = (3 * mesh.cells[:, :, None] + np.arange(3)).reshape(E, 24)
-    I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
-    J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
-    ndof = 3 * mesh.points.shape[0]
-    A = sp.csr_array((np.random.default_rng(0).random(I.size), (I, J)), shape=(ndof, ndof))
-    A.sum_duplicates()
-    A = A + sp.eye(ndof) * 100.0
-    b = np.ones(ndof)
-    d = A.diagonal()
-    it = 0
-    t0 = time.perf_counter()
-    while time.perf_counter() - t0 < budget_s / 2 and it < 200:
-        O.bicgstab(A, b, np.zeros(ndof), lambda v: v / d, tol=0.0, atol=0.0, maxiter=5)
-        it += 5
-    t_it = (time.perf_counter() - t0) / it
+    return t0, time.time()
+
+
+def _spmv_worker(job):
+    """One host process: `reps` products of its row block of the tangent pattern with the
+    full vector (plus the iteration's vector updates on its rows), from a common start."""
+    blk, ndof, reps, start_at = job
+    x = np.ones(ndof)
+    y = np.empty(blk.shape[0])
+    while time.time() < start_at:
+        time.sleep(0.001)
+    t0 = time.time()
+    for _ in range(reps):
+        y = blk @ x
+        y = blk @ x
+        for _k in range(5):        # p, s, x, r updates and the six dots on the block's rows
+            y = y + 0.5 * y
+    return t0, time.time()
+
+
+def cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters, cores=None, budget_s=20.0):
+    """The oracle (numpy/scipy) on the host cores, on a bounded sample of the workload,
+    scaled to s per load step.  Constitutive+tangent+assembly: `cores` spawned processes
+    each run the oracle pass on 2048 cells at the same time (wall time of the slowest, x the
+    passes per step, scaled to all cells).  Krylov: each process multiplies its row block
+    of the full 32^3 tangent pattern (two SpMVs + vector updates per iteration); the
+    iteration time is the slowest block's (synchronisation between iterations is not
+    charged, which favours the CPU)."""
+    import multiprocessing as mp
+    import scipy.sparse as sp
+    cores = cores or os.cpu_count() or 1
+    spec = pkg.material.BENCH_STEEL
+    sd = {k: getattr(spec, k) for k in ("C11", "C12", "C44", "gss_initial", "h", "t_sat", "gss_a", "xm", "r")}
+    E = mesh.cells.shape[0]
+    sub = 2048
+    nchunk = max(1, min(cores, E // sub))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(nchunk) as pool:
+        pool.map(abs, range(nchunk))        # start the workers before the common instant
+        start = time.time() + 3.0
+        jobs = [(mesh.points, mesh.cells[k * sub:(k + 1) * sub], quat, ori[k * sub:(k + 1) * sub], sd, start)
+                for k in range(nchunk)]
+        spans = pool.map(_oracle_pass_worker, jobs)
+        t_pass = max(b for _, b in spans) - min(a for a, _ in spans)
+        t_asm = t_pass * E / (sub * nchunk)
+        # Krylov on the full pattern, split into row blocks
+        dof = (3 * mesh.cells[:, :, None] + np.arange(3)).reshape(E, 24)
+        I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
+        J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
+        ndof = 3 * mesh.points.shape[0]
+        A = sp.csr_array((np.random.default_rng(0).random(I.size), (I, J)), shape=(ndof, ndof))
+        A.sum_duplicates()
+        rows = np.linspace(0, ndof, nchunk + 1).astype(np.int64)
+        reps = 40
+        start = time.time() + 3.0
+        spans = pool.map(_spmv_worker, [(A[rows[k]:rows[k + 1]], ndof, reps, start) for k in range(nchunk)])
+        t_it = (max(b for _, b in spans) - min(a for a, _ in spans)) / reps
     t_step = newton_passes * t_asm + krylov_iters * t_it
-    return {"value": 8 * E / t_step, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": 8 * E / t_step, "unit": UNIT, "cores": nchunk, "kind": "port",
             "s_per_load_step": t_step,
-            "sample": (f"oracle newton_update on {sub} of {E} cells (x{E // sub}) timed {t_asm:.2f}s/pass x "
-                       f"{newton_passes} passes + {it} BiCGSTAB iterations on the full {ndof}-dof pattern "
-                       f"({t_it * 1e3:.1f} ms/it) x {krylov_iters} iterations; counts from this GPU run")}
+            "sample": (f"oracle newton_update on {nchunk} processes x {sub} cells at once ({t_pass:.2f} s wall, "
+                       f"scaled to {E} cells: {t_asm:.2f} s/pass) x {newton_passes} passes + row-block "
+                       f"BiCGSTAB iterations of the full {ndof}-dof pattern on {nchunk} processes "
+                       f"({t_it * 1e3:.2f} ms/it, {reps} timed) x {krylov_iters} iterations")}
 
 
 def run_reference(args):
@@ -276,14 +331,12 @@ def run_reference(args):
     # counts of this workload's load steps measured on the GPU path (same algorithm)
     newton_passes, krylov_iters = REF_COUNTS["passes_per_step"], REF_COUNTS["krylov_iters_per_step"]
     vals = []
-    for k in range(args.warmup + args.steps):
-        r = cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters, budget_s=8.0)
-        if k >= args.warmup:
-            vals.append(r)
+    for k in range(max(1, min(args.steps, 2))):
+        vals.append(cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters))
     v = float(np.median([r["value"] for r in vals]))
     cb = dict(vals[-1])
     cb["value"] = v
-    cb["cores"] = 1
+    cb["sample"] += "; counts per step from the GPU path on this workload"
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 8 * N_EDGE ** 3 / v * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -297,7 +350,7 @@ def run_reference(args):
 # Per-load-step counts of this workload on the GPU path (tension steps 1..20):
 # constitutive+tangent passes (Newton iterations + 1) and BiCGSTAB iterations summed over
 # the step's linear solves.  Refreshed from the GPU bench run.
-REF_COUNTS = {"passes_per_step": 4, "krylov_iters_per_step": 1500}
+REF_COUNTS = {"passes_per_step": 6, "krylov_iters_per_step": 2630}
 
 
 def run_adjoint_config(args, pkg, problem_mod, torch):
@@ -464,6 +517,8 @@ def main():
     else:
         mesh, quat, ori = make_case(pkg, n)
     prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=spec)
+    counter = CountingLib(prob.lib)
+    prob.lib = counter
     st = Stepper(pkg, prob, solver_mod, mesh)
     st.precond = args.precond
     clk = ClockSampler(local).start()
@@ -484,12 +539,14 @@ def main():
     torch.cuda.synchronize()
     wall0 = time.time()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    counter.counting = True
     e0.record()
     for _ in range(args.steps):
         st.step()
         newton.append(prob.stats["newton_iters"])
     e1.record()
     torch.cuda.synchronize()
+    counter.counting = False
     wall1 = time.time()
     barrier()
     t = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, "cuda")
@@ -517,7 +574,7 @@ def main():
                "h2d_bytes_per_step": int(sol_h.numel() * 8), "d2h_bytes_per_step": int((sol_h.numel() + sig_h.numel()) * 8),
                "s_per_load_step": te / args.steps}
 
-    # roofline of the dominant kernel(s)
+    # roofline of the dominant kernel (the persistent BiCGSTAB) and of the constitutive pass
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     fp64 = fp64_peak(lib, torch)
@@ -527,21 +584,40 @@ def main():
     gp_t = gp_ms * 1e-3 / max(gp_n, 1)
     gp_flops = G * gp_flops_per_eval(prob.num_slip, its_t)
     kr_n, kr_ms = regions.get("bicgstab", (0, 0.0))
-    gp_share = (gp_ms + regions.get("gp_eval_post", (0, 0))[1]) / (t * 1e3)
-    kr_share = kr_ms / (t * 1e3)
-    spmv_roof = {"bound": "hbm", "achieved": spmv_bytes / t_spmv / 1e9, "peak": hbm, "unit": "GB/s",
-                 "frac": (spmv_bytes / t_spmv / 1e9) / hbm if hbm else None, "traffic": None,
-                 "kernel": "k_spmv (node-block CSR)", "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-                 "fp64_frac": (spmv_flops / t_spmv / 1e12) / fp64}
+    kr_its = sum(max(k, 0) for k in krylov)
+    kb, kf = krylov_iteration_cost(prob)
+    kr_roof = None
+    if kr_n and kr_ms > 0:
+        tflops = kf * kr_its / (kr_ms * 1e-3) / 1e12
+        gbs = kb * kr_its / (kr_ms * 1e-3) / 1e9
+        kr_roof = {"bound": "fp64", "achieved": tflops, "peak": fp64, "unit": "TFLOP/s", "frac": tflops / fp64,
+                   "traffic": (KRYLOV_DRAM_BYTES_PER_LAUNCH[args.config]
+                               if args.config in KRYLOV_DRAM_BYTES_PER_LAUNCH and n == N_EDGE else None),
+                   "traffic_note": "DRAM bytes per launch (ncu); algorithmic bytes per launch = "
+                                   "algorithmic_bytes_per_iteration x iterations, served from L2",
+                   "kernel": "k_bicgstab<0> (persistent BiCGSTAB, one launch per linear solve)",
+                   "launches": kr_n, "us_per_iteration": kr_ms * 1e3 / max(kr_its, 1),
+                   "algorithmic_bytes_per_iteration": kb, "flops_per_iteration": kf,
+                   "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm if hbm else None},
+                   "peak_source": "cpfem_probe_dfma FP64 (of measured); HBM from MEASURED_PEAKS.json (of measured)"}
+    spmv_roof = {"bound": "fp64", "achieved": spmv_flops / t_spmv / 1e12, "peak": fp64, "unit": "TFLOP/s",
+                 "frac": (spmv_flops / t_spmv / 1e12) / fp64, "traffic": SPMV_DRAM_BYTES.get(args.config) if n == N_EDGE else None,
+                 "kernel": "k_spmv (sliced-ELL, standalone)",
+                 "hbm": {"achieved": spmv_bytes / t_spmv / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": (spmv_bytes / t_spmv / 1e9) / hbm if hbm else None},
+                 "peak_source": "cpfem_probe_dfma FP64 (of measured); HBM from MEASURED_PEAKS.json (of measured)"}
     gp_roof = {"bound": "fp64", "achieved": gp_flops / gp_t / 1e12 if gp_t else None, "peak": fp64,
                "unit": "TFLOP/s", "frac": (gp_flops / gp_t / 1e12) / fp64 if gp_t else None, "traffic": None,
-               "kernel": "k_gp_eval<12,tangent>", "peak_source": "cpfem_probe_dfma (of measured)"}
-    dominant = spmv_roof if kr_share >= gp_share else gp_roof
+               "kernel": "k_gp_eval<N,tangent>", "peak_source": "cpfem_probe_dfma (of measured)"}
+    shares = {"bicgstab": kr_ms / (t * 1e3), "gp_eval_tangent": gp_ms / (t * 1e3),
+              "elem_assemble": regions.get("elem_assemble", (0, 0.0))[1] / (t * 1e3)}
+    dominant = kr_roof if (kr_roof is not None and shares["bicgstab"] >= shares["gp_eval_tangent"]) else gp_roof
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.config == "c1":
         kps = sum(max(k, 0) for k in krylov) / args.steps
         cpu = cpu_baseline_sample(pkg, mesh, quat, ori, passes / args.steps, kps)
+        cpu["sample"] += "; counts per step from this GPU run"
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
@@ -549,12 +625,14 @@ def main():
            "config": dict(workload_config(n, args.config), parallelism="replicas" if world > 1 else "single-gpu",
                           precond={0: "none", 1: "jacobi", 2: "block-jacobi-3x3"}[args.precond]),
            "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
-           "roofline": dominant, "roofline_kernels": {"spmv": spmv_roof, "gp_eval": gp_roof},
+           "roofline": dominant,
+           "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof},
+           "region_shares": shares,
            "cpu_baseline": cpu,
            "regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
            "newton_iters_per_step": newton, "krylov_iters": krylov, "gp_passes": passes,
            "gpu_launches": None}
-    out["gpu_launches"] = count_launches(regions, krylov)
+    out["gpu_launches"] = counter.launches
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -572,15 +650,31 @@ def max_over_ranks(t, world, device):
     return float(tt.item())
 
 
-def count_launches(regions, krylov):
-    """Our kernels launched in the timed region: one per gp_eval / elem_assemble call,
-    5 per BiCGSTAB iteration + precond + init per solve, plus dots, BC and axpy calls."""
-    n = 0
-    for k, (cnt, _) in regions.items():
-        if k.startswith("gp_eval") or k == "elem_assemble":
-            n += cnt
-    n += sum(5 * max(k, 0) + 2 for k in krylov)
-    return n
+class CountingLib:
+    """Forwards to the C ABI and counts the kernels its calls launch (a fixed number per
+    entry point, from the sources: the persistent BiCGSTAB is one launch plus the
+    preconditioner set-up; every other listed entry point launches one kernel)."""
+    LAUNCHES = {"cpfem_gp_eval": 1, "cpfem_elem_assemble": 1, "cpfem_apply_dirichlet": 1, "cpfem_dot": 1,
+                "cpfem_bc_initial_guess": 1, "cpfem_axpy": 1, "cpfem_spmv": 1, "cpfem_bicgstab": 2,
+                "cpfem_bicgstab_ex": 2, "cpfem_cell_average": 1, "cpfem_segmented_dot": 1,
+                "cpfem_bicgstab_batched": 2, "cpfem_gp_vjp": 1}
+
+    def __init__(self, lib):
+        self._lib = lib
+        self.launches = 0
+        self.counting = False
+
+    def __getattr__(self, name):
+        f = getattr(self._lib, name)
+        k = self.LAUNCHES.get(name)
+        if k is None:
+            return f
+
+        def call(*a):
+            if self.counting:
+                self.launches += k
+            return f(*a)
+        return call
 
 
 if __name__ == "__main__":

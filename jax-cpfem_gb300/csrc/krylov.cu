@@ -26,8 +26,8 @@ constexpr int kMaxBlocks = 2048;
 constexpr long long kSpinLimit = 1LL << 25;   // ~1-3 s of polling at ~50 ns per poll
 
 struct GridSync {
-  unsigned int count;
-  unsigned int gen;
+  unsigned int count;   // arrivals so far (monotonic within a launch)
+  unsigned int gen;     // unused (kept for the layout)
   int error;
   int pad;
 };
@@ -165,37 +165,49 @@ __device__ __forceinline__ void apply_m(int precond, const double* __restrict__ 
   }
 }
 
-// Sense-counting grid barrier for a cooperative launch, with a bounded wait.
-__device__ __forceinline__ bool grid_barrier(GridSync* gs, unsigned int& gen) {
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_add_u32(unsigned int* p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Barrier over the nb blocks that share gs (the whole grid of a cooperative launch, or a
+// team of it).  gs->count only grows (it is zeroed before the launch): the k-th barrier is
+// complete when it reaches k*nb.  Thread 0 arrives with a release reduction, which
+// publishes every write the block made before the __syncthreads, and waits with acquire
+// loads; no reset is needed, so the last arrival costs no extra round trip.  The wait is
+// bounded: after kSpinLimit polls the block records an error (also in *gerr) and returns
+// false instead of hanging.
+__device__ __forceinline__ bool counted_barrier(GridSync* gs, unsigned int nb, unsigned int& gen, int* gerr) {
   __shared__ int s_ok;
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned int my = gen;
+    const unsigned int target = (gen + 1u) * nb;
     int ok = 1;
-    const unsigned int arrived = atomicAdd(&gs->count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&gs->count, 0u);
-      __threadfence();
-      atomicExch(&gs->gen, my + 1u);
-    } else {
-      volatile unsigned int* vg = &gs->gen;
-      long long spins = 0;
-      while (*vg == my) {
-        if (++spins > kSpinLimit) {
-          ok = 0;
-          atomicExch(&gs->error, 1);
-          break;
-        }
-        __nanosleep(32);
+    red_release_add_u32(&gs->count, 1u);
+    long long spins = 0;
+    while (ld_acquire_u32(&gs->count) < target) {
+      if (++spins > kSpinLimit) {
+        ok = 0;
+        atomicExch(&gs->error, 1);
+        if (gerr != nullptr) atomicExch(gerr, 1);
+        break;
       }
+      if (spins > 32) __nanosleep(32);
     }
-    __threadfence();
     s_ok = ok && (*(volatile int*)&gs->error == 0);
   }
   __syncthreads();
   gen += 1u;
   return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier(GridSync* gs, unsigned int& gen) {
+  return counted_barrier(gs, gridDim.x, gen, nullptr);
 }
 
 // Publish this block's NV partial sums, cross the grid barrier, and reduce all blocks'
@@ -228,7 +240,7 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* partials, G
 }
 
 template <bool TRANS>
-__global__ void __launch_bounds__(kPThreads) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
+__global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
                                                         const double* __restrict__ b, double* __restrict__ x,
                                                         KWork w, int precond, double tol, double atol,
                                                         int maxiter, int max_restarts) {
@@ -573,38 +585,8 @@ static size_t carve_ragged(void* base, int64_t n_nodes, RWork* w) {
   return off;
 }
 
-// Barrier over the nb blocks of a team (bounded wait, as grid_barrier).
 __device__ __forceinline__ bool team_barrier(GridSync* gs, unsigned int nb, unsigned int& gen, int* gerr) {
-  __shared__ int s_ok;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned int my = gen;
-    int ok = 1;
-    const unsigned int arrived = atomicAdd(&gs->count, 1u);
-    if (arrived == nb - 1) {
-      atomicExch(&gs->count, 0u);
-      __threadfence();
-      atomicExch(&gs->gen, my + 1u);
-    } else {
-      volatile unsigned int* vg = &gs->gen;
-      long long spins = 0;
-      while (*vg == my) {
-        if (++spins > kSpinLimit) {
-          ok = 0;
-          atomicExch(&gs->error, 1);
-          atomicExch(gerr, 1);
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-    s_ok = ok && (*(volatile int*)&gs->error == 0);
-  }
-  __syncthreads();
-  gen += 1u;
-  return s_ok != 0;
+  return counted_barrier(gs, nb, gen, gerr);
 }
 
 // Team-wide sums of NV values: block sum, then (teams of several blocks) publish, barrier
@@ -643,7 +625,7 @@ __device__ __forceinline__ bool team_reduce(double (&v)[NV], double* partials, i
   return ok;
 }
 
-__global__ void __launch_bounds__(kPThreads) k_bicgstab_ragged(
+__global__ void __launch_bounds__(kPThreads, 3) k_bicgstab_ragged(
     const cpfem_sell_t L, const double* __restrict__ vals, const double* __restrict__ b, double* __restrict__ x,
     RWork w, int precond, double tol, double atol, int maxiter, int n_jobs) {
   __shared__ double smem[4 * 32];

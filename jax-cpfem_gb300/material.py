@@ -45,6 +45,12 @@ class MaterialSpec:
     discarded (``crystal_plasticity_OR_design/models_sens_rot.py:170-175``).
     ``per_gp_params`` selects the internal-variable layout: False gives the 4-entry
     list of the plain models, True the 9-entry list of the parameterised ones.
+    ``phases`` makes a multi-phase material (``polycrystal_DPsteel/models_DPsteel_inhomo.py``):
+    one spec per phase supplies that phase's elastic constants, initial slip resistance
+    and Kalidindi parameters, each cell belongs to one phase, and the internal variables
+    are the 10-entry list of that model (the 9 entries plus the lattice-frame stiffness
+    C per GP, ``models_DPsteel_inhomo.py:229``).  ``phase1_fraction`` is the volume
+    fraction of phase 1 when the cells' phases are drawn the way that model draws them.
     """
     C11: float
     C12: float
@@ -62,6 +68,8 @@ class MaterialSpec:
     local_tol: float = 1e-8
     max_sub_step: int = 5
     max_iter: int = 300
+    phases: tuple = ()
+    phase1_fraction: float = 0.4
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)
@@ -96,6 +104,13 @@ class MaterialSpec:
         """(gss_a, h, t_sat, xm, r) -- the order of the parameterised internal variables."""
         return np.array([self.gss_a, self.h, self.t_sat, self.xm, self.r], dtype=np.float64)
 
+    def elastic_row(self):
+        return np.array([self.C11, self.C12, self.C44], dtype=np.float64)
+
+    @property
+    def num_internal_vars(self):
+        return 10 if self.phases else (9 if self.per_gp_params else 4)
+
 
 # Constants of the reference models (file:line of each ``custom_init`` / ``get_maps``).
 COPPER = MaterialSpec(  # singlecrystal_copper/models_copper.py:55-56,94-96,141-149
@@ -124,6 +139,15 @@ BENCH_STEEL = MaterialSpec(
 BENCH_TANTALUM = MaterialSpec(
     C11=267.0e3, C12=161.0e3, C44=82.5e3, gss_initial=160.0, h=150.0, t_sat=300.0, gss_a=1.5,
     xm=0.05, r=1.4, slip="bcc24", coplanar_q=True)
+
+# Dual-phase steel, ferrite (phase 0) + martensite (phase 1), BCC24 with the coplanar
+# 3-block q (polycrystal_DPsteel/models_DPsteel_inhomo.py:55-100,145-179,257-266).
+DP_FERRITE = MaterialSpec(
+    C11=2.314e5, C12=1.347e5, C44=1.164e5, gss_initial=170.0, h=400.0, t_sat=2500.0, gss_a=4.0,
+    xm=0.05, r=1.0, slip="bcc24", coplanar_q=True, per_gp_params=True, local_tol=1e-8, max_sub_step=5)
+DP_MARTENSITE = DP_FERRITE.replace(C11=4.174e5, C12=2.424e5, C44=2.111e5, gss_initial=435.0, h=950.0,
+                                   t_sat=5300.0)
+DP_STEEL = DP_FERRITE.replace(phases=(DP_FERRITE, DP_MARTENSITE), phase1_fraction=0.4)
 
 
 def rot_mat(quat):
@@ -160,6 +184,31 @@ def euler_zyx_deg(angles):
     return Rx @ Ry @ Rz
 
 
+def cubic_tensor(rows):
+    """(..., 3) rows of (C11, C12, C44) -> (..., 3, 3, 3, 3) cubic stiffness in the lattice
+    frame, as the reference fills C (``models_copper.py:92-130``)."""
+    rows = np.asarray(rows, dtype=np.float64)
+    C = np.zeros(rows.shape[:-1] + (3, 3, 3, 3))
+    for i in range(3):
+        for j in range(3):
+            C[..., i, i, j, j] = rows[..., 0] if i == j else rows[..., 1]
+            if i != j:
+                C[..., i, j, i, j] = rows[..., 2]
+                C[..., i, j, j, i] = rows[..., 2]
+    return C
+
+
+def cubic_constants(C, tol=1e-9):
+    """Inverse of ``cubic_tensor`` for (..., 3, 3, 3, 3) arrays; raises unless C has the
+    cubic form (the constitutive kernel stores three constants per stiffness)."""
+    C = np.asarray(C, dtype=np.float64)
+    rows = np.stack([C[..., 0, 0, 0, 0], C[..., 0, 0, 1, 1], C[..., 1, 2, 1, 2]], -1)
+    scale = max(float(np.abs(C).max()) if C.size else 1.0, 1e-300)
+    if C.size and float(np.abs(cubic_tensor(rows) - C).max()) > tol * scale:
+        raise ValueError("per-GP stiffness must have the cubic form (C11, C12, C44) in the lattice frame")
+    return rows
+
+
 def random_quaternions(rng, n):
     """Uniform orientations on SO(3): normalised Gaussian quaternions."""
     q = rng.normal(size=(n, 4))
@@ -179,4 +228,5 @@ def check_orthonormal(R, tol=1e-10):
 
 __all__ = ["MaterialSpec", "FCC12", "BCC12", "BCC24", "SLIP_SYSTEMS", "rot_mat", "euler_zyx_deg",
            "random_quaternions", "check_orthonormal", "COPPER", "CALIB_CASE1", "CALIB_CASE2",
-           "CALIB_CASE4", "SENS_ROT", "STEEL304", "TANTALUM", "BENCH_COPPER", "BENCH_STEEL", "BENCH_TANTALUM"]
+           "CALIB_CASE4", "SENS_ROT", "STEEL304", "TANTALUM", "BENCH_COPPER", "BENCH_STEEL", "BENCH_TANTALUM",
+           "DP_FERRITE", "DP_MARTENSITE", "DP_STEEL", "cubic_tensor", "cubic_constants"]

@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from . import _capi
-from .material import COPPER, MaterialSpec, check_orthonormal, rot_mat
+from .material import COPPER, MaterialSpec, check_orthonormal, cubic_constants, cubic_tensor, rot_mat
 from .mesh import Mesh, shape_grads_jxw
 
 
@@ -278,9 +278,14 @@ class CrystalPlasticity:
             self._bufs[name] = b
         return b
 
-    def custom_init(self, quat, cell_ori_inds):
+    def custom_init(self, quat, cell_ori_inds, phase_inds=None):
         """State at the start of the load history (``models_copper.py:52-133``):
-        Fp^-1 = I, g = g0, slip = 0, rotation of the cell's orientation at every GP."""
+        Fp^-1 = I, g = g0, slip = 0, rotation of the cell's orientation at every GP.
+        A multi-phase material (``MaterialSpec.phases``) also takes each cell's phase:
+        ``phase_inds`` if given, else drawn as ``models_DPsteel_inhomo.py:54-62`` draws it
+        (the first int(E * phase1_fraction) cells are phase 1, then numpy's global
+        shuffle), and per-phase g0, parameters and stiffness
+        (``models_DPsteel_inhomo.py:102-110,184-186,219-229``)."""
         spec = self.material
         E, Q, N, G = self.num_cells, 8, self.num_slip, self.num_gp
         quat = np.asarray(quat, dtype=np.float64).reshape(-1, 4)
@@ -291,15 +296,32 @@ class CrystalPlasticity:
         dev = self.device
         self.rot_table = torch.tensor(R.reshape(-1, 9), dtype=torch.float64, device=dev)
         self.rot_idx = torch.tensor(np.repeat(idx, Q), dtype=torch.int32, device=dev)
-        self.param_table = torch.tensor(spec.param_row()[None, :], dtype=torch.float64, device=dev)
-        self.param_idx = None
-        self.elastic_table = None
         self.fpi = torch.zeros((9, G), dtype=torch.float64, device=dev)
         self.fpi[0] = 1.0
         self.fpi[4] = 1.0
         self.fpi[8] = 1.0
-        self.g = torch.full((N, G), float(spec.gss_initial), dtype=torch.float64, device=dev)
         self.slip = torch.zeros((N, G), dtype=torch.float64, device=dev)
+        if spec.phases:
+            if phase_inds is None:
+                phase_inds = np.zeros(E, dtype=np.int64)
+                phase_inds[:int(E * spec.phase1_fraction)] = 1
+                np.random.shuffle(phase_inds)
+            phase_inds = np.asarray(phase_inds, dtype=np.int64).reshape(-1)
+            if phase_inds.shape[0] != E or phase_inds.min() < 0 or phase_inds.max() >= len(spec.phases):
+                raise ValueError("phase_inds needs one phase index per cell, within the material's phases")
+            self.phase_inds = phase_inds
+            self.param_table = torch.tensor(np.stack([ph.param_row() for ph in spec.phases]), dtype=torch.float64,
+                                            device=dev)
+            self.elastic_table = torch.tensor(np.stack([ph.elastic_row() for ph in spec.phases]),
+                                              dtype=torch.float64, device=dev)
+            self.param_idx = torch.tensor(np.repeat(phase_inds, Q), dtype=torch.int32, device=dev)
+            g0 = torch.tensor([ph.gss_initial for ph in spec.phases], dtype=torch.float64, device=dev)
+            self.g = g0[self.param_idx.long()].expand(N, G).contiguous()
+        else:
+            self.param_table = torch.tensor(spec.param_row()[None, :], dtype=torch.float64, device=dev)
+            self.param_idx = None
+            self.elastic_table = None
+            self.g = torch.full((N, G), float(spec.gss_initial), dtype=torch.float64, device=dev)
         self._views = None
         self._post_cache = None
         self._trial = None
@@ -311,10 +333,15 @@ class CrystalPlasticity:
         views = [self.fpi.t().reshape(E, Q, 3, 3), self.g.t().reshape(E, Q, N),
                  self.slip.t().reshape(E, Q, N),
                  self.rot_table[self.rot_idx.long()].reshape(E, Q, 3, 3)]
-        if self.material.per_gp_params:
+        if self.material.per_gp_params or self.material.phases:
             tab = self.param_table if self.param_idx is None else self.param_table[self.param_idx.long()]
             tab = tab.expand(G, 5) if tab.shape[0] == 1 else tab
             views += [tab[:, k].reshape(E, Q) for k in range(5)]
+        if self.material.phases:
+            el = self.elastic_table if self.param_idx is None else self.elastic_table[self.param_idx.long()]
+            el = el.expand(G, 3) if el.shape[0] == 1 else el
+            C = torch.as_tensor(cubic_tensor(el.cpu().numpy()), device=self.device)
+            views.append(C.reshape(E, Q, 3, 3, 3, 3))
         return views
 
     @property
@@ -348,7 +375,7 @@ class CrystalPlasticity:
 
     def _adopt(self, params):
         spec = self.material
-        expect = 9 if spec.per_gp_params else 4
+        expect = spec.num_internal_vars
         if len(params) != expect:
             raise ValueError(f"expected {expect} internal variables, got {len(params)}")
         old = self._views
@@ -362,17 +389,19 @@ class CrystalPlasticity:
             check_orthonormal(table.cpu().numpy())
             self.rot_table = table.contiguous()
             self.rot_idx = inv.to(torch.int32).contiguous()
-        if spec.per_gp_params:
-            if old is None or any(params[4 + k] is not old[4 + k] for k in range(5)):
+        if spec.phases:
+            if old is None or any(params[4 + k] is not old[4 + k] for k in range(6)):
+                # one row per distinct (parameters, stiffness) combination
                 P = torch.stack([torch.as_tensor(params[4 + k], dtype=torch.float64, device=self.device).reshape(G)
                                  for k in range(5)], dim=1)
-                if bool((P == P[:1]).all()):
-                    self.param_table = P[:1].contiguous()
-                    self.param_idx = None
-                else:
-                    self.param_table = P.contiguous()
-                    self.param_idx = torch.arange(G, dtype=torch.int32, device=self.device)
-        new_views = self._make_views()
+                el = torch.as_tensor(cubic_constants(torch.as_tensor(params[9]).detach().cpu().numpy()
+                                                     .reshape(G, 3, 3, 3, 3)), device=self.device)
+                rows, inv = torch.unique(torch.cat([P, el], dim=1), dim=0, return_inverse=True)
+                self.param_table = rows[:, :5].contiguous()
+                self.elastic_table = rows[:, 5:].contiguous()
+                self.param_idx = inv.to(torch.int32).contiguous()
+        elif spec.per_gp_params:
+            if old is None or any(params[4 + k] is not old[4 + k] for k in range(5)):        new_views = self._make_views()
         # keep the caller's objects for the entries adopted as they are
         self._views = [params[k] if (k >= 3 and old is not None and params[k] is old[k]) else new_views[k]
                        for k in range(len(params))]
@@ -390,7 +419,7 @@ class CrystalPlasticity:
         return [dofs.reshape(self.num_nodes, 3)]
 
     # ------------------------------------------------------------------ GPU passes
-    def _gp_args(self, state, dt, u=None, u_grad=None, num_gp=None, **outs):
+    def _gp_args(self, state, dt, u=None, u_grad=None, num_gp=None, elastic=None, **outs):
         a = _capi.GPArgs()
         fpi, g, slip, rot_table, rot_idx, param_table, param_idx = state
         a.num_gp = self.num_gp if num_gp is None else num_gp
@@ -404,7 +433,10 @@ class CrystalPlasticity:
         a.fpi, a.g, a.slip = _dev_ptr(fpi), _dev_ptr(g), _dev_ptr(slip)
         a.rot_table, a.rot_idx = _dev_ptr(rot_table), _dev_ptr(rot_idx)
         a.param_table, a.param_idx = _dev_ptr(param_table), _dev_ptr(param_idx)
-        a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
+        if elastic is not None:
+            a.elastic_table = _dev_ptr(elastic)
+        else:
+            a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
         a.weight_jxw = 1 if outs.pop("weight_jxw", False) else 0
         cl = outs.pop("cell_list", None)
         if cl is not None:
@@ -547,10 +579,14 @@ class CrystalPlasticity:
         rot_table, inv = torch.unique(R, dim=0, return_inverse=True)
         check_orthonormal(rot_table.cpu().numpy())
         rot_idx = inv.to(torch.int32).contiguous()
-        if self.material.per_gp_params and len(ivars) >= 9:
+        etab = None
+        if (self.material.per_gp_params or self.material.phases) and len(ivars) >= 9:
             ptab = torch.stack([torch.as_tensor(ivars[4 + k], dtype=torch.float64,
                                                 device=self.device).reshape(n) for k in range(5)], 1).contiguous()
             pidx = torch.arange(n, dtype=torch.int32, device=self.device)
+            if len(ivars) >= 10:
+                C = torch.as_tensor(ivars[9]).detach().cpu().numpy().reshape(n, 3, 3, 3, 3)
+                etab = torch.as_tensor(cubic_constants(C), dtype=torch.float64, device=self.device).contiguous()
         else:
             ptab = torch.tensor(self.material.param_row()[None, :], dtype=torch.float64, device=self.device)
             pidx = None
@@ -563,7 +599,7 @@ class CrystalPlasticity:
         its = torch.empty((n,), dtype=torch.int32, device=self.device)
         status = torch.zeros((1,), dtype=torch.int32, device=self.device)
         args = self._gp_args((fpi, g, slip, rot_table, rot_idx, ptab, pidx), self.dt if dt is None else dt,
-                             u_grad=ug, num_gp=n, pk1=P, tangent=D, fpi_new=fn, g_new=gn, slip_new=sn,
+                             u_grad=ug, num_gp=n, elastic=etab, pk1=P, tangent=D, fpi_new=fn, g_new=gn, slip_new=sn,
                              iters=its, status=status)
         self._run_gp(args)
         if check:

@@ -10,6 +10,9 @@ Reads (paths relative to the reference project root):
   polycrystal_304steel/data/vtk/polycrystal_304steel/u_000..015.vtu     per-cell stresses, 16^3, 8 grains
   polycrystal_304steel/data/csv/polycrystal_304steel/quat.txt            its orientations
   singlecrystal_tantalum/data/vtk/singlecrystal_tantalum/u_000..049.vtu  per-cell stresses, 10^3 single crystal
+  polycrystal_DPsteel/data/vtk/polycrystal_DPsteel/u_inhomo_000..049.vtu  per-cell stresses, phases and
+                                                                          orientation indices, 10^3 DP steel
+  polycrystal_DPsteel/data/csv/polycrystal_DPsteel/quat.txt              its orientations (8 rows)
 and writes ``golden.npz``.  The Neper meshes (20^3 of case 4, 16^3 of the 304-steel VTUs,
 10^3 of the tantalum VTUs) are checked to be structured boxes with x-fastest node
 numbering, so only per-cell grain ids are stored.  The VTU fields are float32 (meshio).
@@ -69,10 +72,20 @@ def main():
     bp, bc = box_mesh(10, 10, 10, L, L, L)
     assert np.abs(bp - ta[0]["points"]).max() < 1e-12 and (bc == ta[0]["cells"]).all()
     ta_szz = np.stack([r["cell_data"]["sigma_zz"] for r in ta])
+    ddir = os.path.join(REF, "polycrystal_DPsteel/data/vtk/polycrystal_DPsteel")
+    dp = [vtu.read_vtu(os.path.join(ddir, f"u_inhomo_{i:03d}.vtu")) for i in range(50)]
+    bp, bc = box_mesh(10, 10, 10, 2.0, 2.0, 2.0)
+    assert np.abs(bp - dp[0]["points"]).max() < 1e-12 and (bc == dp[0]["cells"]).all()
+    dp_phase = dp[0]["cell_data"]["phase_inds"].astype(np.int8)
+    dp_ori = dp[0]["cell_data"]["cell_ori_inds"].astype(np.int16)
+    assert all((r["cell_data"]["phase_inds"] == dp_phase).all() for r in dp)
+    dp_sig = np.stack([np.stack([r["cell_data"][f"sigma_{c}"] for c in ("xx", "yy", "zz")]) for r in dp])
+    dp_quat = np.loadtxt(os.path.join(REF, "polycrystal_DPsteel/data/csv/polycrystal_DPsteel/quat.txt"))[:20, 1:]
     np.savez_compressed(os.path.join(HERE, "golden.npz"), case1_szz=case1, case2_szz=case2,
                         case4_szz=c4zz, case4_sxx=c4xx, case4_quat=quat,
                         case4_grain=grains.astype(np.int16), steel_sig=steel_sig, steel_ori=steel_ori,
-                        steel_quat=steel_quat, ta_szz=ta_szz, ta_L=np.array(L))
+                        steel_quat=steel_quat, ta_szz=ta_szz, ta_L=np.array(L), dp_sig=dp_sig,
+                        dp_phase=dp_phase, dp_ori=dp_ori, dp_quat=dp_quat)
     print("wrote golden.npz", case1.shape, case2.shape, c4zz.shape, c4xx.shape, quat.shape, grains.shape)
 
 

@@ -209,3 +209,23 @@ def test_cell_colouring_is_conflict_free(lib, pkg, shape):
     for c in range(nc[0]):
         nodes = cells[color == c].ravel()
         assert np.unique(nodes).size == nodes.size
+
+
+def test_multiphase_spec_and_golden_dp_fixture(pkg):
+    """The dual-phase spec mirrors models_DPsteel_inhomo.py (BCC24, coplanar 3-block q,
+    10 internal variables), cubic C round-trips, and the DP golden fixture is coherent."""
+    m = pkg.material
+    spec = m.DP_STEEL
+    assert spec.num_internal_vars == 10 and spec.num_slip == 24 and spec.to_ctypes().qmode == 1
+    assert [p.gss_initial for p in spec.phases] == [170.0, 435.0]
+    rows = np.stack([p.elastic_row() for p in spec.phases])
+    np.testing.assert_array_equal(m.cubic_constants(m.cubic_tensor(rows)), rows)
+    bad = m.cubic_tensor(rows)
+    bad[0, 0, 1, 0, 2] = 1.0
+    with pytest.raises(ValueError):
+        m.cubic_constants(bad)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+    assert np.bincount(g["dp_phase"]).tolist() == [600, 400]
+    assert g["dp_ori"].max() >= g["dp_quat"].shape[0]          # clamped indices occur
+    assert np.abs(np.linalg.norm(g["dp_quat"], axis=1) - 1).max() < 1e-12
+    assert g["dp_sig"].shape == (50, 3, 1000)

@@ -1,0 +1,91 @@
+"""Multi-phase materials (per-GP stiffness and parameters, the 10-entry internal variables
+of polycrystal_DPsteel/models_DPsteel_inhomo.py) on the GPU: the Gauss-point update
+against the oracle, and the dual-phase steel driver against the reference's VTU output."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cpfem_oracle as O
+from tests.common import gpu_problem, random_gp_inputs
+
+pytestmark = pytest.mark.gpu
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+
+
+def _rel(a, b):
+    a = a.detach().cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def test_gp_update_with_per_gp_stiffness_matches_oracle(pkg, gpu):
+    problem_mod, _ = gpu
+    spec = pkg.material.DP_STEEL
+    prob = gpu_problem(pkg, problem_mod, spec, pkg.box_mesh(1, 1, 1), [[1, 0, 0, 0]], [0])
+    prob.dt = 0.2
+    rng = np.random.default_rng(21)
+    n = 193
+    ug, fpi, g, slip, R = random_gp_inputs(rng, n, 24, strain=2e-3)
+    g = g + 150.0
+    phase = rng.integers(0, 2, n)
+    rows = np.stack([spec.phases[p].param_row() for p in phase])
+    el = np.stack([spec.phases[p].elastic_row() for p in phase])
+    C = pkg.material.cubic_tensor(el)
+    P, D, state, its = prob.gp_map(ug, fpi, g, slip, R, *[rows[:, k] for k in range(5)], C)
+    Pr = np.einsum("gia,gjb,kab->gkij", R, R, O.schmid_tensors(O.SLIP_TABLES["bcc24"]))
+    Cr = np.einsum("gia,gjb,gkc,gld,gabcd->gijkl", R, R, R, R, C)
+    b = O.GPBatch(np.eye(3) + ug, fpi, g, Pr, Cr, rows[:, 3], spec.ao, 0.2)
+    S, its_o, ok = O.local_newton(b, spec.local_tol, spec.max_sub_step)
+    assert ok.all() and its.cpu().numpy().max() > 1
+    assert _rel(P, O.first_pk_stress(b, S)) < 1e-9
+    assert _rel(D, O.tangent(b, S)) < 1e-8
+    Fn, gn, sn = O.hardening_update(S, b, g, slip, rows[:, 1], rows[:, 2], rows[:, 0], rows[:, 4], True)
+    assert _rel(state[0], Fn) < 1e-12 and _rel(state[1], gn) < 1e-10 and _rel(state[2], sn) < 1e-9
+
+
+def test_dp_steel_internal_vars_layout(pkg, gpu):
+    problem_mod, _ = gpu
+    spec = pkg.material.DP_STEEL
+    mesh = pkg.box_mesh(2, 2, 2)
+    phase = np.array([0, 1, 1, 0, 0, 0, 1, 0])
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(GOLD["dp_quat"], np.arange(8), phase), material=spec)
+    iv = prob.internal_vars
+    assert len(iv) == 10 and tuple(iv[9].shape) == (8, 8, 3, 3, 3, 3)
+    assert float(iv[1][1, 0, 0]) == 435.0 and float(iv[1][0, 0, 0]) == 170.0
+    assert float(iv[9][2, 3, 0, 0, 0, 0]) == 4.174e5 and float(iv[5][3, 1]) == 400.0
+    # a list built by the caller (copies) is adopted into the same tables
+    prob.set_params([t.clone() for t in iv])
+    assert prob.param_table.shape[0] == 2 and prob.elastic_table.shape[0] == 2
+
+
+def test_golden_dp_steel_on_gpu(pkg, gpu):
+    """polycrystal_DPsteel_inhomo.py: 10^3 cells of 2 mm, ferrite/martensite phases and
+    orientation indices as stored in its VTU output (indices past the 8 orientations clamp,
+    as JAX indexing does), rollers + pulled top, 50 steps to 1 % with line search;
+    per-cell sigma_zz against the float32 fields of u_inhomo_*.vtu."""
+    problem_mod, solver_mod = gpu
+    spec = pkg.material.DP_STEEL
+    mesh = pkg.box_mesh(10, 10, 10, 2.0, 2.0, 2.0)
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(GOLD["dp_quat"], GOLD["dp_ori"].astype(np.int64),
+                                                                GOLD["dp_phase"].astype(np.int64)), material=spec)
+    P = mesh.points
+    fn = pkg.mesh.face_nodes
+    nodes = [fn(P, 0, 0.0), fn(P, 1, 0.0), fn(P, 2, 0.0), fn(P, 2, 2.0)]
+    disps, ts = np.linspace(0.0, 0.02, 51), np.linspace(0.0, 10.0, 51)
+    nsteps = int(os.environ.get("CPFEM_DP_STEPS", "50"))
+    sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
+    params = prob.internal_vars
+    worst = 0.0
+    for i in range(nsteps):
+        prob.dt = float(ts[i + 1] - ts[i])
+        prob.fes[0].set_dirichlet_lists(nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, float(disps[i + 1])])
+        prob.set_params(params)
+        sol = solver_mod.solver(prob, {"jax_solver": {}, "initial_guess": [sol.reshape(-1, 3)],
+                                       "line_search_flag": True})[0].reshape(-1)
+        sig = prob.compute_avg_stress(sol.reshape(-1, 3), params).cpu().numpy()
+        params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
+        gold = GOLD["dp_sig"][i, 2].astype(np.float64)
+        worst = max(worst, float(np.abs(sig[:, 2, 2] - gold).max() / np.abs(gold).max()))
+        assert abs(sig[:, 2, 2].mean() - gold.mean()) / abs(gold.mean()) < 1e-5, (i, sig[:, 2, 2].mean(), gold.mean())
+    assert worst < 1e-4, worst
