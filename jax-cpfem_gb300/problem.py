@@ -401,7 +401,16 @@ class CrystalPlasticity:
                 self.elastic_table = rows[:, 5:].contiguous()
                 self.param_idx = inv.to(torch.int32).contiguous()
         elif spec.per_gp_params:
-            if old is None or any(params[4 + k] is not old[4 + k] for k in range(5)):        new_views = self._make_views()
+            if old is None or any(params[4 + k] is not old[4 + k] for k in range(5)):
+                P = torch.stack([torch.as_tensor(params[4 + k], dtype=torch.float64, device=self.device).reshape(G)
+                                 for k in range(5)], dim=1)
+                if bool((P == P[:1]).all()):
+                    self.param_table = P[:1].contiguous()
+                    self.param_idx = None
+                else:
+                    self.param_table = P.contiguous()
+                    self.param_idx = torch.arange(G, dtype=torch.int32, device=self.device)
+        new_views = self._make_views()
         # keep the caller's objects for the entries adopted as they are
         self._views = [params[k] if (k >= 3 and old is not None and params[k] is old[k]) else new_views[k]
                        for k in range(len(params))]
