@@ -305,12 +305,54 @@ int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double*
  * calibration/case4.py) stagnate into exact rho = 0 in FP64; restarting lets the solve
  * reach its tolerance instead of returning an unconverged increment.
  */
+/*
+ * Geometric multigrid hierarchy of a structured box of nodes (x fastest, the numbering of
+ * box meshes and of the reference's Neper voxel meshes), the BiCGSTAB preconditioner
+ * precond = 3.  No reference counterpart: the reference preconditions with Jacobi
+ * (jax_solve, crystal_plasticity_OR_design/solver.py:32-33) or PETSc's ILU/Jacobi
+ * (solver.py:63-88).  One V-cycle of damped 3x3 block-Jacobi smoothing on every level,
+ * trilinear prolongation P (zero on Dirichlet dofs of level 0), restriction P^T and
+ * Galerkin coarse operators P^T A P rebuilt from the current tangent by cpfem_mg_setup.
+ * The preconditioner only changes the Krylov iterates: the solve still stops on the
+ * same true-residual tolerance.  Level l+1 has (dims[l][d]-1)/2+1 nodes per direction
+ * (every dims[l][d]-1 even).  The caller owns every array.
+ */
+#define CPFEM_MG_MAX_LEVELS 8
 typedef struct {
-  int32_t precond;        /* 0 none, 1 Jacobi (the reference), 2 3x3 block-Jacobi */
-  int32_t transpose;      /* solve A^T x = b */
+  int32_t num_levels;      /* 2..CPFEM_MG_MAX_LEVELS; level 0 is the system being solved */
+  int32_t pre_sweeps;      /* smoothing sweeps before restriction (>= 1; the first from zero) */
+  int32_t post_sweeps;     /* smoothing sweeps after prolongation (>= 0) */
+  int32_t coarse_sweeps;   /* sweeps on the coarsest level (>= 1) */
+  double omega;            /* damping of the block-Jacobi smoother */
+  int32_t dims[CPFEM_MG_MAX_LEVELS][3];       /* nodes per direction, x fastest */
+  cpfem_sell_t sell[CPFEM_MG_MAX_LEVELS];     /* layout per level (level 0: the system's) */
+  double* values[CPFEM_MG_MAX_LEVELS];        /* levels >= 1: coarse operators (cpfem_mg_setup) */
+  double* minv[CPFEM_MG_MAX_LEVELS];          /* [9*nodes] inverted 3x3 diagonal blocks (setup) */
+  const int8_t* slot[CPFEM_MG_MAX_LEVELS];    /* levels 0..L-2: [27*nodes] slot of each neighbour
+                                                 offset (dz+1)*9+(dy+1)*3+(dx+1), -1 if absent */
+  double* x[CPFEM_MG_MAX_LEVELS];             /* [3*nodes] work vectors of every level */
+  double* t[CPFEM_MG_MAX_LEVELS];
+  double* r[CPFEM_MG_MAX_LEVELS];
+  double* b[CPFEM_MG_MAX_LEVELS];             /* levels >= 1 */
+  const int8_t* free_dof;                     /* [3*nodes of level 0]: 0 on Dirichlet dofs */
+} cpfem_mg_t;
+
+/* Host: the slot table of one level from its node-block CSR pattern (rows sorted, as
+ * cpfem_pattern_build makes them); CPFEM_ERR_ARG if a neighbour is not within one node
+ * in every direction (not a structured box). */
+int cpfem_mg_slot_table(int32_t num_nodes, const int32_t* dims, const int32_t* node_rowptr,
+                        const int32_t* node_cols, int8_t* out);
+/* Device: block-Jacobi inverses of level 0 from values0 (the BC-eliminated tangent), the
+ * Galerkin coarse operators and their block-Jacobi inverses.  Once per new tangent. */
+int cpfem_mg_setup(const cpfem_mg_t* mg, const double* values0, void* stream);
+
+typedef struct {
+  int32_t precond;        /* 0 none, 1 Jacobi (the reference), 2 3x3 block-Jacobi, 3 multigrid */
+  int32_t transpose;      /* solve A^T x = b (precond 0..2) */
   int32_t maxiter;
   int32_t max_restarts;
   double tol, atol;
+  const cpfem_mg_t* mg;   /* precond 3: a hierarchy set up for this matrix */
 } cpfem_krylov_opts_t;
 int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
                       const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream);

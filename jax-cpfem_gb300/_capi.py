@@ -87,17 +87,6 @@ class VjpArgs(ctypes.Structure):
         "status")]
 
 
-class KrylovOpts(ctypes.Structure):
-    _fields_ = [
-        ("precond", ctypes.c_int32),
-        ("transpose", ctypes.c_int32),
-        ("maxiter", ctypes.c_int32),
-        ("max_restarts", ctypes.c_int32),
-        ("tol", ctypes.c_double),
-        ("atol", ctypes.c_double),
-    ]
-
-
 class Sell(ctypes.Structure):
     _fields_ = [
         ("num_nodes", ctypes.c_int32),
@@ -110,12 +99,47 @@ class Sell(ctypes.Structure):
     ]
 
 
+MG_MAX_LEVELS = 8
+
+
+class MGHierarchy(ctypes.Structure):
+    """cpfem_mg_t."""
+    _fields_ = [
+        ("num_levels", ctypes.c_int32),
+        ("pre_sweeps", ctypes.c_int32),
+        ("post_sweeps", ctypes.c_int32),
+        ("coarse_sweeps", ctypes.c_int32),
+        ("omega", ctypes.c_double),
+        ("dims", (ctypes.c_int32 * 3) * MG_MAX_LEVELS),
+        ("sell", Sell * MG_MAX_LEVELS),
+        ("values", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("minv", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("slot", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("x", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("t", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("r", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("b", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("free_dof", ctypes.c_void_p),
+    ]
+
+
+class KrylovOpts(ctypes.Structure):
+    _fields_ = [
+        ("precond", ctypes.c_int32),
+        ("transpose", ctypes.c_int32),
+        ("maxiter", ctypes.c_int32),
+        ("max_restarts", ctypes.c_int32),
+        ("tol", ctypes.c_double),
+        ("atol", ctypes.c_double),
+        ("mg", ctypes.POINTER(MGHierarchy)),
+    ]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _I64 = ctypes.c_int64
 _D = ctypes.c_double
 
-# name -> (restype, argtypes); every symbol declared in include/cpfem_gb300.h
 _SP = ctypes.POINTER(Sell)
 
 # name -> (restype, argtypes); every symbol declared in include/cpfem_gb300.h
@@ -144,6 +168,8 @@ SIGNATURES = {
     "cpfem_bicgstab": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P, _P]),
     "cpfem_bicgstab_noalloc": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P]),
     "cpfem_bicgstab_last_stats": (ctypes.c_int, [_P]),
+    "cpfem_mg_slot_table": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
+    "cpfem_mg_setup": (ctypes.c_int, [ctypes.POINTER(MGHierarchy), _P, _P]),
     "cpfem_bicgstab_ex": (ctypes.c_int, [_SP, _P, _P, _P, ctypes.POINTER(KrylovOpts), _P, _P, _P]),
     "cpfem_bicgstab_batched_workspace_bytes": (ctypes.c_size_t, [_I32]),
     "cpfem_bicgstab_batched": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _D, _D, _I32, _I32, _P, _I32, _P, _P, _P, _P, _P]),

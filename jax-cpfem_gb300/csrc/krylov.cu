@@ -13,6 +13,7 @@
 // an error flag and the solve returns CPFEM_ERR_SOLVE.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 #include <string>
 
@@ -239,11 +240,304 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* partials, G
   return ok;
 }
 
-template <bool TRANS>
+// ---- geometric multigrid (precond 3) ------------------------------------------------
+// Levels of a structured box of nodes, x fastest.  Fine node i of level l and coarse node
+// I of level l+1 are linked when i is within one fine node of 2I in every direction, with
+// the trilinear weight prod_d (1 if i_d = 2 I_d else 1/2).
+
+__device__ __forceinline__ void mg_xyz(int64_t a, const int32_t* dims, int& x, int& y, int& z) {
+  x = (int)(a % dims[0]);
+  const int64_t q = a / dims[0];
+  y = (int)(q % dims[1]);
+  z = (int)(q / dims[1]);
+}
+
+__device__ __forceinline__ void mg_apply_minv(const double* __restrict__ minv, int64_t a, const double* v,
+                                              double* out) {
+  const double* bi = minv + 9 * a;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) out[i] = fma(bi[3 * i], v[0], fma(bi[3 * i + 1], v[1], bi[3 * i + 2] * v[2]));
+}
+
+// One damped block-Jacobi sweep at node a: T = X + omega Minv (B - A X).
+__device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const double* V, const double* minv,
+                                         const double* B, const double* X, double* T, double omega, int64_t a) {
+  double acc[3], r[3], z[3];
+  sell_rows<false, true>(S, V, X, a, acc);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) r[i] = B[3 * a + i] - acc[i];
+  mg_apply_minv(minv, a, r, z);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) T[3 * a + i] = fma(omega, z[i], __ldcg(&X[3 * a + i]));
+}
+
+// Rows of node a restricted to the slots j = q (mod 4) (one lane of a quad).
+__device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const double* __restrict__ vals,
+                                               const double* x, int64_t a, int q, double* acc) {
+  const int64_t g = a >> 5;
+  const int lane = (int)(a & 31);
+  const int64_t c0 = L.group_off[g] + lane;
+  const double* v0 = vals + 9 * L.group_off[g] + lane;
+  const int w = L.group_width[g];
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+#pragma unroll 2
+  for (int j = q; j < w; j += 4) {
+    const int64_t b = __ldg(&L.cols[c0 + 32 * j]);
+    const double x0 = __ldcg(&x[3 * b]), x1 = __ldcg(&x[3 * b + 1]), x2 = __ldcg(&x[3 * b + 2]);
+    const double* vb = v0 + 288 * j;
+    a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[32]), x1, fma(__ldg(&vb[64]), x2, a0)));
+    a1 = fma(__ldg(&vb[96]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[160]), x2, a1)));
+    a2 = fma(__ldg(&vb[192]), x0, fma(__ldg(&vb[224]), x1, fma(__ldg(&vb[256]), x2, a2)));
+  }
+  acc[0] = a0;
+  acc[1] = a1;
+  acc[2] = a2;
+}
+
+__device__ __forceinline__ void quad_sum3(double* v) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    v[i] += __shfl_xor_sync(0xffffffffu, v[i], 1);
+    v[i] += __shfl_xor_sync(0xffffffffu, v[i], 2);
+  }
+}
+
+// Level operations of the V-cycle on a coarse level (l >= 1), one quad of lanes per node:
+// nodes a = tq, tq + sq, ... (tq = this lane's quad, sq = the quads taking part; a warp
+// holds 8 consecutive quads and runs the padded loops in lockstep, so the shuffles always
+// see the whole warp); lane 0 of a node's quad owns its writes.
+__device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, int l, double* X, int64_t tq, int64_t sq,
+                                                int q) {
+  if (q != 0) return;
+  const double* B = mg.b[l];
+  for (int64_t a = tq; a < mg.sell[l].num_nodes; a += sq) {
+    double v[3] = {B[3 * a], B[3 * a + 1], B[3 * a + 2]}, z[3];
+    mg_apply_minv(mg.minv[l], a, v, z);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) X[3 * a + i] = mg.omega * z[i];
+  }
+}
+
+// T = X + omega Minv (B - A X)  (residual = false)  or  R = B - A X  (residual = true)
+__device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, int l, const double* X, double* T, bool residual,
+                                          int64_t tq, int64_t sq, int q) {
+  const cpfem_sell_t& S = mg.sell[l];
+  const double* B = mg.b[l];
+  const int64_t n = S.num_nodes, npad = (n + 7) / 8 * 8;
+  for (int64_t a = tq; a < npad; a += sq) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (a < n) sell_rows_quad(S, mg.values[l], X, a, q, acc);
+    quad_sum3(acc);
+    if (a < n && q == 0) {
+      double r[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) r[i] = B[3 * a + i] - acc[i];
+      if (residual) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) T[3 * a + i] = r[i];
+      } else {
+        double z[3];
+        mg_apply_minv(mg.minv[l], a, r, z);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) T[3 * a + i] = fma(mg.omega, z[i], X[3 * a + i]);
+      }
+    }
+  }
+}
+
+// b_{l+1} = P^T R_l: the 27 fine nodes of a coarse node split over its quad.
+__device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, int l, const double* R, int64_t tq, int64_t sq,
+                                             int q) {
+  const int32_t* df = mg.dims[l];
+  const int32_t* dc = mg.dims[l + 1];
+  double* Bc = mg.b[l + 1];
+  const int64_t nc = mg.sell[l + 1].num_nodes, ncpad = (nc + 7) / 8 * 8;
+  for (int64_t I = tq; I < ncpad; I += sq) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    if (I < nc) {
+      int cx, cy, cz;
+      mg_xyz(I, dc, cx, cy, cz);
+      for (int k = q; k < 27; k += 4) {
+        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+        const int ix = 2 * cx + dx, iy = 2 * cy + dy, iz = 2 * cz + dz;
+        if (ix < 0 || ix >= df[0] || iy < 0 || iy >= df[1] || iz < 0 || iz >= df[2]) continue;
+        const double w = (dx ? 0.5 : 1.0) * (dy ? 0.5 : 1.0) * (dz ? 0.5 : 1.0);
+        const int64_t i = ix + (int64_t)df[0] * (iy + (int64_t)df[1] * iz);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) acc[c] = fma(w, __ldcg(&R[3 * i + c]), acc[c]);
+      }
+    }
+    quad_sum3(acc);
+    if (I < nc && q == 0)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Bc[3 * I + c] = acc[c];
+  }
+}
+
+// X_l += P X_{l+1} at the nodes a = first, first + step, ... (masked on Dirichlet dofs of
+// level 0).
+__device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, double* X, const double* Xc, int64_t first,
+                                           int64_t step) {
+  const int32_t* df = mg.dims[l];
+  const int32_t* dc = mg.dims[l + 1];
+  for (int64_t a = first; a < mg.sell[l].num_nodes; a += step) {
+    int ix, iy, iz;
+    mg_xyz(a, df, ix, iy, iz);
+    const int cx0 = ix >> 1, cy0 = iy >> 1, cz0 = iz >> 1;
+    const int nxc = (ix & 1) + 1, nyc = (iy & 1) + 1, nzc = (iz & 1) + 1;
+    const double w = ((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0);
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int kz = 0; kz < nzc; ++kz)
+      for (int ky = 0; ky < nyc; ++ky)
+        for (int kx = 0; kx < nxc; ++kx) {
+          const int64_t I = (cx0 + kx) + (int64_t)dc[0] * ((cy0 + ky) + (int64_t)dc[1] * (cz0 + kz));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc[c] = fma(w, __ldcg(&Xc[3 * I + c]), acc[c]);
+        }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const bool fixed = (l == 0 && mg.free_dof != nullptr && mg.free_dof[3 * a + c] == 0);
+      if (!fixed) X[3 * a + c] += acc[c];
+    }
+  }
+}
+
+constexpr int64_t kMgLocalNodes = 256;   // levels this small run inside block 0
+
+// One V-cycle out = M^-1 in over every block of the cooperative launch.  Level 0 uses the
+// caller's one-thread-per-node grid-stride mapping (so input written by this thread needs
+// no barrier); coarser levels give every node a quad of lanes, so their few nodes still
+// hide load latency.  The levels with at most kMgLocalNodes nodes run inside block 0 with
+// block barriers while the other blocks wait at the next grid barrier.  Which of x / t
+// holds a level's iterate follows from the sweep counts alone, so every block knows it.
+// Returns with out complete for this thread's own nodes.
+__device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0, const double* in, double* out,
+                          int64_t t0, int64_t stride, GridSync* gs, unsigned int& gen, bool& ok) {
+  const int L = mg.num_levels;
+  const double om = mg.omega;
+  const int64_t tq = t0 >> 2, sq = stride >> 2;
+  const int q = (int)(t0 & 3);
+  const int64_t tqb = threadIdx.x >> 2, sqb = blockDim.x >> 2;   // block-local quads
+  int lb = L;                                                    // first block-local level
+  for (int l = L - 1; l >= 2 && mg.sell[l].num_nodes <= kMgLocalNodes; --l) lb = l;
+  // where each level's iterate lives after its down sweeps / after its up sweeps
+  bool down_t[CPFEM_MG_MAX_LEVELS], up_t[CPFEM_MG_MAX_LEVELS];
+  for (int l = 0; l < L; ++l) {
+    const int nsw = (l == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
+    down_t[l] = ((nsw - 1) & 1) != 0;
+    up_t[l] = (l == L - 1) ? down_t[l] : (down_t[l] != ((mg.post_sweeps & 1) != 0));
+  }
+  // ---- grid-wide levels 0 .. lb-1, down
+  for (int l = 0; l < lb; ++l) {
+    const cpfem_sell_t& S = mg.sell[l];
+    const double* V = (l == 0) ? vals0 : mg.values[l];
+    double* X = mg.x[l];
+    double* T = mg.t[l];
+    const int64_t n = S.num_nodes;
+    if (l == 0) {
+      for (int64_t a = t0; a < n; a += stride) {
+        double v[3] = {in[3 * a], in[3 * a + 1], in[3 * a + 2]}, z[3];
+        mg_apply_minv(mg.minv[0], a, v, z);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) X[3 * a + i] = om * z[i];
+      }
+    } else {
+      mgq_first_sweep(mg, l, X, tq, sq, q);
+    }
+    const int nsw = (l == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
+    for (int k = 1; k < nsw; ++k) {
+      ok = grid_barrier(gs, gen) && ok;
+      if (l == 0) {
+        for (int64_t a = t0; a < n; a += stride) mg_sweep(S, V, mg.minv[0], in, X, T, om, a);
+      } else {
+        mgq_apply(mg, l, X, T, false, tq, sq, q);
+      }
+      double* tmp = X; X = T; T = tmp;
+    }
+    if (l == L - 1) break;
+    ok = grid_barrier(gs, gen) && ok;
+    double* R = mg.r[l];
+    if (l == 0) {
+      for (int64_t a = t0; a < n; a += stride) {
+        double acc[3];
+        sell_rows<false, true>(S, V, X, a, acc);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const double rv = in[3 * a + i] - acc[i];
+          R[3 * a + i] = (mg.free_dof != nullptr && mg.free_dof[3 * a + i] == 0) ? 0.0 : rv;
+        }
+      }
+    } else {
+      mgq_apply(mg, l, X, R, true, tq, sq, q);
+    }
+    ok = grid_barrier(gs, gen) && ok;
+    if (l + 1 < lb) {
+      mgq_restrict(mg, l, R, tq, sq, q);
+    } else if (blockIdx.x == 0) {
+      // ---- block-local levels lb .. L-1: down, coarsest, up to lb
+      mgq_restrict(mg, l, R, tqb, sqb, q);
+      for (int m = lb; m < L; ++m) {
+        double* Xm = mg.x[m];
+        double* Tm = mg.t[m];
+        mgq_first_sweep(mg, m, Xm, tqb, sqb, q);
+        const int nswm = (m == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
+        for (int k = 1; k < nswm; ++k) {
+          __syncthreads();
+          mgq_apply(mg, m, Xm, Tm, false, tqb, sqb, q);
+          double* tmp = Xm; Xm = Tm; Tm = tmp;
+        }
+        if (m == L - 1) break;
+        __syncthreads();
+        mgq_apply(mg, m, Xm, mg.r[m], true, tqb, sqb, q);
+        __syncthreads();
+        mgq_restrict(mg, m, mg.r[m], tqb, sqb, q);
+      }
+      for (int m = L - 2; m >= lb; --m) {
+        double* Xm = down_t[m] ? mg.t[m] : mg.x[m];
+        double* Tm = down_t[m] ? mg.x[m] : mg.t[m];
+        const double* Xc = (m + 1 == L - 1 ? down_t[m + 1] : up_t[m + 1]) ? mg.t[m + 1] : mg.x[m + 1];
+        __syncthreads();
+        if (q == 0) mg_prolong(mg, m, Xm, Xc, tqb, sqb);
+        for (int k = 0; k < mg.post_sweeps; ++k) {
+          __syncthreads();
+          mgq_apply(mg, m, Xm, Tm, false, tqb, sqb, q);
+          double* tmp = Xm; Xm = Tm; Tm = tmp;
+        }
+      }
+    }
+  }
+  // ---- grid-wide levels lb-1 .. 0, up
+  for (int l = lb - 1; l >= 0; --l) {
+    if (l == L - 1) continue;
+    const cpfem_sell_t& S = mg.sell[l];
+    const double* V = (l == 0) ? vals0 : mg.values[l];
+    double* X = down_t[l] ? mg.t[l] : mg.x[l];
+    double* T = down_t[l] ? mg.x[l] : mg.t[l];
+    const double* Xc = (l + 1 == L - 1 ? down_t[l + 1] : up_t[l + 1]) ? mg.t[l + 1] : mg.x[l + 1];
+    ok = grid_barrier(gs, gen) && ok;
+    if (l == 0) mg_prolong(mg, 0, X, Xc, t0, stride);
+    else if (q == 0) mg_prolong(mg, l, X, Xc, tq, sq);
+    for (int k = 0; k < mg.post_sweeps; ++k) {
+      ok = grid_barrier(gs, gen) && ok;
+      if (l == 0) {
+        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep(S, V, mg.minv[0], in, X, T, om, a);
+      } else {
+        mgq_apply(mg, l, X, T, false, tq, sq, q);
+      }
+      double* tmp = X; X = T; T = tmp;
+    }
+  }
+  const double* X0 = up_t[0] ? mg.t[0] : mg.x[0];
+  for (int64_t a = t0; a < mg.sell[0].num_nodes; a += stride)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) out[3 * a + i] = X0[3 * a + i];
+}
+
+template <bool TRANS, bool MG>
 __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
                                                         const double* __restrict__ b, double* __restrict__ x,
                                                         KWork w, int precond, double tol, double atol,
-                                                        int maxiter, int max_restarts) {
+                                                        int maxiter, int max_restarts, const cpfem_mg_t mg) {
   __shared__ double smem[4 * 32];
   __shared__ double bcast[4];
   const int64_t n = L.num_nodes;
@@ -289,10 +583,13 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         pv[i] = w.r[d] + beta * (w.p[d] - omega * w.q[d]);
         w.p[d] = pv[i];
       }
-      apply_m(precond, w.minv, a, pv, ph);
+      if constexpr (!MG) {
+        apply_m(precond, w.minv, a, pv, ph);
 #pragma unroll
-      for (int i = 0; i < 3; ++i) w.phat[3 * a + i] = ph[i];
+        for (int i = 0; i < 3; ++i) w.phat[3 * a + i] = ph[i];
+      }
     }
+    if constexpr (MG) mg_vcycle(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok);
     ok = grid_barrier(w.sync, gen) && ok;
     // q = A phat ; alpha = rho_new / (rhat . q)
     double v1[1] = {0.0};
@@ -319,11 +616,17 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         w.s[d] = sv[i];
         vs[0] = fma(sv[i], sv[i], vs[0]);
       }
-      apply_m(precond, w.minv, a, sv, sh);
+      if constexpr (!MG) {
+        apply_m(precond, w.minv, a, sv, sh);
 #pragma unroll
-      for (int i = 0; i < 3; ++i) w.shat[3 * a + i] = sh[i];
+        for (int i = 0; i < 3; ++i) w.shat[3 * a + i] = sh[i];
+      }
     }
     ok = grid_reduce<1>(vs, parts(), w.sync, gen, smem, bcast) && ok;
+    if constexpr (MG) {
+      mg_vcycle(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
+      ok = grid_barrier(w.sync, gen) && ok;
+    }
     const bool early = vs[0] < atol2;
     // t = A shat ; omega = (t.s)/(t.t)
     double vt[2] = {0.0, 0.0};
@@ -413,16 +716,20 @@ static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms) {
 template <bool TRANS>
 static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double* b, double* x, int precond,
                         double tol, double atol, int32_t maxiter, void* workspace, int32_t* info, cudaStream_t s,
-                        int max_restarts = 0) {
+                        int max_restarts = 0, const cpfem_mg_t* mgp = nullptr) {
   KWork w;
   carve(workspace, L.num_nodes, &w);
   CPFEM_CUDA_TRY(cudaMemsetAsync(w.sync, 0, sizeof(GridSync), s));
-  if (precond != 0) {
+  if (precond == 1 || precond == 2) {
     k_precond_setup<TRANS><<<(unsigned)ceil_div(L.num_nodes, 128), 128, 0, s>>>(L, vals, precond, w.minv);
     CPFEM_CUDA_TRY(cudaGetLastError());
   }
+  cpfem_mg_t mg;
+  memset(&mg, 0, sizeof(mg));
+  if (precond == 3) mg = *mgp;
   int per_sm = 0, sms = 0;
-  int rc = sm_count_and_blocks((const void*)k_bicgstab<TRANS>, &per_sm, &sms);
+  const void* kfn = (precond == 3) ? (const void*)k_bicgstab<false, true> : (const void*)k_bicgstab<TRANS, false>;
+  int rc = sm_count_and_blocks(kfn, &per_sm, &sms);
   if (rc) return rc;
   if (per_sm < 1) {
     set_error("persistent BiCGSTAB kernel cannot be resident");
@@ -436,9 +743,8 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   int pc = precond;
   double tl = tol, at = atol;
   int mi = maxiter, mr = max_restarts;
-  void* args[] = {&Lc, &vals, &bb, &xx, &w, &pc, &tl, &at, &mi, &mr};
-  CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_bicgstab<TRANS>, dim3((unsigned)blocks),
-                                             dim3(kPThreads), args, 0, s));
+  void* args[] = {&Lc, &vals, &bb, &xx, &w, &pc, &tl, &at, &mi, &mr, &mg};
+  CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3((unsigned)blocks), dim3(kPThreads), args, 0, s));
   SolveOut out;
   CPFEM_CUDA_TRY(cudaMemcpyAsync(&out, w.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, s));
   CPFEM_CUDA_TRY(cudaStreamSynchronize(s));
@@ -455,6 +761,100 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
 static bool sell_ok(const cpfem_sell_t* L) {
   return L && L->num_nodes >= 0 && L->group_off && L->group_width && L->cols && L->diag_slot &&
          L->num_groups == (L->num_nodes + 31) / 32;
+}
+
+static int mg_check(const cpfem_mg_t* mg, const cpfem_sell_t* sell) {
+  CPFEM_REQUIRE(mg != nullptr, "precond 3 needs a multigrid hierarchy (opts.mg)");
+  const int L = mg->num_levels;
+  CPFEM_REQUIRE(L >= 2 && L <= CPFEM_MG_MAX_LEVELS, "multigrid num_levels must be 2..CPFEM_MG_MAX_LEVELS");
+  CPFEM_REQUIRE(mg->pre_sweeps >= 1 && mg->post_sweeps >= 0 && mg->coarse_sweeps >= 1, "bad multigrid sweep counts");
+  CPFEM_REQUIRE(mg->omega > 0.0 && mg->omega < 2.0, "multigrid omega must lie in (0, 2)");
+  CPFEM_REQUIRE(sell == nullptr || mg->sell[0].num_nodes == sell->num_nodes, "level 0 must be the system's layout");
+  for (int l = 0; l < L; ++l) {
+    const int64_t n = (int64_t)mg->dims[l][0] * mg->dims[l][1] * mg->dims[l][2];
+    CPFEM_REQUIRE(mg->dims[l][0] >= 1 && mg->dims[l][1] >= 1 && mg->dims[l][2] >= 1 && n == mg->sell[l].num_nodes,
+                  "multigrid dims do not match the level's node count");
+    CPFEM_REQUIRE(sell_ok(&mg->sell[l]) && mg->minv[l] && mg->x[l] && mg->t[l], "multigrid level arrays missing");
+    if (l + 1 < L) CPFEM_REQUIRE(mg->r[l] && mg->slot[l], "multigrid residual/slot arrays missing");
+    if (l >= 1) {
+      CPFEM_REQUIRE(mg->values[l] && mg->b[l], "multigrid coarse arrays missing");
+      for (int d = 0; d < 3; ++d)
+        CPFEM_REQUIRE((mg->dims[l - 1][d] - 1) % 2 == 0 && mg->dims[l][d] == (mg->dims[l - 1][d] - 1) / 2 + 1,
+                      "each multigrid level must halve the cell counts of the finer one");
+    }
+  }
+  return CPFEM_OK;
+}
+
+// Galerkin coarse operator, one thread per (coarse node I, slot s) of the coarse layout,
+// one block per group of 32 coarse nodes: block (I, J) = sum over linked fine pairs
+// (i of I, j of J, j a neighbour of i) of w_iI w_jJ A_f(i, j), Dirichlet dofs of level 0
+// left out on both sides.  Fixed summation order: reproducible.
+__global__ void __launch_bounds__(32 * 27) k_mg_rap(const cpfem_sell_t F, const double* __restrict__ vf,
+                                                     const int8_t* __restrict__ slotf, int fx, int fy, int fz,
+                                                     const cpfem_sell_t C, int cx, int cy,
+                                                     const int8_t* __restrict__ free_dof, double* __restrict__ vc) {
+  const int g = blockIdx.x;
+  const int lane = threadIdx.x & 31, s = threadIdx.x >> 5;
+  const int64_t I = 32LL * g + lane;
+  if (I >= C.num_nodes || s >= C.group_width[g]) return;
+  const int64_t base = 9 * C.group_off[g] + lane + 288LL * s;
+  const int64_t J = C.cols[C.group_off[g] + 32LL * s + lane];
+  double acc[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+  if (!(J == I && s != C.diag_slot[I])) {
+    const int Ix = (int)(I % cx), Iy = (int)((I / cx) % cy), Iz = (int)(I / ((int64_t)cx * cy));
+    const int Jx = (int)(J % cx), Jy = (int)((J / cx) % cy), Jz = (int)(J / ((int64_t)cx * cy));
+    const int del[3] = {Jx - Ix, Jy - Iy, Jz - Iz};
+    // per direction: the linked (a, b) offsets, i = 2I + a, j = 2J + b, |i - j| <= 1
+    int pa[3][7], pb[3][7], np[3];
+    double pw[3][7];
+    bool okd = true;
+    for (int d = 0; d < 3; ++d) {
+      np[d] = 0;
+      if (del[d] < -1 || del[d] > 1) okd = false;
+      for (int a = -1; a <= 1; ++a)
+        for (int b = -1; b <= 1; ++b) {
+          const int dd = a - b - 2 * del[d];
+          if (dd >= -1 && dd <= 1 && np[d] < 7) {
+            pa[d][np[d]] = a;
+            pb[d][np[d]] = b;
+            pw[d][np[d]] = (a ? 0.5 : 1.0) * (b ? 0.5 : 1.0);
+            ++np[d];
+          }
+        }
+    }
+    if (okd) {
+      for (int kz = 0; kz < np[2]; ++kz) {
+        const int iz = 2 * Iz + pa[2][kz], jz = 2 * Jz + pb[2][kz];
+        if (iz < 0 || iz >= fz || jz < 0 || jz >= fz) continue;
+        for (int ky = 0; ky < np[1]; ++ky) {
+          const int iy = 2 * Iy + pa[1][ky], jy = 2 * Jy + pb[1][ky];
+          if (iy < 0 || iy >= fy || jy < 0 || jy >= fy) continue;
+          for (int kx = 0; kx < np[0]; ++kx) {
+            const int ix = 2 * Ix + pa[0][kx], jx = 2 * Jx + pb[0][kx];
+            if (ix < 0 || ix >= fx || jx < 0 || jx >= fx) continue;
+            const int64_t i = ix + (int64_t)fx * (iy + (int64_t)fy * iz);
+            const int64_t j = jx + (int64_t)fx * (jy + (int64_t)fy * jz);
+            const int sf = slotf[27 * i + (jz - iz + 1) * 9 + (jy - iy + 1) * 3 + (jx - ix + 1)];
+            if (sf < 0) continue;
+            const double w = pw[0][kx] * pw[1][ky] * pw[2][kz];
+            const double* blk = vf + 9 * F.group_off[i >> 5] + (i & 31) + 288LL * sf;
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                if (free_dof != nullptr && (free_dof[3 * i + r] == 0 || free_dof[3 * j + c] == 0)) continue;
+                acc[3 * r + c] = fma(w, blk[32 * (3 * r + c)], acc[3 * r + c]);
+              }
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) vc[base + 32 * k] = acc[k];
 }
 
 }  // namespace cpfem
@@ -474,6 +874,28 @@ int cpfem_spmv(const cpfem_sell_t* sell, const double* values, const double* x, 
   else
     k_spmv<false><<<blocks, 256, 0, (cudaStream_t)stream>>>(*sell, values, x, y);
   CPFEM_CUDA_TRY(cudaGetLastError());
+  return CPFEM_OK;
+}
+
+int cpfem_mg_setup(const cpfem_mg_t* mg, const double* values0, void* stream) {
+  CPFEM_REQUIRE(values0 != nullptr, "values0 is null");
+  int rc = mg_check(mg, nullptr);
+  if (rc != CPFEM_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_precond_setup<false><<<(unsigned)ceil_div(mg->sell[0].num_nodes, 128), 128, 0, s>>>(mg->sell[0], values0, 2,
+                                                                                         mg->minv[0]);
+  CPFEM_CUDA_TRY(cudaGetLastError());
+  for (int l = 0; l + 1 < mg->num_levels; ++l) {
+    const double* vf = (l == 0) ? values0 : mg->values[l];
+    const cpfem_sell_t& C = mg->sell[l + 1];
+    k_mg_rap<<<(unsigned)C.num_groups, 32 * 27, 0, s>>>(mg->sell[l], vf, mg->slot[l], mg->dims[l][0], mg->dims[l][1],
+                                                       mg->dims[l][2], C, mg->dims[l + 1][0], mg->dims[l + 1][1],
+                                                       (l == 0) ? mg->free_dof : nullptr, mg->values[l + 1]);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+    k_precond_setup<false><<<(unsigned)ceil_div(C.num_nodes, 128), 128, 0, s>>>(C, mg->values[l + 1], 2,
+                                                                                mg->minv[l + 1]);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+  }
   return CPFEM_OK;
 }
 
@@ -501,7 +923,12 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
   if (sell->num_nodes == 0) return CPFEM_OK;
   CPFEM_REQUIRE(values && b && x && workspace, "bad bicgstab arguments");
   CPFEM_REQUIRE(((uintptr_t)workspace & 255) == 0, "workspace must be 256-byte aligned");
-  CPFEM_REQUIRE(opts->precond >= 0 && opts->precond <= 2, "precond must be 0, 1 or 2");
+  CPFEM_REQUIRE(opts->precond >= 0 && opts->precond <= 3, "precond must be 0, 1, 2 or 3");
+  if (opts->precond == 3) {
+    CPFEM_REQUIRE(!opts->transpose, "the multigrid preconditioner solves A x = b only");
+    const int rc = mg_check(opts->mg, sell);
+    if (rc != CPFEM_OK) return rc;
+  }
   CPFEM_REQUIRE(opts->maxiter >= 0, "maxiter must be >= 0");
   CPFEM_REQUIRE(opts->max_restarts >= 0, "max_restarts must be >= 0");
   CPFEM_REQUIRE(!opts->transpose || sell->tpos != nullptr, "transpose needs tpos");
@@ -510,13 +937,14 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
     return run_bicgstab<true>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
                               info, s, opts->max_restarts);
   return run_bicgstab<false>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                             info, s, opts->max_restarts);
+                             info, s, opts->max_restarts, opts->mg);
 }
 
 int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x, int32_t precond,
                    int32_t transpose, double tol, double atol, int32_t maxiter, void* workspace, int32_t* info,
                    void* stream) {
-  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol};
+  CPFEM_REQUIRE(precond >= 0 && precond <= 2, "precond must be 0, 1 or 2 (multigrid: cpfem_bicgstab_ex)");
+  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol, nullptr};
   return cpfem_bicgstab_ex(sell, values, b, x, &o, workspace, info, stream);
 }
 

@@ -234,3 +234,42 @@ extern "C" int cpfem_color_cells(int32_t num_cells, const int32_t* cells, int32_
   *num_colors = nc;
   return CPFEM_OK;
 }
+
+// Slot of every neighbour offset of every node of a structured box (x fastest):
+// out[27*i + (dz+1)*9 + (dy+1)*3 + (dx+1)] = position of that neighbour in row i of the
+// node-block pattern (= its sliced-ELL slot), -1 where the neighbour does not exist.
+extern "C" int cpfem_mg_slot_table(int32_t num_nodes, const int32_t* dims, const int32_t* node_rowptr,
+                                   const int32_t* node_cols, int8_t* out) {
+  if (num_nodes < 0 || !dims || !node_rowptr || !node_cols || !out) {
+    cpfem::set_error("bad slot-table arguments");
+    return CPFEM_ERR_ARG;
+  }
+  const int64_t nx = dims[0], ny = dims[1], nz = dims[2];
+  if (nx < 1 || ny < 1 || nz < 1 || nx * ny * nz != num_nodes) {
+    cpfem::set_error("dims do not match num_nodes");
+    return CPFEM_ERR_ARG;
+  }
+  for (int64_t i = 0; i < num_nodes; ++i) {
+    for (int c = 0; c < 27; ++c) out[27 * i + c] = -1;
+    const int64_t ix = i % nx, iy = (i / nx) % ny, iz = i / (nx * ny);
+    const int32_t r0 = node_rowptr[i], r1 = node_rowptr[i + 1];
+    if (r1 - r0 > 127) {
+      cpfem::set_error("row too long for a structured box");
+      return CPFEM_ERR_ARG;
+    }
+    for (int32_t p = r0; p < r1; ++p) {
+      const int64_t j = node_cols[p];
+      if (j < 0 || j >= num_nodes) {
+        cpfem::set_error("column out of range");
+        return CPFEM_ERR_ARG;
+      }
+      const int64_t dx = j % nx - ix, dy = (j / nx) % ny - iy, dz = j / (nx * ny) - iz;
+      if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+        cpfem::set_error("pattern is not a structured box of the given dims (neighbour beyond one node)");
+        return CPFEM_ERR_ARG;
+      }
+      out[27 * i + (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] = (int8_t)(p - r0);
+    }
+  }
+  return CPFEM_OK;
+}

@@ -46,6 +46,29 @@ def box_mesh(nx, ny, nz, Lx=1.0, Ly=1.0, Lz=1.0):
     return Mesh(points, cells)
 
 
+def structured_dims(points, rtol=1e-9):
+    """Node counts (nx, ny, nz) per direction when the points are a tensor grid numbered
+    x fastest (box meshes, the reference's Neper voxel meshes), else None."""
+    P = np.asarray(points, dtype=np.float64)
+    if P.ndim != 2 or P.shape[1] != 3 or P.shape[0] == 0:
+        return None
+    span = max(float(np.ptp(P, axis=0).max()), 1e-300)
+    tol = rtol * span
+    # the first row (x fastest) ends where y first changes, the first plane where z does
+    row = np.nonzero(np.abs(P[:, 1] - P[0, 1]) > tol)[0]
+    nx = int(row[0]) if row.size else P.shape[0]
+    plane = np.nonzero(np.abs(P[:, 2] - P[0, 2]) > tol)[0]
+    nxy = int(plane[0]) if plane.size else P.shape[0]
+    if nx < 1 or nxy % nx or P.shape[0] % nxy:
+        return None
+    ny, nz = nxy // nx, P.shape[0] // nxy
+    gx, gy, gz = P[:nx, 0], P[:nxy:nx, 1], P[::nxy, 2]
+    grid = np.stack(np.meshgrid(gz, gy, gx, indexing="ij")[::-1], axis=-1).reshape(-1, 3)
+    if np.abs(grid - P).max() > tol:
+        return None
+    return nx, ny, nz
+
+
 def voronoi_grains(mesh, num_grains, seed):
     """Grain id per cell: seeds uniform in the bounding box from ``default_rng(seed)``,
     each cell assigned to the seed nearest its centroid (Euclidean, non-periodic)."""

@@ -14,12 +14,14 @@ Internally the per-GP state is stored structure-of-arrays (component-major), and
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
 from . import _capi
 from .material import COPPER, MaterialSpec, check_orthonormal, cubic_constants, cubic_tensor, rot_mat
-from .mesh import Mesh, shape_grads_jxw
+from .mesh import Mesh, box_mesh, shape_grads_jxw, structured_dims
 
 
 def _dev_ptr(t):
@@ -252,6 +254,112 @@ class CrystalPlasticity:
         counts = np.bincount(color, minlength=int(nc[0]))
         self.color_cells = torch.tensor(order, device=dev)
         self.color_ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+
+    def _coarse_layout(self, dims):
+        """Node-block pattern and sliced-ELL layout of a structured box of nodes ``dims``
+        (the coarse levels of the multigrid hierarchy)."""
+        bm = box_mesh(dims[0] - 1, dims[1] - 1, dims[2] - 1)
+        n = dims[0] * dims[1] * dims[2]
+        cells = np.ascontiguousarray(bm.cells, dtype=np.int32)
+        E = cells.shape[0]
+        nb = np.zeros(1, dtype=np.int64)
+        _capi.check(self.lib.cpfem_pattern_count(E, cells.ctypes.data, n, nb.ctypes.data))
+        rowptr = np.zeros(n + 1, dtype=np.int32)
+        cols = np.zeros(int(nb[0]), dtype=np.int32)
+        epos = np.zeros(E * 64, dtype=np.uint8)
+        tpos = np.zeros(int(nb[0]), dtype=np.int32)
+        _capi.check(self.lib.cpfem_pattern_build(E, cells.ctypes.data, n, rowptr.ctypes.data, cols.ctypes.data,
+                                                 epos.ctypes.data, tpos.ctypes.data))
+        slots = np.zeros(1, dtype=np.int64)
+        _capi.check(self.lib.cpfem_sell_count(n, rowptr.ctypes.data, slots.ctypes.data))
+        ng = (n + 31) // 32
+        goff = np.zeros(ng + 1, dtype=np.int64)
+        gw = np.zeros(ng, dtype=np.int32)
+        scols = np.zeros(int(slots[0]), dtype=np.int32)
+        stpos = np.zeros(int(slots[0]), dtype=np.int32)
+        dslot = np.zeros(n, dtype=np.int32)
+        _capi.check(self.lib.cpfem_sell_build(n, rowptr.ctypes.data, cols.ctypes.data, tpos.ctypes.data,
+                                              goff.ctypes.data, gw.ctypes.data, scols.ctypes.data,
+                                              stpos.ctypes.data, dslot.ctypes.data))
+        arrays = [torch.tensor(v, device=self.device) for v in (goff, gw, scols, stpos, dslot)]
+        sell = _capi.Sell(n, ng, *(a.data_ptr() for a in arrays))
+        return rowptr, cols, goff, sell, arrays, 9 * int(slots[0])
+
+    def multigrid(self, max_levels=5, pre_sweeps=1, post_sweeps=1, coarse_sweeps=8, omega=0.45):
+        """Geometric multigrid hierarchy of a structured box mesh for the BiCGSTAB
+        preconditioner ``precond=3`` (built once; coarse operators by ``mg_setup``).
+        Levels halve the cell counts while every count stays even, up to max_levels."""
+        key = (max_levels, pre_sweeps, post_sweeps, coarse_sweeps, omega)
+        if getattr(self, "_mg", None) is not None and self._mg_key == key:
+            return self._mg
+        dims = structured_dims(self.mesh.points)
+        if dims is None:
+            raise ValueError("the multigrid preconditioner needs a structured box mesh (a tensor grid of nodes "
+                             "numbered x fastest)")
+        levels = [tuple(dims)]
+        while len(levels) < max_levels and all((d - 1) % 2 == 0 and d >= 3 for d in levels[-1]):
+            levels.append(tuple((d - 1) // 2 + 1 for d in levels[-1]))
+        if len(levels) < 2:
+            raise ValueError("the multigrid preconditioner needs even cell counts to coarsen")
+        dev = self.device
+        mg = _capi.MGHierarchy()
+        mg.num_levels, mg.pre_sweeps, mg.post_sweeps, mg.coarse_sweeps = len(levels), pre_sweeps, post_sweeps, coarse_sweeps
+        mg.omega = float(omega)
+        keep = []
+        self.mg_layouts = []   # (rowptr, cols, group_off, values) per level, for inspection
+
+        def buf(n, dtype=torch.float64):
+            t = torch.zeros(n, dtype=dtype, device=dev)
+            keep.append(t)
+            return t.data_ptr()
+
+        for l, d in enumerate(levels):
+            n = d[0] * d[1] * d[2]
+            for k in range(3):
+                mg.dims[l][k] = d[k]
+            if l == 0:
+                rowptr, cols = self._rowptr_np, self._cols_np
+                mg.sell[0] = self.sell
+                self.mg_layouts.append((rowptr, cols, self._goff_np, None))
+            else:
+                rowptr, cols, goff, sell, arrays, nvals = self._coarse_layout(d)
+                keep += arrays
+                mg.sell[l] = sell
+                mg.values[l] = buf(nvals)
+                self.mg_layouts.append((rowptr, cols, goff, keep[-1]))
+                mg.b[l] = buf(3 * n)
+            if l + 1 < len(levels):
+                slot = np.zeros(27 * n, dtype=np.int8)
+                dd = np.asarray(d, dtype=np.int32)
+                _capi.check(self.lib.cpfem_mg_slot_table(n, dd.ctypes.data, rowptr.ctypes.data, cols.ctypes.data,
+                                                         slot.ctypes.data))
+                st = torch.tensor(slot, device=dev)
+                keep.append(st)
+                mg.slot[l] = st.data_ptr()
+                mg.r[l] = buf(3 * n)
+            mg.minv[l] = buf(9 * n)
+            mg.x[l] = buf(3 * n)
+            mg.t[l] = buf(3 * n)
+        free = torch.ones(3 * self.num_nodes, dtype=torch.int8, device=dev)
+        mg.free_dof = free.data_ptr()
+        self._mg, self._mg_keep, self._mg_free, self._mg_key = mg, keep, free, key
+        self._mg_bc_token = None
+        self.mg_levels = levels
+        return mg
+
+    def mg_setup(self, values, **kw):
+        """Coarse operators and smoother blocks of the hierarchy for the current
+        (BC-eliminated) tangent ``values``."""
+        mg = self.multigrid(**kw)
+        fe = self.fes[0]
+        if self._mg_bc_token != fe.bc_token:
+            self._mg_free.fill_(1)
+            if fe.bc_dofs.numel():
+                self._mg_free[fe.bc_dofs.long()] = 0
+            self._mg_bc_token = fe.bc_token
+        with self.region("mg_setup"):
+            _capi.check(self.lib.cpfem_mg_setup(ctypes.byref(mg), _dev_ptr(values), _stream()))
+        return mg
 
     def csr_map(self):
         """Index of every scalar-CSR value (scipy's order) in the sliced-ELL values."""

@@ -36,18 +36,25 @@ def norm(problem, x):
     return math.sqrt(_dot(problem, x, x))
 
 
-def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, restarts=0):
+def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, restarts=0,
+             mg_options=None):
     """``jax.scipy.sparse.linalg.bicgstab`` on the device matrix (``solver.py:34-40``), one
     persistent cooperative launch.  precond: 0 none, 1 Jacobi 1/diag(A) (the
-    reference), 2 3x3 block-Jacobi.  restarts > 0 restarts at a breakdown instead of
-    stopping there (jax stops).  Returns (x, iterations or breakdown code, converged)."""
+    reference), 2 3x3 block-Jacobi, 3 geometric multigrid V-cycle (structured box
+    meshes; ``mg_options`` go to ``CrystalPlasticity.multigrid``).  restarts > 0 restarts at
+    a breakdown instead of stopping there (jax stops).  Returns (x, iterations or breakdown
+    code, converged)."""
     lib = problem.lib
     x = x0.clone()
     nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
-                            float(tol), float(atol))
+                            float(tol), float(atol), None)
+    if int(precond) == 3:
+        if A.transposed:
+            raise ValueError("the multigrid preconditioner solves A x = b only (no transposed solve)")
+        opts.mg = ctypes.pointer(problem.mg_setup(A.values, **(mg_options or {})))
     with problem.region("bicgstab"):
         _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b.contiguous()), _dev_ptr(x),
                                           ctypes.byref(opts), _dev_ptr(ws), info.ctypes.data, _stream()))
@@ -59,11 +66,12 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
     ``||Ax - b|| < 0.1`` check."""
     opts = opts or {}
     pc = opts.get("precond", precond)
-    pc = {True: 1, False: 0, "jacobi": 1, "block3": 2, "block_jacobi": 2}.get(pc, pc)
+    pc = {True: 1, False: 0, "jacobi": 1, "block3": 2, "block_jacobi": 2, "mg": 3, "multigrid": 3}.get(pc, pc)
     rs = opts.get("restart_on_breakdown", 0)
     rs = 20 if rs is True else int(rs or 0)
     x, k, ok = bicgstab(problem, A, b, x0, precond=pc, tol=opts.get("tol", 1e-10),
-                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000), restarts=rs)
+                        atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000), restarts=rs,
+                        mg_options=opts.get("mg_options"))
     problem.stats["krylov_iters"].append(k)
     r = A.matvec(x)
     r.sub_(b)

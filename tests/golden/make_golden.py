@@ -76,16 +76,25 @@ def main():
     dp = [vtu.read_vtu(os.path.join(ddir, f"u_inhomo_{i:03d}.vtu")) for i in range(50)]
     bp, bc = box_mesh(10, 10, 10, 2.0, 2.0, 2.0)
     assert np.abs(bp - dp[0]["points"]).max() < 1e-12 and (bc == dp[0]["cells"]).all()
+    # The files were written by a run whose two phases had their elastic constants
+    # exchanged relative to their Kalidindi parameters: the saved C11/C12/C44 fields carry
+    # the martensite constants on the cells whose saved phase_inds is 0 (ferrite
+    # parameters) and the ferrite constants on the others.  Both maps are kept: the phase
+    # of the plastic parameters (phase_inds) and the phase of the stiffness (from C11).
+    c11 = dp[0]["cell_data"]["C11"]
+    assert set(np.unique(c11).tolist()) == {231400.0, 417400.0}
     dp_phase = dp[0]["cell_data"]["phase_inds"].astype(np.int8)
+    dp_stiff_phase = (c11 > 3.0e5).astype(np.int8)
+    assert (dp_stiff_phase == 1 - dp_phase).all()
     dp_ori = dp[0]["cell_data"]["cell_ori_inds"].astype(np.int16)
-    assert all((r["cell_data"]["phase_inds"] == dp_phase).all() for r in dp)
+    assert all((r["cell_data"]["phase_inds"] == dp[0]["cell_data"]["phase_inds"]).all() for r in dp)
     dp_sig = np.stack([np.stack([r["cell_data"][f"sigma_{c}"] for c in ("xx", "yy", "zz")]) for r in dp])
     dp_quat = np.loadtxt(os.path.join(REF, "polycrystal_DPsteel/data/csv/polycrystal_DPsteel/quat.txt"))[:20, 1:]
     np.savez_compressed(os.path.join(HERE, "golden.npz"), case1_szz=case1, case2_szz=case2,
                         case4_szz=c4zz, case4_sxx=c4xx, case4_quat=quat,
                         case4_grain=grains.astype(np.int16), steel_sig=steel_sig, steel_ori=steel_ori,
                         steel_quat=steel_quat, ta_szz=ta_szz, ta_L=np.array(L), dp_sig=dp_sig,
-                        dp_phase=dp_phase, dp_ori=dp_ori, dp_quat=dp_quat)
+                        dp_phase=dp_phase, dp_stiff_phase=dp_stiff_phase, dp_ori=dp_ori, dp_quat=dp_quat)
     print("wrote golden.npz", case1.shape, case2.shape, c4zz.shape, c4xx.shape, quat.shape, grains.shape)
 
 

@@ -225,7 +225,8 @@ def test_multiphase_spec_and_golden_dp_fixture(pkg):
     with pytest.raises(ValueError):
         m.cubic_constants(bad)
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
-    assert np.bincount(g["dp_phase"]).tolist() == [600, 400]
+    assert np.bincount(g["dp_phase"]).tolist() == [600, 400]     # phase of the Kalidindi parameters
+    assert (g["dp_stiff_phase"] == 1 - g["dp_phase"]).all()     # the stiffness the files were made with
     assert g["dp_ori"].max() >= g["dp_quat"].shape[0]          # clamped indices occur
     assert np.abs(np.linalg.norm(g["dp_quat"], axis=1) - 1).max() < 1e-12
     assert g["dp_sig"].shape == (50, 3, 1000)

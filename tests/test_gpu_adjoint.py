@@ -80,3 +80,18 @@ def test_autograd_function_wraps_the_adjoint(pkg, gpu):
     # element scatter uses FP64 atomics: two backward runs agree to rounding, not bitwise
     assert np.allclose(th.grad.numpy(), tb, rtol=1e-7, atol=0)
     assert np.allclose(eu.grad.numpy(), eb, rtol=1e-7, atol=1e-300)
+
+
+def test_calibration_recovers_parameters(pkg, gpu):
+    """L-BFGS-B with adjoint gradients (the loop of calibration_case1_..._GB.py) recovers
+    h0 and g0 from a target curve made with them scaled by 1.15 and 0.9."""
+    problem_mod, _ = gpu
+    calib = importlib.import_module("jax-cpfem_gb300.calibration")
+    adjoint, h, theta, euler = _history(pkg, problem_mod, steps=5)
+    truth = theta.copy()
+    truth[0] *= 1.15
+    truth[1] *= 0.9
+    target = h.forward(truth, euler).cpu().numpy()[:, 2, 2]
+    res = calib.calibrate(h, target, theta, euler, names=("h0", "g0"), x0=1.0, bounds=(0.4, 3.0), maxiter=40)
+    assert res.objective < 1e-12, res
+    np.testing.assert_allclose(res.multipliers, [1.15, 0.9], rtol=1e-4)

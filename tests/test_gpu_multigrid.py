@@ -1,0 +1,127 @@
+"""Geometric-multigrid preconditioner (precond 3): the device Galerkin coarse operator
+against P^T A P formed on the host from the assembled tangent, and multigrid-BiCGSTAB
+solves and load steps against the Jacobi path and the oracle."""
+import importlib
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import torch
+
+from oracle import cpfem_oracle as O
+from tests.common import gpu_problem, oracle_problem, roller_bcs
+
+pytestmark = pytest.mark.gpu
+
+
+def _block_matrix(layout, values):
+    """Scalar CSR of a sliced-ELL node-block matrix (rows sorted)."""
+    rowptr, cols, goff, _ = layout
+    v = values.detach().cpu().numpy()
+    n = rowptr.size - 1
+    I, J, V = [], [], []
+    for a in range(n):
+        g, lane = a >> 5, a & 31
+        for j in range(rowptr[a + 1] - rowptr[a]):
+            b = cols[rowptr[a] + j]
+            for r in range(3):
+                for c in range(3):
+                    I.append(3 * a + r)
+                    J.append(3 * b + c)
+                    V.append(v[9 * goff[g] + lane + 32 * (9 * j + 3 * r + c)])
+    return sp.csr_array((V, (I, J)), shape=(3 * n, 3 * n))
+
+
+def _prolong(dims):
+    def p1(nf):
+        nc = (nf - 1) // 2 + 1
+        rows, cols, vals = [], [], []
+        for i in range(nf):
+            if i % 2 == 0:
+                rows.append(i)
+                cols.append(i // 2)
+                vals.append(1.0)
+            else:
+                rows.extend([i, i])
+                cols.extend([(i - 1) // 2, (i + 1) // 2])
+                vals.extend([0.5, 0.5])
+        return sp.csr_array((vals, (rows, cols)), shape=(nf, nc))
+    Pn = sp.kron(sp.kron(p1(dims[2]), p1(dims[1])), p1(dims[0]))
+    return sp.kron(Pn, sp.eye(3)).tocsr()
+
+
+def _plastic_case(pkg, problem_mod, n=8, grains=4, strain=3e-3):
+    spec = pkg.material.BENCH_STEEL
+    mesh = pkg.box_mesh(n, n, n)
+    ori, rng = pkg.mesh.voronoi_grains(mesh, grains, 2)
+    quat = pkg.material.random_quaternions(rng, grains)
+    bcs = roller_bcs(pkg.mesh, mesh.points, strain)
+    prob = gpu_problem(pkg, problem_mod, spec, mesh, quat, ori, bcs)
+    prob.dt = 0.1
+    P = mesh.points
+    u = np.zeros_like(P)
+    u[:, 2] = strain * P[:, 2]
+    u[:, :2] = -0.3 * strain * P[:, :2]
+    return spec, mesh, quat, ori, bcs, prob, torch.tensor(u.reshape(-1), device="cuda")
+
+
+def test_coarse_operator_is_galerkin_product(pkg, gpu):
+    problem_mod, solver_mod = gpu
+    _, mesh, _, _, _, prob, u = _plastic_case(pkg, problem_mod)
+    res, A = solver_mod.newton_update_helper(prob, u)
+    prob.mg_setup(A.values)
+    assert [l[0] for l in prob.mg_levels][:3] == [9, 5, 3]
+    A0 = A.to_scipy()
+    free = np.ones(A0.shape[0])
+    free[prob.fes[0].bc_dofs.cpu().numpy()] = 0.0
+    P = sp.diags(free) @ _prolong(prob.mg_levels[0])
+    A1 = (P.T @ A0 @ P).toarray()
+    D1 = _block_matrix(prob.mg_layouts[1], prob.mg_layouts[1][3]).toarray()
+    assert np.abs(D1 - A1).max() / np.abs(A1).max() < 1e-13
+    P2 = _prolong(prob.mg_levels[1])
+    A2 = (P2.T @ sp.csr_array(A1) @ P2).toarray()
+    D2 = _block_matrix(prob.mg_layouts[2], prob.mg_layouts[2][3]).toarray()
+    assert np.abs(D2 - A2).max() / np.abs(A2).max() < 1e-13
+
+
+def test_multigrid_bicgstab_solves_the_tangent(pkg, gpu):
+    problem_mod, solver_mod = gpu
+    _, _, _, _, _, prob, u = _plastic_case(pkg, problem_mod, n=16)
+    res, A = solver_mod.newton_update_helper(prob, u)
+    x0 = solver_mod.initial_increment(prob, u)
+    xj, kj, okj = solver_mod.bicgstab(prob, A, -res, x0, precond=1)
+    xm, km, okm = solver_mod.bicgstab(prob, A, -res, x0, precond=3)
+    assert okj and okm and 0 < km < kj / 4, (kj, km)
+    assert float((xm - xj).abs().max() / xj.abs().max()) < 1e-8
+    r = A.matvec(xm) + res
+    assert float(r.norm()) <= 1e-10 * max(float(res.norm()), 1.0) * 10
+
+
+def test_load_steps_with_multigrid_match_oracle(pkg, gpu):
+    """Three tension steps of a 4^3, 4-grain polycrystal with the multigrid-preconditioned
+    linear solve: per-cell stress and u against the oracle (Jacobi BiCGSTAB)."""
+    problem_mod, solver_mod = gpu
+    spec = pkg.material.BENCH_STEEL
+    mesh = pkg.box_mesh(4, 4, 4)
+    ori, rng = pkg.mesh.voronoi_grains(mesh, 4, 0)
+    quat = pkg.material.random_quaternions(rng, 4)
+    prob = gpu_problem(pkg, problem_mod, spec, mesh, quat, ori)
+    orc = oracle_problem(spec, mesh, quat, ori)
+    disps, ts = np.linspace(0, 3e-3, 4), np.linspace(0, 0.3, 4)
+    bcf = lambda d: roller_bcs(pkg.mesh, mesh.points, d)
+    sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
+    params = prob.internal_vars
+    out = []
+    for i in range(3):
+        prob.dt = float(ts[i + 1] - ts[i])
+        bcs = bcf(float(disps[i + 1]))
+        prob.fes[0].set_dirichlet_lists([b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs])
+        prob.set_params(params)
+        sol = solver_mod.solver(prob, {"jax_solver": {"precond": "mg"}, "tol": 1e-9, "rel_tol": 1e-12,
+                                       "initial_guess": [sol.reshape(-1, 3)]})[0].reshape(-1)
+        out.append(prob.compute_avg_stress(sol.reshape(-1, 3), params).cpu().numpy())
+        params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
+    s_o, u_o = O.run_load_steps(orc, disps, ts, bcf, {"tol": 1e-9, "rel_tol": 1e-12})
+    s = np.array(out)
+    assert np.abs(s - s_o).max() / np.abs(s_o).max() < 1e-8
+    assert float(np.abs(sol.cpu().numpy() - u_o).max() / np.abs(u_o).max()) < 1e-8

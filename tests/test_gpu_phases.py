@@ -60,24 +60,30 @@ def test_dp_steel_internal_vars_layout(pkg, gpu):
 
 
 def test_golden_dp_steel_on_gpu(pkg, gpu):
-    """polycrystal_DPsteel_inhomo.py: 10^3 cells of 2 mm, ferrite/martensite phases and
-    orientation indices as stored in its VTU output (indices past the 8 orientations clamp,
-    as JAX indexing does), rollers + pulled top, 50 steps to 1 % with line search;
-    per-cell sigma_zz against the float32 fields of u_inhomo_*.vtu."""
+    """polycrystal_DPsteel_inhomo.py: 10^3 cells of 2 mm, ferrite/martensite, orientation
+    indices from its VTU output (indices past the 8 orientations clamp, as JAX indexing
+    does), rollers + pulled top, 50 steps to 1 % with line search; per-cell sigma_zz against
+    the float32 fields of u_inhomo_*.vtu.  The files were made with the phases' elastic
+    constants exchanged relative to their Kalidindi parameters (their saved C11/C12/C44
+    fields show it), so the run is rebuilt through the 10-entry internal variables: each
+    cell gets its saved phase's parameters and g0, and the stiffness the file records."""
     problem_mod, solver_mod = gpu
     spec = pkg.material.DP_STEEL
     mesh = pkg.box_mesh(10, 10, 10, 2.0, 2.0, 2.0)
-    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(GOLD["dp_quat"], GOLD["dp_ori"].astype(np.int64),
-                                                                GOLD["dp_phase"].astype(np.int64)), material=spec)
+    ph = GOLD["dp_phase"].astype(np.int64)
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(GOLD["dp_quat"], GOLD["dp_ori"].astype(np.int64), ph),
+                                         material=spec)
+    params = prob.internal_vars
+    el = np.stack([spec.phases[p].elastic_row() for p in GOLD["dp_stiff_phase"].astype(np.int64)])
+    C = np.repeat(pkg.material.cubic_tensor(el)[:, None], 8, axis=1)
+    params = list(params[:9]) + [torch.tensor(C, device="cuda")]
     P = mesh.points
     fn = pkg.mesh.face_nodes
     nodes = [fn(P, 0, 0.0), fn(P, 1, 0.0), fn(P, 2, 0.0), fn(P, 2, 2.0)]
     disps, ts = np.linspace(0.0, 0.02, 51), np.linspace(0.0, 10.0, 51)
-    nsteps = int(os.environ.get("CPFEM_DP_STEPS", "50"))
     sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
-    params = prob.internal_vars
-    worst = 0.0
-    for i in range(nsteps):
+    worst, worst_mean = 0.0, 0.0
+    for i in range(50):
         prob.dt = float(ts[i + 1] - ts[i])
         prob.fes[0].set_dirichlet_lists(nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, float(disps[i + 1])])
         prob.set_params(params)
@@ -87,5 +93,6 @@ def test_golden_dp_steel_on_gpu(pkg, gpu):
         params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
         gold = GOLD["dp_sig"][i, 2].astype(np.float64)
         worst = max(worst, float(np.abs(sig[:, 2, 2] - gold).max() / np.abs(gold).max()))
-        assert abs(sig[:, 2, 2].mean() - gold.mean()) / abs(gold.mean()) < 1e-5, (i, sig[:, 2, 2].mean(), gold.mean())
-    assert worst < 1e-4, worst
+        worst_mean = max(worst_mean, abs(sig[:, 2, 2].mean() - gold.mean()) / abs(gold.mean()))
+    # float32 fields: ~6e-8 relative per value
+    assert worst_mean < 1e-7 and worst < 5e-7, (worst_mean, worst)
