@@ -71,6 +71,7 @@ class Stepper:
         self.pkg, self.prob, self.solver, self.mesh = pkg, prob, solver_mod, mesh
         self.i = 0
         self.precond = 1
+        self.mg_options = None
         self.params = prob.internal_vars
         import torch
         self.sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
@@ -87,7 +88,7 @@ class Stepper:
             guess = sol_h.to("cuda", non_blocking=True)
         else:
             guess = self.sol
-        sol = self.solver.solver(prob, {"jax_solver": {"precond": self.precond},
+        sol = self.solver.solver(prob, {"jax_solver": {"precond": self.precond, "mg_options": self.mg_options},
                                         "initial_guess": [guess.reshape(-1, 3)]})[0]
         sig = prob.compute_avg_stress(sol, self.params)
         self.params = prob.update_int_vars_gp(sol, self.params)
@@ -489,6 +490,8 @@ def main():
     ap.add_argument("--edge", type=int, default=N_EDGE, help="cube edge in cells (32 = the benchmark)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
+                    help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
     ap.add_argument("--no-jacobi-leg", action="store_true",
                     help="skip the two extra load steps timed with the reference's Jacobi preconditioner")
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"],
@@ -543,6 +546,7 @@ def main():
     prob.lib = counter
     st = Stepper(pkg, prob, solver_mod, mesh)
     st.precond = args.precond
+    st.mg_options = {"refresh": args.mg_refresh}
     clk = ClockSampler(local).start()
     time.sleep(1.0)
     # warm-up with the timers on, so every kernel the timed steps use (including torch's
@@ -617,6 +621,7 @@ def main():
                   "ms_per_step": max_over_ranks(j0.elapsed_time(j1) * 1e-3, world, "cuda") / 2 * 1e3,
                   "krylov_iters": [int(k) for k in prob.stats["krylov_iters"][k0:]]}
         st.precond = args.precond
+    st.mg_options = {"refresh": args.mg_refresh}
 
     # roofline of the dominant kernel (the persistent BiCGSTAB) and of the constitutive pass
     peaks = measured_peaks()
@@ -680,7 +685,8 @@ def main():
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": dict(workload_config(n, args.config), parallelism="replicas" if world > 1 else "single-gpu",
-                          precond={0: "none", 1: "jacobi", 2: "block-jacobi-3x3", 3: "multigrid-vcycle"}[args.precond]),
+                          precond={0: "none", 1: "jacobi", 2: "block-jacobi-3x3", 3: "multigrid-vcycle"}[args.precond],
+                          mg_refresh=args.mg_refresh if args.precond == 3 else None),
            "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
            "roofline": dominant,
            "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof},

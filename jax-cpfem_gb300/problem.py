@@ -347,9 +347,11 @@ class CrystalPlasticity:
         self.mg_levels = levels
         return mg
 
-    def mg_setup(self, values, **kw):
+    def mg_setup(self, values, refresh="newton", **kw):
         """Coarse operators and smoother blocks of the hierarchy for the current
-        (BC-eliminated) tangent ``values``."""
+        (BC-eliminated) tangent ``values``.  refresh="step" keeps the hierarchy of the
+        first Newton iteration of a load step for the rest of the step (the Krylov
+        operator is always the current tangent; only the preconditioner ages)."""
         mg = self.multigrid(**kw)
         fe = self.fes[0]
         if self._mg_bc_token != fe.bc_token:
@@ -357,8 +359,13 @@ class CrystalPlasticity:
             if fe.bc_dofs.numel():
                 self._mg_free[fe.bc_dofs.long()] = 0
             self._mg_bc_token = fe.bc_token
+        if refresh == "step" and getattr(self, "_mg_setup_key", None) == (fe.bc_token, self._state_token):
+            return mg
+        if refresh not in ("newton", "step"):
+            raise ValueError("mg refresh must be 'newton' or 'step'")
         with self.region("mg_setup"):
             _capi.check(self.lib.cpfem_mg_setup(ctypes.byref(mg), _dev_ptr(values), _stream()))
+        self._mg_setup_key = (fe.bc_token, self._state_token)
         return mg
 
     def csr_map(self):
