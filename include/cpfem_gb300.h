@@ -312,7 +312,8 @@ int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double*
  * (jax_solve, crystal_plasticity_OR_design/solver.py:32-33) or PETSc's ILU/Jacobi
  * (solver.py:63-88).  One V-cycle of damped 3x3 block-Jacobi smoothing on every level,
  * trilinear prolongation P (zero on Dirichlet dofs of level 0), restriction P^T and
- * Galerkin coarse operators P^T A P rebuilt from the current tangent by cpfem_mg_setup.
+ * Galerkin coarse operators P^T A P rebuilt from the current tangent by cpfem_mg_setup
+ * (P is a tensor product, so the product runs as three 1-D coarsening passes).
  * The preconditioner only changes the Krylov iterates: the solve still stops on the
  * same true-residual tolerance.  Level l+1 has (dims[l][d]-1)/2+1 nodes per direction
  * (every dims[l][d]-1 even).  The caller owns every array.
@@ -328,13 +329,17 @@ typedef struct {
   cpfem_sell_t sell[CPFEM_MG_MAX_LEVELS];     /* layout per level (level 0: the system's) */
   double* values[CPFEM_MG_MAX_LEVELS];        /* levels >= 1: coarse operators (cpfem_mg_setup) */
   double* minv[CPFEM_MG_MAX_LEVELS];          /* [9*nodes] inverted 3x3 diagonal blocks (setup) */
-  const int8_t* slot[CPFEM_MG_MAX_LEVELS];    /* levels 0..L-2: [27*nodes] slot of each neighbour
+  const int8_t* slot[CPFEM_MG_MAX_LEVELS];    /* every level: [27*nodes] slot of each neighbour
                                                  offset (dz+1)*9+(dy+1)*3+(dx+1), -1 if absent */
   double* x[CPFEM_MG_MAX_LEVELS];             /* [3*nodes] work vectors of every level */
   double* t[CPFEM_MG_MAX_LEVELS];
   double* r[CPFEM_MG_MAX_LEVELS];
   double* b[CPFEM_MG_MAX_LEVELS];             /* levels >= 1 */
   const int8_t* free_dof;                     /* [3*nodes of level 0]: 0 on Dirichlet dofs */
+  double* scratch[2];                         /* Galerkin product in three 1-D passes: stencils of
+                                                 the x-coarsened and xy-coarsened operators, each
+                                                 [243*scratch_nodes] */
+  int64_t scratch_nodes;                      /* >= max over l of dims_c[0]*dims[l][1]*dims[l][2] */
 } cpfem_mg_t;
 
 /* Host: the slot table of one level from its node-block CSR pattern (rows sorted, as

@@ -120,6 +120,8 @@ class MGHierarchy(ctypes.Structure):
         ("r", ctypes.c_void_p * MG_MAX_LEVELS),
         ("b", ctypes.c_void_p * MG_MAX_LEVELS),
         ("free_dof", ctypes.c_void_p),
+        ("scratch", ctypes.c_void_p * 2),
+        ("scratch_nodes", ctypes.c_int64),
     ]
 
 

@@ -775,7 +775,13 @@ static int mg_check(const cpfem_mg_t* mg, const cpfem_sell_t* sell) {
     CPFEM_REQUIRE(mg->dims[l][0] >= 1 && mg->dims[l][1] >= 1 && mg->dims[l][2] >= 1 && n == mg->sell[l].num_nodes,
                   "multigrid dims do not match the level's node count");
     CPFEM_REQUIRE(sell_ok(&mg->sell[l]) && mg->minv[l] && mg->x[l] && mg->t[l], "multigrid level arrays missing");
-    if (l + 1 < L) CPFEM_REQUIRE(mg->r[l] && mg->slot[l], "multigrid residual/slot arrays missing");
+    CPFEM_REQUIRE(mg->slot[l], "multigrid slot table missing");
+    if (l + 1 < L) {
+      CPFEM_REQUIRE(mg->r[l], "multigrid residual array missing");
+      const int64_t need = (int64_t)((mg->dims[l][0] - 1) / 2 + 1) * mg->dims[l][1] * mg->dims[l][2];
+      CPFEM_REQUIRE(mg->scratch[0] && mg->scratch[1] && mg->scratch_nodes >= need,
+                    "multigrid scratch missing or too small");
+    }
     if (l >= 1) {
       CPFEM_REQUIRE(mg->values[l] && mg->b[l], "multigrid coarse arrays missing");
       for (int d = 0; d < 3; ++d)
@@ -786,75 +792,78 @@ static int mg_check(const cpfem_mg_t* mg, const cpfem_sell_t* sell) {
   return CPFEM_OK;
 }
 
-// Galerkin coarse operator, one thread per (coarse node I, slot s) of the coarse layout,
-// one block per group of 32 coarse nodes: block (I, J) = sum over linked fine pairs
-// (i of I, j of J, j a neighbour of i) of w_iI w_jJ A_f(i, j), Dirichlet dofs of level 0
-// left out on both sides.  Fixed summation order: reproducible.
-__global__ void __launch_bounds__(32 * 27) k_mg_rap(const cpfem_sell_t F, const double* __restrict__ vf,
-                                                     const int8_t* __restrict__ slotf, int fx, int fy, int fz,
-                                                     const cpfem_sell_t C, int cx, int cy,
-                                                     const int8_t* __restrict__ free_dof, double* __restrict__ vc) {
-  const int g = blockIdx.x;
-  const int lane = threadIdx.x & 31, s = threadIdx.x >> 5;
-  const int64_t I = 32LL * g + lane;
-  if (I >= C.num_nodes || s >= C.group_width[g]) return;
-  const int64_t base = 9 * C.group_off[g] + lane + 288LL * s;
-  const int64_t J = C.cols[C.group_off[g] + 32LL * s + lane];
+// Galerkin coarse operator P^T A P by three 1-D passes: P = P_z (x) P_y (x) P_x, so
+// coarsening one direction at a time keeps a 27-point stencil and needs 7 (same coarse
+// neighbour) or 3 (next one) fine pairs per output block instead of up to 343.  One thread
+// per (output node, stencil offset); input and output stencils are [node][27][9]; the
+// first pass reads the sliced-ELL fine operator through its slot table (Dirichlet dofs of
+// level 0 left out on both sides), the last writes the coarse sliced-ELL operator.
+// Fixed summation order: reproducible.
+__global__ void __launch_bounds__(256) k_mg_rap_dir(int dir, int ix, int iy, int iz, int ox, int oy, int oz,
+                                                    const cpfem_sell_t F, const double* __restrict__ vf,
+                                                    const int8_t* __restrict__ slot_in,
+                                                    const double* __restrict__ sin_,
+                                                    const int8_t* __restrict__ free_dof, double* __restrict__ sout,
+                                                    const cpfem_sell_t C, const int8_t* __restrict__ slot_out,
+                                                    double* __restrict__ vc) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nout = (int64_t)ox * oy * oz;
+  if (t >= 27 * nout) return;
+  const int64_t o = t / 27;
+  const int off = (int)(t % 27);
+  int oc[3] = {(int)(o % ox), (int)((o / ox) % oy), (int)(o / ((int64_t)ox * oy))};
+  int d[3] = {off % 3 - 1, (off / 3) % 3 - 1, off / 9 - 1};
+  const int din[3] = {ix, iy, iz};
+  const int del = d[dir];
   double acc[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) acc[k] = 0.0;
-  if (!(J == I && s != C.diag_slot[I])) {
-    const int Ix = (int)(I % cx), Iy = (int)((I / cx) % cy), Iz = (int)(I / ((int64_t)cx * cy));
-    const int Jx = (int)(J % cx), Jy = (int)((J / cx) % cy), Jz = (int)(J / ((int64_t)cx * cy));
-    const int del[3] = {Jx - Ix, Jy - Iy, Jz - Iz};
-    // per direction: the linked (a, b) offsets, i = 2I + a, j = 2J + b, |i - j| <= 1
-    int pa[3][7], pb[3][7], np[3];
-    double pw[3][7];
-    bool okd = true;
-    for (int d = 0; d < 3; ++d) {
-      np[d] = 0;
-      if (del[d] < -1 || del[d] > 1) okd = false;
-      for (int a = -1; a <= 1; ++a)
-        for (int b = -1; b <= 1; ++b) {
-          const int dd = a - b - 2 * del[d];
-          if (dd >= -1 && dd <= 1 && np[d] < 7) {
-            pa[d][np[d]] = a;
-            pb[d][np[d]] = b;
-            pw[d][np[d]] = (a ? 0.5 : 1.0) * (b ? 0.5 : 1.0);
-            ++np[d];
-          }
-        }
-    }
-    if (okd) {
-      for (int kz = 0; kz < np[2]; ++kz) {
-        const int iz = 2 * Iz + pa[2][kz], jz = 2 * Jz + pb[2][kz];
-        if (iz < 0 || iz >= fz || jz < 0 || jz >= fz) continue;
-        for (int ky = 0; ky < np[1]; ++ky) {
-          const int iy = 2 * Iy + pa[1][ky], jy = 2 * Jy + pb[1][ky];
-          if (iy < 0 || iy >= fy || jy < 0 || jy >= fy) continue;
-          for (int kx = 0; kx < np[0]; ++kx) {
-            const int ix = 2 * Ix + pa[0][kx], jx = 2 * Jx + pb[0][kx];
-            if (ix < 0 || ix >= fx || jx < 0 || jx >= fx) continue;
-            const int64_t i = ix + (int64_t)fx * (iy + (int64_t)fy * iz);
-            const int64_t j = jx + (int64_t)fx * (jy + (int64_t)fy * jz);
-            const int sf = slotf[27 * i + (jz - iz + 1) * 9 + (jy - iy + 1) * 3 + (jx - ix + 1)];
-            if (sf < 0) continue;
-            const double w = pw[0][kx] * pw[1][ky] * pw[2][kz];
-            const double* blk = vf + 9 * F.group_off[i >> 5] + (i & 31) + 288LL * sf;
+  for (int a = -1; a <= 1; ++a)
+    for (int b = -1; b <= 1; ++b) {
+      const int e = 2 * del + b - a;      // input offset along dir
+      if (e < -1 || e > 1) continue;
+      int ic[3] = {oc[0], oc[1], oc[2]};
+      ic[dir] = 2 * oc[dir] + a;
+      int jc[3] = {ic[0] + d[0], ic[1] + d[1], ic[2] + d[2]};
+      jc[dir] = ic[dir] + e;
+      bool inside = true;
 #pragma unroll
-            for (int r = 0; r < 3; ++r)
+      for (int k = 0; k < 3; ++k)
+        inside = inside && ic[k] >= 0 && ic[k] < din[k] && jc[k] >= 0 && jc[k] < din[k];
+      if (!inside) continue;
+      const int64_t i = ic[0] + (int64_t)ix * (ic[1] + (int64_t)iy * ic[2]);
+      int ed[3] = {d[0], d[1], d[2]};
+      ed[dir] = e;
+      const int code = (ed[2] + 1) * 9 + (ed[1] + 1) * 3 + (ed[0] + 1);
+      const double w = (a ? 0.5 : 1.0) * (b ? 0.5 : 1.0);
+      if (sin_ == nullptr) {
+        const int sf = slot_in[27 * i + code];
+        if (sf < 0) continue;
+        const int64_t j = jc[0] + (int64_t)ix * (jc[1] + (int64_t)iy * jc[2]);
+        const double* blk = vf + 9 * F.group_off[i >> 5] + (i & 31) + 288LL * sf;
 #pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                if (free_dof != nullptr && (free_dof[3 * i + r] == 0 || free_dof[3 * j + c] == 0)) continue;
-                acc[3 * r + c] = fma(w, blk[32 * (3 * r + c)], acc[3 * r + c]);
-              }
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            if (free_dof != nullptr && (free_dof[3 * i + r] == 0 || free_dof[3 * j + c] == 0)) continue;
+            acc[3 * r + c] = fma(w, __ldg(&blk[32 * (3 * r + c)]), acc[3 * r + c]);
           }
-        }
+      } else {
+        const double* blk = sin_ + 9 * (27 * i + code);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = fma(w, __ldg(&blk[k]), acc[k]);
       }
     }
-  }
+  if (sout != nullptr) {
 #pragma unroll
-  for (int k = 0; k < 9; ++k) vc[base + 32 * k] = acc[k];
+    for (int k = 0; k < 9; ++k) sout[9 * (27 * o + off) + k] = acc[k];
+  } else {
+    const int s = slot_out[27 * o + off];
+    if (s < 0) return;
+    double* blk = vc + 9 * C.group_off[o >> 5] + (o & 31) + 288LL * s;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) blk[32 * k] = acc[k];
+  }
 }
 
 }  // namespace cpfem
@@ -887,10 +896,26 @@ int cpfem_mg_setup(const cpfem_mg_t* mg, const double* values0, void* stream) {
   CPFEM_CUDA_TRY(cudaGetLastError());
   for (int l = 0; l + 1 < mg->num_levels; ++l) {
     const double* vf = (l == 0) ? values0 : mg->values[l];
+    const int32_t* fi = mg->dims[l];
+    const int32_t* co = mg->dims[l + 1];
     const cpfem_sell_t& C = mg->sell[l + 1];
-    k_mg_rap<<<(unsigned)C.num_groups, 32 * 27, 0, s>>>(mg->sell[l], vf, mg->slot[l], mg->dims[l][0], mg->dims[l][1],
-                                                       mg->dims[l][2], C, mg->dims[l + 1][0], mg->dims[l + 1][1],
-                                                       (l == 0) ? mg->free_dof : nullptr, mg->values[l + 1]);
+    // x pass: fine SELL -> scratch[0] (co.x, fi.y, fi.z); y pass -> scratch[1] (co.x, co.y,
+    // fi.z); z pass -> the coarse SELL
+    const int64_t n1 = (int64_t)co[0] * fi[1] * fi[2], n2 = (int64_t)co[0] * co[1] * fi[2];
+    const int64_t n3 = (int64_t)co[0] * co[1] * co[2];
+    k_mg_rap_dir<<<(unsigned)ceil_div(27 * n1, 256), 256, 0, s>>>(0, fi[0], fi[1], fi[2], co[0], fi[1], fi[2],
+                                                                   mg->sell[l], vf, mg->slot[l], nullptr,
+                                                                   (l == 0) ? mg->free_dof : nullptr,
+                                                                   mg->scratch[0], C, nullptr, nullptr);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+    k_mg_rap_dir<<<(unsigned)ceil_div(27 * n2, 256), 256, 0, s>>>(1, co[0], fi[1], fi[2], co[0], co[1], fi[2],
+                                                                   mg->sell[l], nullptr, nullptr, mg->scratch[0],
+                                                                   nullptr, mg->scratch[1], C, nullptr, nullptr);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+    k_mg_rap_dir<<<(unsigned)ceil_div(27 * n3, 256), 256, 0, s>>>(2, co[0], co[1], fi[2], co[0], co[1], co[2],
+                                                                   mg->sell[l], nullptr, nullptr, mg->scratch[1],
+                                                                   nullptr, nullptr, C, mg->slot[l + 1],
+                                                                   mg->values[l + 1]);
     CPFEM_CUDA_TRY(cudaGetLastError());
     k_precond_setup<false><<<(unsigned)ceil_div(C.num_nodes, 128), 128, 0, s>>>(C, mg->values[l + 1], 2,
                                                                                 mg->minv[l + 1]);

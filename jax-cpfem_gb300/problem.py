@@ -328,20 +328,24 @@ class CrystalPlasticity:
                 mg.values[l] = buf(nvals)
                 self.mg_layouts.append((rowptr, cols, goff, keep[-1]))
                 mg.b[l] = buf(3 * n)
+            slot = np.zeros(27 * n, dtype=np.int8)
+            dd = np.asarray(d, dtype=np.int32)
+            _capi.check(self.lib.cpfem_mg_slot_table(n, dd.ctypes.data, rowptr.ctypes.data, cols.ctypes.data,
+                                                     slot.ctypes.data))
+            st = torch.tensor(slot, device=dev)
+            keep.append(st)
+            mg.slot[l] = st.data_ptr()
             if l + 1 < len(levels):
-                slot = np.zeros(27 * n, dtype=np.int8)
-                dd = np.asarray(d, dtype=np.int32)
-                _capi.check(self.lib.cpfem_mg_slot_table(n, dd.ctypes.data, rowptr.ctypes.data, cols.ctypes.data,
-                                                         slot.ctypes.data))
-                st = torch.tensor(slot, device=dev)
-                keep.append(st)
-                mg.slot[l] = st.data_ptr()
                 mg.r[l] = buf(3 * n)
             mg.minv[l] = buf(9 * n)
             mg.x[l] = buf(3 * n)
             mg.t[l] = buf(3 * n)
         free = torch.ones(3 * self.num_nodes, dtype=torch.int8, device=dev)
         mg.free_dof = free.data_ptr()
+        # stencils of the x- and xy-coarsened operators of the three-pass Galerkin product
+        sn = max(((d[0] - 1) // 2 + 1) * d[1] * d[2] for d in levels[:-1])
+        mg.scratch[0], mg.scratch[1] = buf(243 * sn), buf(243 * sn)
+        mg.scratch_nodes = sn
         self._mg, self._mg_keep, self._mg_free, self._mg_key = mg, keep, free, key
         self._mg_bc_token = None
         self.mg_levels = levels
