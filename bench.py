@@ -72,6 +72,7 @@ class Stepper:
         self.i = 0
         self.precond = 1
         self.mg_options = None
+        self.grid_blocks = 0
         self.params = prob.internal_vars
         import torch
         self.sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
@@ -88,7 +89,8 @@ class Stepper:
             guess = sol_h.to("cuda", non_blocking=True)
         else:
             guess = self.sol
-        sol = self.solver.solver(prob, {"jax_solver": {"precond": self.precond, "mg_options": self.mg_options},
+        sol = self.solver.solver(prob, {"jax_solver": {"precond": self.precond, "mg_options": self.mg_options,
+                                                       "grid_blocks": self.grid_blocks},
                                         "initial_guess": [guess.reshape(-1, 3)]})[0]
         sig = prob.compute_avg_stress(sol, self.params)
         self.params = prob.update_int_vars_gp(sol, self.params)
@@ -492,6 +494,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
                     help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
+    ap.add_argument("--no-tune", action="store_true", help="skip the linear-solver autotuning before warm-up ends")
     ap.add_argument("--no-jacobi-leg", action="store_true",
                     help="skip the two extra load steps timed with the reference's Jacobi preconditioner")
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"],
@@ -552,8 +555,23 @@ def main():
     # warm-up with the timers on, so every kernel the timed steps use (including torch's
     # small reductions) has run once before the clock starts
     prob.timing = True
-    for _ in range(args.warmup):
+    tuned = None
+    for w in range(args.warmup):
         st.step()
+        if w == 0 and args.precond == 3 and not args.no_tune:
+            # autotune the multigrid / launch settings on the next step's first Newton system
+            tuning = import_module("jax-cpfem_gb300.tuning")
+            nodes, comps, vals = roller_lists(pkg, mesh, STRAIN_STEP * (st.i + 1))
+            prob.fes[0].set_dirichlet_lists(nodes, comps, vals)
+            prob.set_params(st.params)
+            res, A = solver_mod.newton_update_helper(prob, st.sol)
+            x0 = solver_mod.initial_increment(prob, st.sol).clone()
+            cfg, table = tuning.tune_linear_solver(prob, A, -res, x0)
+            st.grid_blocks = cfg["grid_blocks"]
+            st.mg_options = dict({k: v for k, v in cfg.items() if k != "grid_blocks"}, refresh=args.mg_refresh)
+            tuned = {"chosen": cfg, "candidates": len(table),
+                     "default_ms": round(table[0][1], 3), "chosen_ms": round(min(t[1] for t in table
+                                                                                   if t[0] == cfg), 3)}
     torch.cuda.synchronize()
     prob.timer_ms()
 
@@ -607,7 +625,8 @@ def main():
     # the same load steps with the reference's Jacobi-preconditioned BiCGSTAB, for comparison
     jacobi = None
     if args.precond != 1 and not args.no_jacobi_leg:
-        st.precond = 1
+        st.precond, gb = 1, st.grid_blocks
+        st.grid_blocks = 0
         st.step()
         torch.cuda.synchronize()
         k0 = len(prob.stats["krylov_iters"])
@@ -620,8 +639,7 @@ def main():
         jacobi = {"precond": "jacobi (the reference's)", "steps": 2,
                   "ms_per_step": max_over_ranks(j0.elapsed_time(j1) * 1e-3, world, "cuda") / 2 * 1e3,
                   "krylov_iters": [int(k) for k in prob.stats["krylov_iters"][k0:]]}
-        st.precond = args.precond
-    st.mg_options = {"refresh": args.mg_refresh}
+        st.precond, st.grid_blocks = args.precond, gb
 
     # roofline of the dominant kernel (the persistent BiCGSTAB) and of the constitutive pass
     peaks = measured_peaks()
@@ -690,7 +708,7 @@ def main():
            "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
            "roofline": dominant,
            "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof},
-           "region_shares": shares, "jacobi_leg": jacobi,
+           "region_shares": shares, "jacobi_leg": jacobi, "tuned_linear_solver": tuned,
            "cpu_baseline": cpu,
            "regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
            "newton_iters_per_step": newton, "krylov_iters": krylov, "gp_passes": passes,

@@ -358,6 +358,9 @@ typedef struct {
   int32_t max_restarts;
   double tol, atol;
   const cpfem_mg_t* mg;   /* precond 3: a hierarchy set up for this matrix */
+  int32_t grid_blocks;    /* blocks of the persistent launch; 0: one per 256 nodes, at most the
+                             co-resident limit (larger requests are clamped to it) */
+  int32_t pad;
 } cpfem_krylov_opts_t;
 int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
                       const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream);

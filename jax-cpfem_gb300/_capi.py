@@ -134,6 +134,8 @@ class KrylovOpts(ctypes.Structure):
         ("tol", ctypes.c_double),
         ("atol", ctypes.c_double),
         ("mg", ctypes.POINTER(MGHierarchy)),
+        ("grid_blocks", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
     ]
 
 

@@ -716,7 +716,7 @@ static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms) {
 template <bool TRANS>
 static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double* b, double* x, int precond,
                         double tol, double atol, int32_t maxiter, void* workspace, int32_t* info, cudaStream_t s,
-                        int max_restarts = 0, const cpfem_mg_t* mgp = nullptr) {
+                        int max_restarts = 0, const cpfem_mg_t* mgp = nullptr, int grid_blocks = 0) {
   KWork w;
   carve(workspace, L.num_nodes, &w);
   CPFEM_CUDA_TRY(cudaMemsetAsync(w.sync, 0, sizeof(GridSync), s));
@@ -736,6 +736,7 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
     return CPFEM_ERR_CUDA;
   }
   int64_t blocks = std::min<int64_t>((int64_t)per_sm * sms, ceil_div(L.num_nodes, kPThreads));
+  if (grid_blocks > 0) blocks = std::min<int64_t>((int64_t)per_sm * sms, grid_blocks);
   blocks = std::max<int64_t>(1, std::min<int64_t>(blocks, kMaxBlocks));
   cpfem_sell_t Lc = L;
   const double* bb = b;
@@ -956,20 +957,21 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
   }
   CPFEM_REQUIRE(opts->maxiter >= 0, "maxiter must be >= 0");
   CPFEM_REQUIRE(opts->max_restarts >= 0, "max_restarts must be >= 0");
+  CPFEM_REQUIRE(opts->grid_blocks >= 0, "grid_blocks must be >= 0");
   CPFEM_REQUIRE(!opts->transpose || sell->tpos != nullptr, "transpose needs tpos");
   cudaStream_t s = (cudaStream_t)stream;
   if (opts->transpose)
     return run_bicgstab<true>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                              info, s, opts->max_restarts);
+                              info, s, opts->max_restarts, nullptr, opts->grid_blocks);
   return run_bicgstab<false>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                             info, s, opts->max_restarts, opts->mg);
+                             info, s, opts->max_restarts, opts->mg, opts->grid_blocks);
 }
 
 int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x, int32_t precond,
                    int32_t transpose, double tol, double atol, int32_t maxiter, void* workspace, int32_t* info,
                    void* stream) {
   CPFEM_REQUIRE(precond >= 0 && precond <= 2, "precond must be 0, 1 or 2 (multigrid: cpfem_bicgstab_ex)");
-  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol, nullptr};
+  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol, nullptr, 0, 0};
   return cpfem_bicgstab_ex(sell, values, b, x, &o, workspace, info, stream);
 }
 

@@ -289,9 +289,11 @@ class CrystalPlasticity:
         """Geometric multigrid hierarchy of a structured box mesh for the BiCGSTAB
         preconditioner ``precond=3`` (built once; coarse operators by ``mg_setup``).
         Levels halve the cell counts while every count stays even, up to max_levels."""
-        key = (max_levels, pre_sweeps, post_sweeps, coarse_sweeps, omega)
-        if getattr(self, "_mg", None) is not None and self._mg_key == key:
-            return self._mg
+        if getattr(self, "_mg", None) is not None and self._mg_key == max_levels:
+            mg = self._mg   # same levels: only the smoother settings may change
+            mg.pre_sweeps, mg.post_sweeps, mg.coarse_sweeps = pre_sweeps, post_sweeps, coarse_sweeps
+            mg.omega = float(omega)
+            return mg
         dims = structured_dims(self.mesh.points)
         if dims is None:
             raise ValueError("the multigrid preconditioner needs a structured box mesh (a tensor grid of nodes "
@@ -346,7 +348,7 @@ class CrystalPlasticity:
         sn = max(((d[0] - 1) // 2 + 1) * d[1] * d[2] for d in levels[:-1])
         mg.scratch[0], mg.scratch[1] = buf(243 * sn), buf(243 * sn)
         mg.scratch_nodes = sn
-        self._mg, self._mg_keep, self._mg_free, self._mg_key = mg, keep, free, key
+        self._mg, self._mg_keep, self._mg_free, self._mg_key = mg, keep, free, max_levels
         self._mg_bc_token = None
         self.mg_levels = levels
         return mg

@@ -37,7 +37,7 @@ def norm(problem, x):
 
 
 def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, restarts=0,
-             mg_options=None):
+             mg_options=None, grid_blocks=0):
     """``jax.scipy.sparse.linalg.bicgstab`` on the device matrix (``solver.py:34-40``), one
     persistent cooperative launch.  precond: 0 none, 1 Jacobi 1/diag(A) (the
     reference), 2 3x3 block-Jacobi, 3 geometric multigrid V-cycle (structured box
@@ -50,7 +50,7 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
-                            float(tol), float(atol), None)
+                            float(tol), float(atol), None, int(grid_blocks), 0)
     if int(precond) == 3:
         if A.transposed:
             raise ValueError("the multigrid preconditioner solves A x = b only (no transposed solve)")
@@ -71,7 +71,7 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
     rs = 20 if rs is True else int(rs or 0)
     x, k, ok = bicgstab(problem, A, b, x0, precond=pc, tol=opts.get("tol", 1e-10),
                         atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000), restarts=rs,
-                        mg_options=opts.get("mg_options"))
+                        mg_options=opts.get("mg_options"), grid_blocks=opts.get("grid_blocks", 0))
     problem.stats["krylov_iters"].append(k)
     r = A.matvec(x)
     r.sub_(b)

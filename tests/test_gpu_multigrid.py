@@ -125,3 +125,18 @@ def test_load_steps_with_multigrid_match_oracle(pkg, gpu):
     s = np.array(out)
     assert np.abs(s - s_o).max() / np.abs(s_o).max() < 1e-8
     assert float(np.abs(sol.cpu().numpy() - u_o).max() / np.abs(u_o).max()) < 1e-8
+
+
+def test_autotuner_picks_a_converging_configuration(pkg, gpu):
+    problem_mod, solver_mod = gpu
+    tuning = importlib.import_module("jax-cpfem_gb300.tuning")
+    _, _, _, _, _, prob, u = _plastic_case(pkg, problem_mod, n=8)
+    res, A = solver_mod.newton_update_helper(prob, u)
+    x0 = solver_mod.initial_increment(prob, u).clone()
+    cfg, table = tuning.tune_linear_solver(prob, A, -res, x0, reps=1,
+                                           search=(("omega", (0.4, 0.5)), ("grid_blocks", (0, 8))))
+    assert len(table) >= 3 and set(cfg) == set(tuning.DEFAULT)
+    mg = {k: cfg[k] for k in ("max_levels", "pre_sweeps", "post_sweeps", "coarse_sweeps", "omega")}
+    x, k, ok = solver_mod.bicgstab(prob, A, -res, x0, precond=3, mg_options=mg, grid_blocks=cfg["grid_blocks"])
+    xj, kj, okj = solver_mod.bicgstab(prob, A, -res, x0, precond=1)
+    assert ok and okj and float((x - xj).abs().max() / xj.abs().max()) < 1e-8
