@@ -102,6 +102,10 @@ typedef struct {
                                  untouched (a ragged batch skips its converged instances) */
   int32_t num_listed;
   int32_t pad;
+  const int32_t* order;       /* [num_gp] permutation or NULL (no cell list): thread t
+                                 evaluates GP order[t].  Ordering GPs by their previous
+                                 local-Newton iteration count keeps a warp's lanes busy for
+                                 the same number of iterations; results are unchanged. */
 } cpfem_gp_args_t;
 
 /*

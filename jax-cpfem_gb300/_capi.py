@@ -68,6 +68,7 @@ class GPArgs(ctypes.Structure):
         ("cell_list", ctypes.c_void_p),
         ("num_listed", ctypes.c_int32),
         ("pad", ctypes.c_int32),
+        ("order", ctypes.c_void_p),
     ]
 
 

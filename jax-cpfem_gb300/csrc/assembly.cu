@@ -64,6 +64,13 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
       return;
     }
     gp = 8 * c + (tid & 7);
+  } else if (a.order != nullptr) {
+    if (tid >= G) return;
+    gp = a.order[tid];
+    if (gp < 0 || gp >= G) {
+      atomicOr(a.status, CPFEM_GP_BOUNDS);
+      return;
+    }
   }
   if (gp >= G) return;
 
@@ -127,19 +134,13 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
     if (bits) atomicOr(a.status, bits);
   }
 
-  double Gm[9], H[9], P[9];
+  double Gm[9], H[9], W[9], Y[9], P[9], idet;
   mm3(Fpi, R, Gm);
+  cp_stress<NS>(F, Gm, st, H, W, Y, idet, P);
   const double w = (a.weight_jxw && a.jxw != nullptr) ? a.jxw[gp] : 1.0;
-  double* tan = a.tangent;
-  auto store = [&](int kl, const double* col) {
-#pragma unroll
-    for (int c = 0; c < 9; ++c) tan[(int64_t)(9 * c + kl) * G + gp] = col[c] * w;
-  };
-  if (TANGENT && tan != nullptr)
-    cp_outputs<NS, true>(m, cc, F, Gm, st, H, P, store);
-  else
-    cp_outputs<NS, false>(m, cc, F, Gm, st, H, P, store);
 
+  // every output but the tangent first, so that the tangent computation (the register-
+  // heaviest part) runs with only what it needs live
   if (a.pk1 != nullptr)
 #pragma unroll
     for (int c = 0; c < 9; ++c) a.pk1[c * G + gp] = P[c] * w;
@@ -178,6 +179,14 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
     for (int c = 0; c < 9; ++c) a.s_out[c * G + gp] = Sg[c];
   }
   if (a.iters != nullptr) a.iters[gp] = st.iters;
+  if (TANGENT && a.tangent != nullptr) {
+    double* tan = a.tangent;
+    auto store = [&](int kl, const double* col) {
+#pragma unroll
+      for (int c = 0; c < 9; ++c) tan[(int64_t)(9 * c + kl) * G + gp] = col[c] * w;
+    };
+    cp_tangent<NS>(m, cc, F, Gm, st, H, W, Y, idet, store);
+  }
 }
 
 // ------------------------------------------------------------------------------------
@@ -382,6 +391,8 @@ int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void
   CPFEM_REQUIRE(a.cell_list == nullptr || (a.u != nullptr && a.status != nullptr && a.num_listed >= 0 &&
                                            a.num_listed <= a.num_cells),
                 "a cell list needs nodal u, a status word and 0 <= num_listed <= num_cells");
+  CPFEM_REQUIRE(a.order == nullptr || (a.cell_list == nullptr && a.status != nullptr),
+                "an evaluation order excludes a cell list and needs a status word");
   CPFEM_REQUIRE(a.slip_new == nullptr || a.slip != nullptr, "slip_new needs slip");
   CPFEM_REQUIRE(md.qmode == 0 || md.num_slip % 3 == 0, "qmode 1 needs num_slip % 3 == 0");
   cudaStream_t s = (cudaStream_t)stream;

@@ -164,31 +164,37 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, 
   st.iters = it;
 }
 
-// Stress and consistent tangent at the converged state.
+// Stress at the converged state.
 //   H = Fp^-1_old R B,  Fe_l = F H,  P = F Y,  Y = H s H^T / det H
-// dP/dF = d_ik Y_lJ + (dP/ds)(ds/dF) with ds/dF = J^-1 C : sym(Fe_l[k,:] (x) H[l,:]),
-// the implicit-function tangent of f_jvp (models_copper.py:251-259).
-// The tangent column for F_kl is handed to store_col(kl, col[9]) as soon as it is
-// known, so the 81 entries never need to be live at once.
-template <int NS, bool WITH_TANGENT, class StoreCol>
-CPFEM_HD void cp_outputs(const MatDev& m, const Cub& cc, const double* F, const double* G /*Fp^-1_old R*/,
-                                           const GPSolve<NS>& st, double* H, double* P,
-                                           StoreCol store_col) {
-  double S[9], W[9], Y[9];
+// (algebraically the reference's det(F) sigma F^-T with sigma = Fe S Fe^T / det Fe,
+// models_copper.py:155-162).  W = s H^T and 1/det H are kept for the tangent.
+template <int NS>
+CPFEM_HD void cp_stress(const double* F, const double* G /*Fp^-1_old R*/, const GPSolve<NS>& st, double* H,
+                        double* W, double* Y, double& idet, double* P) {
+  double S[9];
   mm3(G, st.B, H);
   S[0] = st.s[0]; S[4] = st.s[1]; S[8] = st.s[2];
   S[5] = S[7] = st.s[3];
   S[2] = S[6] = st.s[4];
   S[1] = S[3] = st.s[5];
-  const double detH = det3(H);
-  const double idet = 1.0 / detH;
+  idet = 1.0 / det3(H);
   mm3_bt(S, H, W);           // W = s H^T
   mm3(H, W, Y);              // H s H^T
 #pragma unroll
   for (int k = 0; k < 9; ++k) Y[k] *= idet;
   mm3(F, Y, P);
-  if (!WITH_TANGENT) return;
+}
 
+// Consistent tangent at the converged state:
+// dP/dF = d_ik Y_lJ + (dP/ds)(ds/dF) with ds/dF = J^-1 C : sym(Fe_l[k,:] (x) H[l,:]),
+// the implicit-function tangent of f_jvp (models_copper.py:251-259).
+// The tangent column for F_kl is handed to store_col(kl, col[9]) as soon as it is
+// known, so the 81 entries never need to be live at once.  Called after every other
+// output of the Gauss point is written, so only what it needs is live.
+template <int NS, class StoreCol>
+CPFEM_HD void cp_tangent(const MatDev& m, const Cub& cc, const double* F, const double* G /*Fp^-1_old R*/,
+                         const GPSolve<NS>& st, const double* H, const double* W, const double* Y, double idet,
+                         StoreCol store_col) {
   // dP/ds for the 6 symmetric basis directions
   double Bi[9];
   inv3(st.B, Bi);

@@ -204,6 +204,7 @@ class CrystalPlasticity:
         self.stats = {"gp_passes": 0, "krylov_iters": [], "local_iters_max": 0}
         self.timing = False
         self.timers = {}
+        self.sort_gps = True     # order each tangent pass by the previous pass's local-Newton counts
         self.custom_init(*additional_info)
 
     # ------------------------------------------------------------------ set-up
@@ -626,13 +627,18 @@ class CrystalPlasticity:
             values = self._buf("values", (self.num_values,))
             values.zero_()
             dw = self._buf("tangent_w", (81, G))
-        its = self._buf("iters", (G,), torch.int32) if self.timing else None
+        ordered = self.sort_gps and need_tangent and cell_list is None
+        its = self._buf("iters", (G,), torch.int32) if (self.timing or ordered) else None
+        order = self._bufs.get("gp_order") if ordered else None
         if need_tangent and trial is None:
             trial = self.new_trial()
         trial = trial if need_tangent else {}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its, cell_list=cell_list, **trial)
+                             iters=its, cell_list=cell_list, order=order, **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
+        if ordered:
+            # the next pass runs the GPs heaviest first, in runs of equal local-Newton counts
+            self._bufs["gp_order"] = torch.argsort(its, descending=True, stable=True).to(torch.int32)
         if its is not None and need_tangent and cell_list is None:
             acc = self._bufs.setdefault("iters_acc", torch.zeros(2, dtype=torch.float64, device=self.device))
             acc[0] += its.sum()

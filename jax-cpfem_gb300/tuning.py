@@ -21,10 +21,10 @@ DEFAULT = {"max_levels": 5, "pre_sweeps": 1, "post_sweeps": 1, "coarse_sweeps": 
            "grid_blocks": 0}
 SEARCH = (("omega", (0.35, 0.4, 0.45)),
           ("pre_sweeps", (1, 2)),
-          ("post_sweeps", (1, 2)),
+          ("post_sweeps", (0, 1, 2)),
           ("coarse_sweeps", (4, 8, 12)),
           ("max_levels", (3, 4, 5)),
-          ("grid_blocks", (0, 152, 304, 456)))
+          ("grid_blocks", (0, 76, 104, 152, 304)))
 
 
 def _time_solve(problem, A, b, x0, cfg, reps):
