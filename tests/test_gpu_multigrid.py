@@ -140,3 +140,32 @@ def test_autotuner_picks_a_converging_configuration(pkg, gpu):
     x, k, ok = solver_mod.bicgstab(prob, A, -res, x0, precond=3, mg_options=mg, grid_blocks=cfg["grid_blocks"])
     xj, kj, okj = solver_mod.bicgstab(prob, A, -res, x0, precond=1)
     assert ok and okj and float((x - xj).abs().max() / xj.abs().max()) < 1e-8
+
+
+def test_golden_case4_with_multigrid(pkg, gpu):
+    """The first 20 steps of calibration_case4 scenario 0 (20^3 Neper voxels, corner BCs with
+    a free rigid rotation about z) with the multigrid-preconditioned solve: mean sigma_zz
+    against the reference's curve."""
+    import os
+    problem_mod, solver_mod = gpu
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+    L = 0.0295
+    mesh = pkg.box_mesh(20, 20, 20, L, L, L)
+    prob = gpu_problem(pkg, problem_mod, pkg.material.CALIB_CASE4, mesh, gold["case4_quat"],
+                       gold["case4_grain"].astype(np.int64))
+    c = pkg.mesh.corner_nodes(mesh.points, (0.0, 0.0, 0.0))
+    bot, top = pkg.mesh.face_nodes(mesh.points, 2, 0.0), pkg.mesh.face_nodes(mesh.points, 2, L)
+    disps, ts = np.linspace(0, 0.025 * L, 81), np.linspace(0, 2.5, 81)
+    sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
+    params = prob.internal_vars
+    out = []
+    for i in range(20):
+        prob.dt = float(ts[i + 1] - ts[i])
+        prob.fes[0].set_dirichlet_lists([c, c, bot, top], [0, 1, 2, 2], [0.0, 0.0, 0.0, float(disps[i + 1])])
+        prob.set_params(params)
+        sol = solver_mod.solver(prob, {"jax_solver": {"precond": "mg", "restart_on_breakdown": True}, "tol": 1e-7,
+                                       "line_search_flag": True, "initial_guess": [sol.reshape(-1, 3)]})[0].reshape(-1)
+        out.append(float(prob.compute_avg_stress(sol.reshape(-1, 3), params)[:, 2, 2].mean()))
+        params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
+    rel = np.abs((np.array(out) - gold["case4_szz"][:20]) / gold["case4_szz"][:20])
+    assert rel.max() < 1e-5, rel
