@@ -392,7 +392,9 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
 
     disps = STRAIN_STEP * np.arange(nsteps + 1)
     ts = DT * np.arange(nsteps + 1)
-    h = adjoint.LoadHistory(prob, disps, ts, bc_fn, quat)
+    # forward and transposed (adjoint) solves with the same preconditioner
+    h = adjoint.LoadHistory(prob, disps, ts, bc_fn, quat, solver_options={"jax_solver": {"precond": args.precond}},
+                            adjoint_options={"precond": args.precond})
     theta = np.array([spec.h, spec.gss_initial, spec.t_sat, spec.gss_a, spec.xm])
     euler = np.zeros((N_GRAINS, 3))
     # synthetic target: h0, g0, gs scaled by 1.1 under the same seed
@@ -411,7 +413,8 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
     out = {"metric": METRIC, "value": t_bwd / t_fwd, "unit": "backward/forward time", "higher_is_better": False,
            "n_gpus": 1, "steps": nsteps, "warmup": 0, "dtype": "f64", "data": "synthetic",
            "config": dict(workload_config(n), workload=f"adjoint-fcc-polycrystal-{n}^3-{N_GRAINS}grains",
-                          load_steps=nsteps, params="h0,g0,gs,a,m + 64x3 Euler angles"),
+                          load_steps=nsteps, params="h0,g0,gs,a,m + 64x3 Euler angles",
+                          precond={1: "jacobi", 2: "block-jacobi-3x3", 3: "multigrid-vcycle"}.get(args.precond)),
            "forward_s": t_fwd, "backward_s": t_bwd, "gradient_over_forward": (t_fwd + t_bwd) / t_fwd,
            "objective": float(((s - target) ** 2).mean()), "theta_grad": tb.tolist(),
            "euler_grad_norm": float(np.linalg.norm(eb)), "adjoint_krylov_iters": h.krylov_iters}

@@ -252,26 +252,37 @@ __device__ __forceinline__ void mg_xyz(int64_t a, const int32_t* dims, int& x, i
   z = (int)(q / dims[1]);
 }
 
+// z = D^-1 v with the stored inverse diagonal block; TRANS uses its transpose, which is
+// the inverse of the diagonal block of A^T.
+template <bool TRANS = false>
 __device__ __forceinline__ void mg_apply_minv(const double* __restrict__ minv, int64_t a, const double* v,
                                               double* out) {
   const double* bi = minv + 9 * a;
+  if (TRANS) {
 #pragma unroll
-  for (int i = 0; i < 3; ++i) out[i] = fma(bi[3 * i], v[0], fma(bi[3 * i + 1], v[1], bi[3 * i + 2] * v[2]));
+    for (int i = 0; i < 3; ++i) out[i] = fma(bi[i], v[0], fma(bi[3 + i], v[1], bi[6 + i] * v[2]));
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) out[i] = fma(bi[3 * i], v[0], fma(bi[3 * i + 1], v[1], bi[3 * i + 2] * v[2]));
+  }
 }
 
-// One damped block-Jacobi sweep at node a: T = X + omega Minv (B - A X).
+// One damped block-Jacobi sweep at node a: T = X + omega Minv (B - A X) (A^T when TRANS).
+template <bool TRANS>
 __device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const double* V, const double* minv,
                                          const double* B, const double* X, double* T, double omega, int64_t a) {
   double acc[3], r[3], z[3];
-  sell_rows<false, true>(S, V, X, a, acc);
+  sell_rows<TRANS, true>(S, V, X, a, acc);
 #pragma unroll
   for (int i = 0; i < 3; ++i) r[i] = B[3 * a + i] - acc[i];
-  mg_apply_minv(minv, a, r, z);
+  mg_apply_minv<TRANS>(minv, a, r, z);
 #pragma unroll
   for (int i = 0; i < 3; ++i) T[3 * a + i] = fma(omega, z[i], __ldcg(&X[3 * a + i]));
 }
 
-// Rows of node a restricted to the slots j = q (mod 4) (one lane of a quad).
+// Rows of node a of A x (A^T x when TRANS) restricted to the slots j = q (mod 4) (one
+// lane of a quad).
+template <bool TRANS>
 __device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const double* __restrict__ vals,
                                                const double* x, int64_t a, int q, double* acc) {
   const int64_t g = a >> 5;
@@ -284,10 +295,18 @@ __device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const doub
   for (int j = q; j < w; j += 4) {
     const int64_t b = __ldg(&L.cols[c0 + 32 * j]);
     const double x0 = __ldcg(&x[3 * b]), x1 = __ldcg(&x[3 * b + 1]), x2 = __ldcg(&x[3 * b + 2]);
-    const double* vb = v0 + 288 * j;
-    a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[32]), x1, fma(__ldg(&vb[64]), x2, a0)));
-    a1 = fma(__ldg(&vb[96]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[160]), x2, a1)));
-    a2 = fma(__ldg(&vb[192]), x0, fma(__ldg(&vb[224]), x1, fma(__ldg(&vb[256]), x2, a2)));
+    if (!TRANS) {
+      const double* vb = v0 + 288 * j;
+      a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[32]), x1, fma(__ldg(&vb[64]), x2, a0)));
+      a1 = fma(__ldg(&vb[96]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[160]), x2, a1)));
+      a2 = fma(__ldg(&vb[192]), x0, fma(__ldg(&vb[224]), x1, fma(__ldg(&vb[256]), x2, a2)));
+    } else {
+      const int64_t tp = __ldg(&L.tpos[c0 + 32 * j]);
+      const double* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
+      a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[96]), x1, fma(__ldg(&vb[192]), x2, a0)));
+      a1 = fma(__ldg(&vb[32]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[224]), x2, a1)));
+      a2 = fma(__ldg(&vb[64]), x0, fma(__ldg(&vb[160]), x1, fma(__ldg(&vb[256]), x2, a2)));
+    }
   }
   acc[0] = a0;
   acc[1] = a1;
@@ -306,19 +325,21 @@ __device__ __forceinline__ void quad_sum3(double* v) {
 // nodes a = tq, tq + sq, ... (tq = this lane's quad, sq = the quads taking part; a warp
 // holds 8 consecutive quads and runs the padded loops in lockstep, so the shuffles always
 // see the whole warp); lane 0 of a node's quad owns its writes.
+template <bool TRANS>
 __device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, int l, double* X, int64_t tq, int64_t sq,
                                                 int q) {
   if (q != 0) return;
   const double* B = mg.b[l];
   for (int64_t a = tq; a < mg.sell[l].num_nodes; a += sq) {
     double v[3] = {B[3 * a], B[3 * a + 1], B[3 * a + 2]}, z[3];
-    mg_apply_minv(mg.minv[l], a, v, z);
+    mg_apply_minv<TRANS>(mg.minv[l], a, v, z);
 #pragma unroll
     for (int i = 0; i < 3; ++i) X[3 * a + i] = mg.omega * z[i];
   }
 }
 
 // T = X + omega Minv (B - A X)  (residual = false)  or  R = B - A X  (residual = true)
+template <bool TRANS>
 __device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, int l, const double* X, double* T, bool residual,
                                           int64_t tq, int64_t sq, int q) {
   const cpfem_sell_t& S = mg.sell[l];
@@ -326,7 +347,7 @@ __device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, int l, const dou
   const int64_t n = S.num_nodes, npad = (n + 7) / 8 * 8;
   for (int64_t a = tq; a < npad; a += sq) {
     double acc[3] = {0.0, 0.0, 0.0};
-    if (a < n) sell_rows_quad(S, mg.values[l], X, a, q, acc);
+    if (a < n) sell_rows_quad<TRANS>(S, mg.values[l], X, a, q, acc);
     quad_sum3(acc);
     if (a < n && q == 0) {
       double r[3];
@@ -337,7 +358,7 @@ __device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, int l, const dou
         for (int i = 0; i < 3; ++i) T[3 * a + i] = r[i];
       } else {
         double z[3];
-        mg_apply_minv(mg.minv[l], a, r, z);
+        mg_apply_minv<TRANS>(mg.minv[l], a, r, z);
 #pragma unroll
         for (int i = 0; i < 3; ++i) T[3 * a + i] = fma(mg.omega, z[i], X[3 * a + i]);
       }
@@ -411,6 +432,7 @@ constexpr int64_t kMgLocalNodes = 256;   // levels this small run inside block 0
 // block barriers while the other blocks wait at the next grid barrier.  Which of x / t
 // holds a level's iterate follows from the sweep counts alone, so every block knows it.
 // Returns with out complete for this thread's own nodes.
+template <bool TRANS>
 __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0, const double* in, double* out,
                           int64_t t0, int64_t stride, GridSync* gs, unsigned int& gen, bool& ok) {
   const int L = mg.num_levels;
@@ -437,20 +459,20 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     if (l == 0) {
       for (int64_t a = t0; a < n; a += stride) {
         double v[3] = {in[3 * a], in[3 * a + 1], in[3 * a + 2]}, z[3];
-        mg_apply_minv(mg.minv[0], a, v, z);
+        mg_apply_minv<TRANS>(mg.minv[0], a, v, z);
 #pragma unroll
         for (int i = 0; i < 3; ++i) X[3 * a + i] = om * z[i];
       }
     } else {
-      mgq_first_sweep(mg, l, X, tq, sq, q);
+      mgq_first_sweep<TRANS>(mg, l, X, tq, sq, q);
     }
     const int nsw = (l == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
     for (int k = 1; k < nsw; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < n; a += stride) mg_sweep(S, V, mg.minv[0], in, X, T, om, a);
+        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, V, mg.minv[0], in, X, T, om, a);
       } else {
-        mgq_apply(mg, l, X, T, false, tq, sq, q);
+        mgq_apply<TRANS>(mg, l, X, T, false, tq, sq, q);
       }
       double* tmp = X; X = T; T = tmp;
     }
@@ -460,7 +482,7 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     if (l == 0) {
       for (int64_t a = t0; a < n; a += stride) {
         double acc[3];
-        sell_rows<false, true>(S, V, X, a, acc);
+        sell_rows<TRANS, true>(S, V, X, a, acc);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
           const double rv = in[3 * a + i] - acc[i];
@@ -468,7 +490,7 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
         }
       }
     } else {
-      mgq_apply(mg, l, X, R, true, tq, sq, q);
+      mgq_apply<TRANS>(mg, l, X, R, true, tq, sq, q);
     }
     ok = grid_barrier(gs, gen) && ok;
     if (l + 1 < lb) {
@@ -479,16 +501,16 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
       for (int m = lb; m < L; ++m) {
         double* Xm = mg.x[m];
         double* Tm = mg.t[m];
-        mgq_first_sweep(mg, m, Xm, tqb, sqb, q);
+        mgq_first_sweep<TRANS>(mg, m, Xm, tqb, sqb, q);
         const int nswm = (m == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
         for (int k = 1; k < nswm; ++k) {
           __syncthreads();
-          mgq_apply(mg, m, Xm, Tm, false, tqb, sqb, q);
+          mgq_apply<TRANS>(mg, m, Xm, Tm, false, tqb, sqb, q);
           double* tmp = Xm; Xm = Tm; Tm = tmp;
         }
         if (m == L - 1) break;
         __syncthreads();
-        mgq_apply(mg, m, Xm, mg.r[m], true, tqb, sqb, q);
+        mgq_apply<TRANS>(mg, m, Xm, mg.r[m], true, tqb, sqb, q);
         __syncthreads();
         mgq_restrict(mg, m, mg.r[m], tqb, sqb, q);
       }
@@ -500,7 +522,7 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
         if (q == 0) mg_prolong(mg, m, Xm, Xc, tqb, sqb);
         for (int k = 0; k < mg.post_sweeps; ++k) {
           __syncthreads();
-          mgq_apply(mg, m, Xm, Tm, false, tqb, sqb, q);
+          mgq_apply<TRANS>(mg, m, Xm, Tm, false, tqb, sqb, q);
           double* tmp = Xm; Xm = Tm; Tm = tmp;
         }
       }
@@ -520,9 +542,9 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     for (int k = 0; k < mg.post_sweeps; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep(S, V, mg.minv[0], in, X, T, om, a);
+        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, V, mg.minv[0], in, X, T, om, a);
       } else {
-        mgq_apply(mg, l, X, T, false, tq, sq, q);
+        mgq_apply<TRANS>(mg, l, X, T, false, tq, sq, q);
       }
       double* tmp = X; X = T; T = tmp;
     }
@@ -589,7 +611,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         for (int i = 0; i < 3; ++i) w.phat[3 * a + i] = ph[i];
       }
     }
-    if constexpr (MG) mg_vcycle(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok);
+    if constexpr (MG) mg_vcycle<TRANS>(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok);
     ok = grid_barrier(w.sync, gen) && ok;
     // q = A phat ; alpha = rho_new / (rhat . q)
     double v1[1] = {0.0};
@@ -624,7 +646,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
     }
     ok = grid_reduce<1>(vs, parts(), w.sync, gen, smem, bcast) && ok;
     if constexpr (MG) {
-      mg_vcycle(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
+      mg_vcycle<TRANS>(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
       ok = grid_barrier(w.sync, gen) && ok;
     }
     const bool early = vs[0] < atol2;
@@ -728,7 +750,7 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   memset(&mg, 0, sizeof(mg));
   if (precond == 3) mg = *mgp;
   int per_sm = 0, sms = 0;
-  const void* kfn = (precond == 3) ? (const void*)k_bicgstab<false, true> : (const void*)k_bicgstab<TRANS, false>;
+  const void* kfn = (precond == 3) ? (const void*)k_bicgstab<TRANS, true> : (const void*)k_bicgstab<TRANS, false>;
   int rc = sm_count_and_blocks(kfn, &per_sm, &sms);
   if (rc) return rc;
   if (per_sm < 1) {
@@ -951,7 +973,7 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
   CPFEM_REQUIRE(((uintptr_t)workspace & 255) == 0, "workspace must be 256-byte aligned");
   CPFEM_REQUIRE(opts->precond >= 0 && opts->precond <= 3, "precond must be 0, 1, 2 or 3");
   if (opts->precond == 3) {
-    CPFEM_REQUIRE(!opts->transpose, "the multigrid preconditioner solves A x = b only");
+    CPFEM_REQUIRE(!opts->transpose || sell->tpos != nullptr, "a transposed multigrid solve needs tpos");
     const int rc = mg_check(opts->mg, sell);
     if (rc != CPFEM_OK) return rc;
   }
@@ -962,7 +984,7 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
   cudaStream_t s = (cudaStream_t)stream;
   if (opts->transpose)
     return run_bicgstab<true>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                              info, s, opts->max_restarts, nullptr, opts->grid_blocks);
+                              info, s, opts->max_restarts, opts->mg, opts->grid_blocks);
   return run_bicgstab<false>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
                              info, s, opts->max_restarts, opts->mg, opts->grid_blocks);
 }

@@ -52,8 +52,7 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
                             float(tol), float(atol), None, int(grid_blocks), 0)
     if int(precond) == 3:
-        if A.transposed:
-            raise ValueError("the multigrid preconditioner solves A x = b only (no transposed solve)")
+        # the same hierarchy serves A^T (coarse operators (P^T A P)^T, transposed smoother)
         opts.mg = ctypes.pointer(problem.mg_setup(A.values, **(mg_options or {})))
     with problem.region("bicgstab"):
         _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b.contiguous()), _dev_ptr(x),

@@ -169,3 +169,20 @@ def test_golden_case4_with_multigrid(pkg, gpu):
         params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
     rel = np.abs((np.array(out) - gold["case4_szz"][:20]) / gold["case4_szz"][:20])
     assert rel.max() < 1e-5, rel
+
+
+def test_transposed_multigrid_solve(pkg, gpu):
+    """The adjoint's transposed system A^T mu = f with the same hierarchy: against the
+    Jacobi-preconditioned transposed solve."""
+    problem_mod, solver_mod = gpu
+    _, _, _, _, _, prob, u = _plastic_case(pkg, problem_mod, n=16)
+    res, A = solver_mod.newton_update_helper(prob, u)
+    f = torch.randn_like(res)
+    f[prob.fes[0].bc_dofs.long()] = 0.0
+    x0 = torch.zeros_like(res)
+    xj, kj, okj = solver_mod.bicgstab(prob, A.T, f, x0, precond=1)
+    xm, km, okm = solver_mod.bicgstab(prob, A.T, f, x0, precond=3)
+    assert okj and okm and 0 < km < kj / 4, (kj, km)
+    assert float((xm - xj).abs().max() / xj.abs().max()) < 1e-8
+    r = A.T.matvec(xm) - f
+    assert float(r.norm()) <= 1e-9 * max(float(f.norm()), 1.0)
