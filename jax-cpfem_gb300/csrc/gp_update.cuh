@@ -93,11 +93,15 @@ CPFEM_HD void cp_residual(const MatDev& m, const Cub& cc, const double* Ct, cons
 }
 
 // J = dr/ds = I + sum_a kk_a (C : sym(M^T d_a (x) n_a)) (x) pv_a
+//           = I + C : Q,   Q = sum_a sym(M^T d_a (x) n_a) (x) (kk_a pv_a)
+// (C is linear, so it is applied once to the six columns of Q instead of once per slip
+// system).
 template <int NS>
 CPFEM_HD void cp_jacobian(const MatDev& m, const Cub& cc, const double* kk, const double* M,
                                             double* J) {
+  double* Q = J;   // Q accumulates in J, then J = I + C : Q column by column in place
 #pragma unroll
-  for (int i = 0; i < 36; ++i) J[i] = (i % 7 == 0) ? 1.0 : 0.0;
+  for (int i = 0; i < 36; ++i) Q[i] = 0.0;
 #pragma unroll
   for (int a = 0; a < NS; ++a) {
     const double* d = m.d[a];
@@ -112,14 +116,22 @@ CPFEM_HD void cp_jacobian(const MatDev& m, const Cub& cc, const double* kk, cons
     q[3] = 0.5 * fma(w[1], n[2], w[2] * n[1]);
     q[4] = 0.5 * fma(w[0], n[2], w[2] * n[0]);
     q[5] = 0.5 * fma(w[0], n[1], w[1] * n[0]);
-    double t[6];
-    cubic_apply(cc, q, t);
+    double c[6];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      const double ti = kk[a] * t[i];
+    for (int j = 0; j < 6; ++j) c[j] = kk[a] * m.pv[a][j];
 #pragma unroll
-      for (int j = 0; j < 6; ++j) J[6 * i + j] = fma(ti, m.pv[a][j], J[6 * i + j]);
-    }
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) Q[6 * i + j] = fma(q[i], c[j], Q[6 * i + j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double col[6], t[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) col[i] = Q[6 * i + j];
+    cubic_apply(cc, col, t);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) J[6 * i + j] = (i == j ? 1.0 : 0.0) + t[i];
   }
 }
 

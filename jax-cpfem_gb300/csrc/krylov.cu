@@ -1102,7 +1102,7 @@ __device__ __forceinline__ bool team_reduce(double (&v)[NV], double* partials, i
   return ok;
 }
 
-__global__ void __launch_bounds__(kPThreads, 3) k_bicgstab_ragged(
+__global__ void __launch_bounds__(kPThreads, 4) k_bicgstab_ragged(
     const cpfem_sell_t L, const double* __restrict__ vals, const double* __restrict__ b, double* __restrict__ x,
     RWork w, int precond, double tol, double atol, int maxiter, int n_jobs) {
   __shared__ double smem[4 * 32];
