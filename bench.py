@@ -248,11 +248,13 @@ def krylov_iteration_cost(prob, precond=1):
 def gp_flops_per_eval(num_slip, iters_mean, tangent=True):
     """Algorithmic FP64 flops of one GP update (FMA = 2; pow, div, sqrt = 1 each):
     per local iteration one residual (tau 12N, power/slip 6N, L_p 18N, 3x3 products and
-    strain 130) + one 6x6 Jacobian (N*(18+12+12+72)) + LU/solve (~230); the tangent adds
-    a Jacobian + LU, 6 dP/ds directions (20N+220 each) and 9 columns (~220 each)."""
+    strain 130) + one 6x6 Jacobian (per slip M^T d 18, sym(. (x) n) 15, kk pv 6, rank-one
+    update 72; the cubic stiffness once on six columns, ~100) + LU/solve (~230); the
+    tangent adds a Jacobian + LU, 6 dP/ds directions (20N+220 each) and 9 columns (~220
+    each)."""
     N = num_slip
     residual = 36 * N + 130
-    jac = 114 * N
+    jac = 111 * N + 100
     lu = 230
     per_iter = residual + jac + lu
     setup = 120 + residual
