@@ -644,14 +644,15 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         for (int i = 0; i < 3; ++i) w.shat[3 * a + i] = sh[i];
       }
     }
-    ok = grid_reduce<1>(vs, parts(), w.sync, gen, smem, bcast) && ok;
-    if constexpr (MG) {
+    if constexpr (!MG) {
+      ok = grid_reduce<1>(vs, parts(), w.sync, gen, smem, bcast) && ok;   // also the shat halo barrier
+    } else {
+      // the V-cycle starts on this thread's own s; s.s joins the t reduction below
       mg_vcycle<TRANS>(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
       ok = grid_barrier(w.sync, gen) && ok;
     }
-    const bool early = vs[0] < atol2;
     // t = A shat ; omega = (t.s)/(t.t)
-    double vt[2] = {0.0, 0.0};
+    double vt[3] = {0.0, 0.0, MG ? vs[0] : 0.0};
     for (int64_t a = t0; a < n; a += stride) {
       double acc[3];
       sell_rows<TRANS, true>(L, vals, w.shat, a, acc);
@@ -663,7 +664,16 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         vt[1] = fma(acc[i], acc[i], vt[1]);
       }
     }
-    ok = grid_reduce<2>(vt, parts(), w.sync, gen, smem, bcast) && ok;
+    if constexpr (MG) {
+      ok = grid_reduce<3>(vt, parts(), w.sync, gen, smem, bcast) && ok;
+      vs[0] = vt[2];
+    } else {
+      double vt2[2] = {vt[0], vt[1]};
+      ok = grid_reduce<2>(vt2, parts(), w.sync, gen, smem, bcast) && ok;
+      vt[0] = vt2[0];
+      vt[1] = vt2[1];
+    }
+    const bool early = vs[0] < atol2;
     omega = vt[0] / vt[1];
     // x and r update
     double vr[2] = {0.0, 0.0};
