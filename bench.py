@@ -223,26 +223,32 @@ def krylov_iteration_cost(prob, precond=1):
     value per SpMV plus ~30 per dof (updates, Jacobi, six dot products).  With the
     multigrid preconditioner, two V-cycles: per level (pre_sweeps - 1) + residual +
     post_sweeps (coarsest: coarse_sweeps - 1) SpMVs with block-Jacobi applies (18 flops
-    per node each), plus restriction (27 x 3 FMAs per coarse node) and prolongation."""
+    per node each), plus restriction (27 x 3 FMAs per coarse node) and prolongation.
+    Returns (bytes, FP64 flops, FP32 flops): an FP32 V-cycle moves 4-byte values and
+    vectors and its flops leave the FP64 pipe."""
     nnz, nb, ndof = prob.nnz, prob.num_blocks, prob.num_total_dofs_all_vars
     spmv = 8 * nnz + 4 * nb + 16 * ndof
-    bytes_it, flops_it = 2 * spmv + 21 * 8 * ndof, 4.0 * nnz + 30.0 * ndof
+    bytes_it, flops_it, flops32_it = 2 * spmv + 21 * 8 * ndof, 4.0 * nnz + 30.0 * ndof, 0.0
     if precond == 3 and getattr(prob, "mg_layouts", None):
         mg = prob._mg
+        w = 4.0 if mg.precision == 1 else 8.0
         L = len(prob.mg_layouts)
         for l, (rowptr, _, _, _) in enumerate(prob.mg_layouts):
             n = rowptr.size - 1
             blocks = int(rowptr[-1])
             ops = (mg.coarse_sweeps - 1) if l == L - 1 else (mg.pre_sweeps - 1 + 1 + mg.post_sweeps)
             lf = ops * (18.0 * blocks + 18.0 * n) + 18.0 * n
-            lb = ops * (72.0 * blocks + 4.0 * blocks + 48.0 * n) + 48.0 * n
+            lb = ops * (9 * w * blocks + 4.0 * blocks + 6 * w * n) + 6 * w * n
             if l + 1 < L:
                 nc = prob.mg_layouts[l + 1][0].size - 1
                 lf += 2 * 27 * 3 * nc + 2 * 8 * 3 * n
-                lb += 8 * 3 * (n + nc) * 2
-            flops_it += 2 * lf
+                lb += w * 3 * (n + nc) * 2
+            if mg.precision == 1:
+                flops32_it += 2 * lf
+            else:
+                flops_it += 2 * lf
             bytes_it += 2 * lb
-    return bytes_it, flops_it
+    return bytes_it, flops_it, flops32_it
 
 
 def gp_flops_per_eval(num_slip, iters_mean, tangent=True):
@@ -657,7 +663,8 @@ def main():
     gp_flops = G * gp_flops_per_eval(prob.num_slip, its_t)
     kr_n, kr_ms = regions.get("bicgstab", (0, 0.0))
     kr_its = sum(max(k, 0) for k in krylov)
-    kb, kf = krylov_iteration_cost(prob, args.precond)
+    kb, kf, kf32 = krylov_iteration_cost(prob, args.precond)
+    mg_fp32 = args.precond == 3 and getattr(prob, "_mg", None) is not None and prob._mg.precision == 1
     kr_roof = None
     if kr_n and kr_ms > 0:
         tflops = kf * kr_its / (kr_ms * 1e-3) / 1e12
@@ -668,11 +675,13 @@ def main():
                                else None),
                    "traffic_note": "DRAM bytes per launch (ncu); algorithmic bytes per launch = "
                                    "algorithmic_bytes_per_iteration x iterations, served from L2",
-                   "kernel": ("k_bicgstab<0,1> (persistent multigrid-preconditioned BiCGSTAB, one launch per "
-                              "linear solve)" if args.precond == 3 else
+                   "kernel": ("k_bicgstab<0,%d> (persistent multigrid-preconditioned BiCGSTAB, %s V-cycle, one "
+                              "launch per linear solve)" % ((2, "FP32") if mg_fp32 else (1, "FP64"))
+                              if args.precond == 3 else
                               "k_bicgstab<0,0> (persistent BiCGSTAB, one launch per linear solve)"),
                    "launches": kr_n, "us_per_iteration": kr_ms * 1e3 / max(kr_its, 1),
                    "algorithmic_bytes_per_iteration": kb, "flops_per_iteration": kf,
+                   "fp32_flops_per_iteration": kf32,
                    "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm if hbm else None},
                    "peak_source": "cpfem_probe_dfma FP64 (of measured); HBM from MEASURED_PEAKS.json (of measured)"}
     spmv_roof = {"bound": "fp64", "achieved": spmv_flops / t_spmv / 1e12, "peak": fp64, "unit": "TFLOP/s",

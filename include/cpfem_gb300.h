@@ -344,8 +344,27 @@ typedef struct {
                                                  the x-coarsened and xy-coarsened operators, each
                                                  [243*scratch_nodes] */
   int64_t scratch_nodes;                      /* >= max over l of dims_c[0]*dims[l][1]*dims[l][2] */
+  int32_t precision;       /* 0: the V-cycle in FP64 on the arrays above; 1: in FP32 on the
+                              arrays below (set up from the FP64 operators).  The Krylov
+                              iteration stays FP64 either way: with the preconditioner on
+                              the right, q = A phat and t = A shat are FP64 products of the
+                              actual phat / shat, so r stays the residual of the FP64 system
+                              and the stop rule is unchanged; only the iterates differ. */
+  int32_t local_nodes;     /* levels >= 2 with at most this many nodes run inside one block
+                              (0: 256) */
+  float* values32[CPFEM_MG_MAX_LEVELS];       /* precision 1: every level's operator in FP32,
+                                                 level 0 a copy of the system (setup) */
+  float* minv32[CPFEM_MG_MAX_LEVELS];         /* precision 1: [9*nodes] */
+  float* x32[CPFEM_MG_MAX_LEVELS];            /* precision 1: [3*nodes] work vectors */
+  float* t32[CPFEM_MG_MAX_LEVELS];
+  float* r32[CPFEM_MG_MAX_LEVELS];            /* levels < num_levels-1 */
+  float* b32[CPFEM_MG_MAX_LEVELS];            /* levels >= 1 */
 } cpfem_mg_t;
 
+/* Host: sizeof of this header's structs as compiled into the library (0 material, 1 gp
+ * args, 2 vjp args, 3 sell, 4 mg hierarchy, 5 krylov opts; 0 for any other value), so a
+ * binding can check its own mirror of each layout. */
+size_t cpfem_struct_size(int32_t which);
 /* Host: the slot table of one level from its node-block CSR pattern (rows sorted, as
  * cpfem_pattern_build makes them); CPFEM_ERR_ARG if a neighbour is not within one node
  * in every direction (not a structured box). */

@@ -123,6 +123,14 @@ class MGHierarchy(ctypes.Structure):
         ("free_dof", ctypes.c_void_p),
         ("scratch", ctypes.c_void_p * 2),
         ("scratch_nodes", ctypes.c_int64),
+        ("precision", ctypes.c_int32),
+        ("local_nodes", ctypes.c_int32),
+        ("values32", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("minv32", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("x32", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("t32", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("r32", ctypes.c_void_p * MG_MAX_LEVELS),
+        ("b32", ctypes.c_void_p * MG_MAX_LEVELS),
     ]
 
 
@@ -174,12 +182,16 @@ SIGNATURES = {
     "cpfem_bicgstab_noalloc": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P]),
     "cpfem_bicgstab_last_stats": (ctypes.c_int, [_P]),
     "cpfem_mg_slot_table": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
+    "cpfem_struct_size": (ctypes.c_size_t, [_I32]),
     "cpfem_mg_setup": (ctypes.c_int, [ctypes.POINTER(MGHierarchy), _P, _P]),
     "cpfem_bicgstab_ex": (ctypes.c_int, [_SP, _P, _P, _P, ctypes.POINTER(KrylovOpts), _P, _P, _P]),
     "cpfem_bicgstab_batched_workspace_bytes": (ctypes.c_size_t, [_I32]),
     "cpfem_bicgstab_batched": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _D, _D, _I32, _I32, _P, _I32, _P, _P, _P, _P, _P]),
     "cpfem_probe_dfma": (ctypes.c_int, [_I64, _I32, _P, _P, _P]),
 }
+
+# the order of cpfem_struct_size's argument
+STRUCTS = (Material, GPArgs, VjpArgs, Sell, MGHierarchy, KrylovOpts)
 
 _lib = None
 
@@ -199,6 +211,10 @@ def load():
         fn.argtypes = args
     if lib.cpfem_abi_version() != 1:
         raise ImportError("libcpfem_gb300.so ABI version mismatch")
+    for which, st in enumerate(STRUCTS):
+        if lib.cpfem_struct_size(which) != ctypes.sizeof(st):
+            raise ImportError(f"libcpfem_gb300.so: {st.__name__} is {ctypes.sizeof(st)} bytes here but "
+                              f"{lib.cpfem_struct_size(which)} in the library (stale build?)")
     _lib = lib
     return lib
 

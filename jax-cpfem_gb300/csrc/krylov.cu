@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #include <string>
 
@@ -74,38 +75,42 @@ static size_t carve(void* base, int64_t n_nodes, KWork* w) {
   return off;
 }
 
-// Three rows of node a of A x (or A^T x).  COHERENT selects L2 loads for x, needed when
-// x was written by other blocks earlier in the same launch.
-template <bool TRANS, bool COHERENT>
-__device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const double* __restrict__ vals,
-                                          const double* x, int64_t a, double* acc) {
+__device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Three rows of node a of A x (or A^T x), in the precision R of the values and x (FP64 for
+// the Krylov iteration, FP32 inside a single-precision V-cycle).  COHERENT selects L2
+// loads for x, needed when x was written by other blocks earlier in the same launch.
+template <bool TRANS, bool COHERENT, typename R>
+__device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const R* __restrict__ vals,
+                                          const R* x, int64_t a, R* acc) {
   const int64_t g = a >> 5;
   const int lane = (int)(a & 31);
   const int64_t c0 = L.group_off[g] + lane;
-  const double* v0 = vals + 9 * L.group_off[g] + lane;
+  const R* v0 = vals + 9 * L.group_off[g] + lane;
   const int w = L.group_width[g];
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  R a0 = R(0), a1 = R(0), a2 = R(0);
 #pragma unroll 3
   for (int j = 0; j < w; ++j) {
     const int64_t b = __ldg(&L.cols[c0 + 32 * j]);
-    double x0, x1, x2;
+    R x0, x1, x2;
     if (COHERENT) {
       x0 = __ldcg(&x[3 * b]); x1 = __ldcg(&x[3 * b + 1]); x2 = __ldcg(&x[3 * b + 2]);
     } else {
       x0 = __ldg(&x[3 * b]); x1 = __ldg(&x[3 * b + 1]); x2 = __ldg(&x[3 * b + 2]);
     }
     if (!TRANS) {
-      const double* vj = v0 + 288 * j;
-      a0 = fma(__ldg(&vj[0]), x0, fma(__ldg(&vj[32]), x1, fma(__ldg(&vj[64]), x2, a0)));
-      a1 = fma(__ldg(&vj[96]), x0, fma(__ldg(&vj[128]), x1, fma(__ldg(&vj[160]), x2, a1)));
-      a2 = fma(__ldg(&vj[192]), x0, fma(__ldg(&vj[224]), x1, fma(__ldg(&vj[256]), x2, a2)));
+      const R* vj = v0 + 288 * j;
+      a0 = mad(__ldg(&vj[0]), x0, mad(__ldg(&vj[32]), x1, mad(__ldg(&vj[64]), x2, a0)));
+      a1 = mad(__ldg(&vj[96]), x0, mad(__ldg(&vj[128]), x1, mad(__ldg(&vj[160]), x2, a1)));
+      a2 = mad(__ldg(&vj[192]), x0, mad(__ldg(&vj[224]), x1, mad(__ldg(&vj[256]), x2, a2)));
     } else {
       // A^T[3a+i][3b+k] = A[3b+k][3a+i]: node b, slot tpos, row k, column i
       const int64_t tp = __ldg(&L.tpos[c0 + 32 * j]);
-      const double* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
-      a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[96]), x1, fma(__ldg(&vb[192]), x2, a0)));
-      a1 = fma(__ldg(&vb[32]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[224]), x2, a1)));
-      a2 = fma(__ldg(&vb[64]), x0, fma(__ldg(&vb[160]), x1, fma(__ldg(&vb[256]), x2, a2)));
+      const R* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
+      a0 = mad(__ldg(&vb[0]), x0, mad(__ldg(&vb[96]), x1, mad(__ldg(&vb[192]), x2, a0)));
+      a1 = mad(__ldg(&vb[32]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[224]), x2, a1)));
+      a2 = mad(__ldg(&vb[64]), x0, mad(__ldg(&vb[160]), x1, mad(__ldg(&vb[256]), x2, a2)));
     }
   }
   acc[0] = a0;
@@ -254,58 +259,58 @@ __device__ __forceinline__ void mg_xyz(int64_t a, const int32_t* dims, int& x, i
 
 // z = D^-1 v with the stored inverse diagonal block; TRANS uses its transpose, which is
 // the inverse of the diagonal block of A^T.
-template <bool TRANS = false>
-__device__ __forceinline__ void mg_apply_minv(const double* __restrict__ minv, int64_t a, const double* v,
-                                              double* out) {
-  const double* bi = minv + 9 * a;
+template <bool TRANS, typename R>
+__device__ __forceinline__ void mg_apply_minv(const R* __restrict__ minv, int64_t a, const R* v, R* out) {
+  const R* bi = minv + 9 * a;
   if (TRANS) {
 #pragma unroll
-    for (int i = 0; i < 3; ++i) out[i] = fma(bi[i], v[0], fma(bi[3 + i], v[1], bi[6 + i] * v[2]));
+    for (int i = 0; i < 3; ++i) out[i] = mad(bi[i], v[0], mad(bi[3 + i], v[1], bi[6 + i] * v[2]));
   } else {
 #pragma unroll
-    for (int i = 0; i < 3; ++i) out[i] = fma(bi[3 * i], v[0], fma(bi[3 * i + 1], v[1], bi[3 * i + 2] * v[2]));
+    for (int i = 0; i < 3; ++i) out[i] = mad(bi[3 * i], v[0], mad(bi[3 * i + 1], v[1], bi[3 * i + 2] * v[2]));
   }
 }
 
-// One damped block-Jacobi sweep at node a: T = X + omega Minv (B - A X) (A^T when TRANS).
-template <bool TRANS>
-__device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const double* V, const double* minv,
-                                         const double* B, const double* X, double* T, double omega, int64_t a) {
-  double acc[3], r[3], z[3];
+// One damped block-Jacobi sweep at node a of level 0: T = X + omega Minv (B - A X) (A^T
+// when TRANS); B is the Krylov vector being preconditioned (FP64), the rest in precision R.
+template <bool TRANS, typename R>
+__device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const R* V, const R* minv, const double* B,
+                                         const R* X, R* T, R omega, int64_t a) {
+  R acc[3], r[3], z[3];
   sell_rows<TRANS, true>(S, V, X, a, acc);
 #pragma unroll
-  for (int i = 0; i < 3; ++i) r[i] = B[3 * a + i] - acc[i];
+  for (int i = 0; i < 3; ++i) r[i] = (R)B[3 * a + i] - acc[i];
   mg_apply_minv<TRANS>(minv, a, r, z);
 #pragma unroll
-  for (int i = 0; i < 3; ++i) T[3 * a + i] = fma(omega, z[i], __ldcg(&X[3 * a + i]));
+  for (int i = 0; i < 3; ++i) T[3 * a + i] = mad(omega, z[i], __ldcg(&X[3 * a + i]));
 }
 
 // Rows of node a of A x (A^T x when TRANS) restricted to the slots j = q (mod 4) (one
 // lane of a quad).
-template <bool TRANS>
-__device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const double* __restrict__ vals,
-                                               const double* x, int64_t a, int q, double* acc) {
+template <bool TRANS, typename R>
+__device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const R* __restrict__ vals, const R* x,
+                                               int64_t a, int q, R* acc) {
   const int64_t g = a >> 5;
   const int lane = (int)(a & 31);
   const int64_t c0 = L.group_off[g] + lane;
-  const double* v0 = vals + 9 * L.group_off[g] + lane;
+  const R* v0 = vals + 9 * L.group_off[g] + lane;
   const int w = L.group_width[g];
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  R a0 = R(0), a1 = R(0), a2 = R(0);
 #pragma unroll 2
   for (int j = q; j < w; j += 4) {
     const int64_t b = __ldg(&L.cols[c0 + 32 * j]);
-    const double x0 = __ldcg(&x[3 * b]), x1 = __ldcg(&x[3 * b + 1]), x2 = __ldcg(&x[3 * b + 2]);
+    const R x0 = __ldcg(&x[3 * b]), x1 = __ldcg(&x[3 * b + 1]), x2 = __ldcg(&x[3 * b + 2]);
     if (!TRANS) {
-      const double* vb = v0 + 288 * j;
-      a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[32]), x1, fma(__ldg(&vb[64]), x2, a0)));
-      a1 = fma(__ldg(&vb[96]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[160]), x2, a1)));
-      a2 = fma(__ldg(&vb[192]), x0, fma(__ldg(&vb[224]), x1, fma(__ldg(&vb[256]), x2, a2)));
+      const R* vb = v0 + 288 * j;
+      a0 = mad(__ldg(&vb[0]), x0, mad(__ldg(&vb[32]), x1, mad(__ldg(&vb[64]), x2, a0)));
+      a1 = mad(__ldg(&vb[96]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[160]), x2, a1)));
+      a2 = mad(__ldg(&vb[192]), x0, mad(__ldg(&vb[224]), x1, mad(__ldg(&vb[256]), x2, a2)));
     } else {
       const int64_t tp = __ldg(&L.tpos[c0 + 32 * j]);
-      const double* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
-      a0 = fma(__ldg(&vb[0]), x0, fma(__ldg(&vb[96]), x1, fma(__ldg(&vb[192]), x2, a0)));
-      a1 = fma(__ldg(&vb[32]), x0, fma(__ldg(&vb[128]), x1, fma(__ldg(&vb[224]), x2, a1)));
-      a2 = fma(__ldg(&vb[64]), x0, fma(__ldg(&vb[160]), x1, fma(__ldg(&vb[256]), x2, a2)));
+      const R* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
+      a0 = mad(__ldg(&vb[0]), x0, mad(__ldg(&vb[96]), x1, mad(__ldg(&vb[192]), x2, a0)));
+      a1 = mad(__ldg(&vb[32]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[224]), x2, a1)));
+      a2 = mad(__ldg(&vb[64]), x0, mad(__ldg(&vb[160]), x1, mad(__ldg(&vb[256]), x2, a2)));
     }
   }
   acc[0] = a0;
@@ -313,7 +318,35 @@ __device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const doub
   acc[2] = a2;
 }
 
-__device__ __forceinline__ void quad_sum3(double* v) {
+// The arrays of a V-cycle in precision R: FP64 uses the hierarchy's own operators (level
+// 0: the system's values), FP32 the single-precision copies cpfem_mg_setup makes.
+template <typename R>
+struct MgArrays;
+template <>
+struct MgArrays<double> {
+  const cpfem_mg_t& m;
+  const double* v0;
+  __device__ __forceinline__ const double* values(int l) const { return l == 0 ? v0 : m.values[l]; }
+  __device__ __forceinline__ const double* minv(int l) const { return m.minv[l]; }
+  __device__ __forceinline__ double* x(int l) const { return m.x[l]; }
+  __device__ __forceinline__ double* t(int l) const { return m.t[l]; }
+  __device__ __forceinline__ double* r(int l) const { return m.r[l]; }
+  __device__ __forceinline__ double* b(int l) const { return m.b[l]; }
+};
+template <>
+struct MgArrays<float> {
+  const cpfem_mg_t& m;
+  const double* v0;
+  __device__ __forceinline__ const float* values(int l) const { return m.values32[l]; }
+  __device__ __forceinline__ const float* minv(int l) const { return m.minv32[l]; }
+  __device__ __forceinline__ float* x(int l) const { return m.x32[l]; }
+  __device__ __forceinline__ float* t(int l) const { return m.t32[l]; }
+  __device__ __forceinline__ float* r(int l) const { return m.r32[l]; }
+  __device__ __forceinline__ float* b(int l) const { return m.b32[l]; }
+};
+
+template <typename R>
+__device__ __forceinline__ void quad_sum3(R* v) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     v[i] += __shfl_xor_sync(0xffffffffu, v[i], 1);
@@ -325,56 +358,61 @@ __device__ __forceinline__ void quad_sum3(double* v) {
 // nodes a = tq, tq + sq, ... (tq = this lane's quad, sq = the quads taking part; a warp
 // holds 8 consecutive quads and runs the padded loops in lockstep, so the shuffles always
 // see the whole warp); lane 0 of a node's quad owns its writes.
-template <bool TRANS>
-__device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, int l, double* X, int64_t tq, int64_t sq,
-                                                int q) {
+template <bool TRANS, typename R>
+__device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, const MgArrays<R>& A, int l, R* X, int64_t tq,
+                                                int64_t sq, int q) {
   if (q != 0) return;
-  const double* B = mg.b[l];
+  const R* B = A.b(l);
+  const R* Mi = A.minv(l);
+  const R om = (R)mg.omega;
   for (int64_t a = tq; a < mg.sell[l].num_nodes; a += sq) {
-    double v[3] = {B[3 * a], B[3 * a + 1], B[3 * a + 2]}, z[3];
-    mg_apply_minv<TRANS>(mg.minv[l], a, v, z);
+    R v[3] = {B[3 * a], B[3 * a + 1], B[3 * a + 2]}, z[3];
+    mg_apply_minv<TRANS>(Mi, a, v, z);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) X[3 * a + i] = mg.omega * z[i];
+    for (int i = 0; i < 3; ++i) X[3 * a + i] = om * z[i];
   }
 }
 
-// T = X + omega Minv (B - A X)  (residual = false)  or  R = B - A X  (residual = true)
-template <bool TRANS>
-__device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, int l, const double* X, double* T, bool residual,
-                                          int64_t tq, int64_t sq, int q) {
+// T = X + omega Minv (B - A X)  (residual = false)  or  T = B - A X  (residual = true)
+template <bool TRANS, typename R>
+__device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, const MgArrays<R>& A, int l, const R* X, R* T,
+                                          bool residual, int64_t tq, int64_t sq, int q) {
   const cpfem_sell_t& S = mg.sell[l];
-  const double* B = mg.b[l];
+  const R* B = A.b(l);
+  const R* V = A.values(l);
+  const R om = (R)mg.omega;
   const int64_t n = S.num_nodes, npad = (n + 7) / 8 * 8;
   for (int64_t a = tq; a < npad; a += sq) {
-    double acc[3] = {0.0, 0.0, 0.0};
-    if (a < n) sell_rows_quad<TRANS>(S, mg.values[l], X, a, q, acc);
+    R acc[3] = {R(0), R(0), R(0)};
+    if (a < n) sell_rows_quad<TRANS>(S, V, X, a, q, acc);
     quad_sum3(acc);
     if (a < n && q == 0) {
-      double r[3];
+      R r[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) r[i] = B[3 * a + i] - acc[i];
       if (residual) {
 #pragma unroll
         for (int i = 0; i < 3; ++i) T[3 * a + i] = r[i];
       } else {
-        double z[3];
-        mg_apply_minv<TRANS>(mg.minv[l], a, r, z);
+        R z[3];
+        mg_apply_minv<TRANS>(A.minv(l), a, r, z);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) T[3 * a + i] = fma(mg.omega, z[i], X[3 * a + i]);
+        for (int i = 0; i < 3; ++i) T[3 * a + i] = mad(om, z[i], X[3 * a + i]);
       }
     }
   }
 }
 
-// b_{l+1} = P^T R_l: the 27 fine nodes of a coarse node split over its quad.
-__device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, int l, const double* R, int64_t tq, int64_t sq,
-                                             int q) {
+// b_{l+1} = P^T Res_l: the 27 fine nodes of a coarse node split over its quad.
+template <typename R>
+__device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, const MgArrays<R>& A, int l, const R* Res,
+                                             int64_t tq, int64_t sq, int q) {
   const int32_t* df = mg.dims[l];
   const int32_t* dc = mg.dims[l + 1];
-  double* Bc = mg.b[l + 1];
+  R* Bc = A.b(l + 1);
   const int64_t nc = mg.sell[l + 1].num_nodes, ncpad = (nc + 7) / 8 * 8;
   for (int64_t I = tq; I < ncpad; I += sq) {
-    double acc[3] = {0.0, 0.0, 0.0};
+    R acc[3] = {R(0), R(0), R(0)};
     if (I < nc) {
       int cx, cy, cz;
       mg_xyz(I, dc, cx, cy, cz);
@@ -382,10 +420,10 @@ __device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, int l, const 
         const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
         const int ix = 2 * cx + dx, iy = 2 * cy + dy, iz = 2 * cz + dz;
         if (ix < 0 || ix >= df[0] || iy < 0 || iy >= df[1] || iz < 0 || iz >= df[2]) continue;
-        const double w = (dx ? 0.5 : 1.0) * (dy ? 0.5 : 1.0) * (dz ? 0.5 : 1.0);
+        const R w = (dx ? R(0.5) : R(1)) * (dy ? R(0.5) : R(1)) * (dz ? R(0.5) : R(1));
         const int64_t i = ix + (int64_t)df[0] * (iy + (int64_t)df[1] * iz);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) acc[c] = fma(w, __ldcg(&R[3 * i + c]), acc[c]);
+        for (int c = 0; c < 3; ++c) acc[c] = mad(w, __ldcg(&Res[3 * i + c]), acc[c]);
       }
     }
     quad_sum3(acc);
@@ -397,7 +435,8 @@ __device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, int l, const 
 
 // X_l += P X_{l+1} at the nodes a = first, first + step, ... (masked on Dirichlet dofs of
 // level 0).
-__device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, double* X, const double* Xc, int64_t first,
+template <typename R>
+__device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, R* X, const R* Xc, int64_t first,
                                            int64_t step) {
   const int32_t* df = mg.dims[l];
   const int32_t* dc = mg.dims[l + 1];
@@ -406,14 +445,14 @@ __device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, double* 
     mg_xyz(a, df, ix, iy, iz);
     const int cx0 = ix >> 1, cy0 = iy >> 1, cz0 = iz >> 1;
     const int nxc = (ix & 1) + 1, nyc = (iy & 1) + 1, nzc = (iz & 1) + 1;
-    const double w = ((ix & 1) ? 0.5 : 1.0) * ((iy & 1) ? 0.5 : 1.0) * ((iz & 1) ? 0.5 : 1.0);
-    double acc[3] = {0.0, 0.0, 0.0};
+    const R w = ((ix & 1) ? R(0.5) : R(1)) * ((iy & 1) ? R(0.5) : R(1)) * ((iz & 1) ? R(0.5) : R(1));
+    R acc[3] = {R(0), R(0), R(0)};
     for (int kz = 0; kz < nzc; ++kz)
       for (int ky = 0; ky < nyc; ++ky)
         for (int kx = 0; kx < nxc; ++kx) {
           const int64_t I = (cx0 + kx) + (int64_t)dc[0] * ((cy0 + ky) + (int64_t)dc[1] * (cz0 + kz));
 #pragma unroll
-          for (int c = 0; c < 3; ++c) acc[c] = fma(w, __ldcg(&Xc[3 * I + c]), acc[c]);
+          for (int c = 0; c < 3; ++c) acc[c] = mad(w, __ldcg(&Xc[3 * I + c]), acc[c]);
         }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -423,25 +462,28 @@ __device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, double* 
   }
 }
 
-constexpr int64_t kMgLocalNodes = 256;   // levels this small run inside block 0
+constexpr int64_t kMgLocalNodes = 256;   // default: levels this small run inside block 0
 
-// One V-cycle out = M^-1 in over every block of the cooperative launch.  Level 0 uses the
-// caller's one-thread-per-node grid-stride mapping (so input written by this thread needs
-// no barrier); coarser levels give every node a quad of lanes, so their few nodes still
-// hide load latency.  The levels with at most kMgLocalNodes nodes run inside block 0 with
-// block barriers while the other blocks wait at the next grid barrier.  Which of x / t
-// holds a level's iterate follows from the sweep counts alone, so every block knows it.
-// Returns with out complete for this thread's own nodes.
-template <bool TRANS>
+// One V-cycle out = M^-1 in over every block of the cooperative launch, in precision R
+// (in and out are the FP64 Krylov vectors).  Level 0 uses the caller's one-thread-per-node
+// grid-stride mapping (so input written by this thread needs no barrier); coarser levels
+// give every node a quad of lanes, so their few nodes still hide load latency.  The levels
+// (from level 2 on) with at most local_nodes nodes run inside block 0 with block barriers
+// while the other blocks wait at the next grid barrier.  Which of x / t holds a level's
+// iterate follows from the sweep counts alone, so every block knows it.  Returns with out
+// complete for this thread's own nodes.
+template <bool TRANS, typename R>
 __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0, const double* in, double* out,
                           int64_t t0, int64_t stride, GridSync* gs, unsigned int& gen, bool& ok) {
+  const MgArrays<R> A{mg, vals0};
   const int L = mg.num_levels;
-  const double om = mg.omega;
+  const R om = (R)mg.omega;
   const int64_t tq = t0 >> 2, sq = stride >> 2;
   const int q = (int)(t0 & 3);
   const int64_t tqb = threadIdx.x >> 2, sqb = blockDim.x >> 2;   // block-local quads
+  const int64_t local_nodes = mg.local_nodes > 0 ? (int64_t)mg.local_nodes : kMgLocalNodes;
   int lb = L;                                                    // first block-local level
-  for (int l = L - 1; l >= 2 && mg.sell[l].num_nodes <= kMgLocalNodes; --l) lb = l;
+  for (int l = L - 1; l >= 2 && mg.sell[l].num_nodes <= local_nodes; --l) lb = l;
   // where each level's iterate lives after its down sweeps / after its up sweeps
   bool down_t[CPFEM_MG_MAX_LEVELS], up_t[CPFEM_MG_MAX_LEVELS];
   for (int l = 0; l < L; ++l) {
@@ -452,78 +494,78 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
   // ---- grid-wide levels 0 .. lb-1, down
   for (int l = 0; l < lb; ++l) {
     const cpfem_sell_t& S = mg.sell[l];
-    const double* V = (l == 0) ? vals0 : mg.values[l];
-    double* X = mg.x[l];
-    double* T = mg.t[l];
+    const R* V = A.values(l);
+    R* X = A.x(l);
+    R* T = A.t(l);
     const int64_t n = S.num_nodes;
     if (l == 0) {
       for (int64_t a = t0; a < n; a += stride) {
-        double v[3] = {in[3 * a], in[3 * a + 1], in[3 * a + 2]}, z[3];
-        mg_apply_minv<TRANS>(mg.minv[0], a, v, z);
+        R v[3] = {(R)in[3 * a], (R)in[3 * a + 1], (R)in[3 * a + 2]}, z[3];
+        mg_apply_minv<TRANS>(A.minv(0), a, v, z);
 #pragma unroll
         for (int i = 0; i < 3; ++i) X[3 * a + i] = om * z[i];
       }
     } else {
-      mgq_first_sweep<TRANS>(mg, l, X, tq, sq, q);
+      mgq_first_sweep<TRANS>(mg, A, l, X, tq, sq, q);
     }
     const int nsw = (l == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
     for (int k = 1; k < nsw; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, V, mg.minv[0], in, X, T, om, a);
+        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, V, A.minv(0), in, X, T, om, a);
       } else {
-        mgq_apply<TRANS>(mg, l, X, T, false, tq, sq, q);
+        mgq_apply<TRANS>(mg, A, l, X, T, false, tq, sq, q);
       }
-      double* tmp = X; X = T; T = tmp;
+      R* tmp = X; X = T; T = tmp;
     }
     if (l == L - 1) break;
     ok = grid_barrier(gs, gen) && ok;
-    double* R = mg.r[l];
+    R* Res = A.r(l);
     if (l == 0) {
       for (int64_t a = t0; a < n; a += stride) {
-        double acc[3];
+        R acc[3];
         sell_rows<TRANS, true>(S, V, X, a, acc);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const double rv = in[3 * a + i] - acc[i];
-          R[3 * a + i] = (mg.free_dof != nullptr && mg.free_dof[3 * a + i] == 0) ? 0.0 : rv;
+          const R rv = (R)in[3 * a + i] - acc[i];
+          Res[3 * a + i] = (mg.free_dof != nullptr && mg.free_dof[3 * a + i] == 0) ? R(0) : rv;
         }
       }
     } else {
-      mgq_apply<TRANS>(mg, l, X, R, true, tq, sq, q);
+      mgq_apply<TRANS>(mg, A, l, X, Res, true, tq, sq, q);
     }
     ok = grid_barrier(gs, gen) && ok;
     if (l + 1 < lb) {
-      mgq_restrict(mg, l, R, tq, sq, q);
+      mgq_restrict(mg, A, l, Res, tq, sq, q);
     } else if (blockIdx.x == 0) {
       // ---- block-local levels lb .. L-1: down, coarsest, up to lb
-      mgq_restrict(mg, l, R, tqb, sqb, q);
+      mgq_restrict(mg, A, l, Res, tqb, sqb, q);
       for (int m = lb; m < L; ++m) {
-        double* Xm = mg.x[m];
-        double* Tm = mg.t[m];
-        mgq_first_sweep<TRANS>(mg, m, Xm, tqb, sqb, q);
+        R* Xm = A.x(m);
+        R* Tm = A.t(m);
+        mgq_first_sweep<TRANS>(mg, A, m, Xm, tqb, sqb, q);
         const int nswm = (m == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
         for (int k = 1; k < nswm; ++k) {
           __syncthreads();
-          mgq_apply<TRANS>(mg, m, Xm, Tm, false, tqb, sqb, q);
-          double* tmp = Xm; Xm = Tm; Tm = tmp;
+          mgq_apply<TRANS>(mg, A, m, Xm, Tm, false, tqb, sqb, q);
+          R* tmp = Xm; Xm = Tm; Tm = tmp;
         }
         if (m == L - 1) break;
         __syncthreads();
-        mgq_apply<TRANS>(mg, m, Xm, mg.r[m], true, tqb, sqb, q);
+        mgq_apply<TRANS>(mg, A, m, Xm, A.r(m), true, tqb, sqb, q);
         __syncthreads();
-        mgq_restrict(mg, m, mg.r[m], tqb, sqb, q);
+        mgq_restrict(mg, A, m, A.r(m), tqb, sqb, q);
       }
       for (int m = L - 2; m >= lb; --m) {
-        double* Xm = down_t[m] ? mg.t[m] : mg.x[m];
-        double* Tm = down_t[m] ? mg.x[m] : mg.t[m];
-        const double* Xc = (m + 1 == L - 1 ? down_t[m + 1] : up_t[m + 1]) ? mg.t[m + 1] : mg.x[m + 1];
+        R* Xm = down_t[m] ? A.t(m) : A.x(m);
+        R* Tm = down_t[m] ? A.x(m) : A.t(m);
+        const R* Xc = (m + 1 == L - 1 ? down_t[m + 1] : up_t[m + 1]) ? A.t(m + 1) : A.x(m + 1);
         __syncthreads();
         if (q == 0) mg_prolong(mg, m, Xm, Xc, tqb, sqb);
         for (int k = 0; k < mg.post_sweeps; ++k) {
           __syncthreads();
-          mgq_apply<TRANS>(mg, m, Xm, Tm, false, tqb, sqb, q);
-          double* tmp = Xm; Xm = Tm; Tm = tmp;
+          mgq_apply<TRANS>(mg, A, m, Xm, Tm, false, tqb, sqb, q);
+          R* tmp = Xm; Xm = Tm; Tm = tmp;
         }
       }
     }
@@ -532,34 +574,37 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
   for (int l = lb - 1; l >= 0; --l) {
     if (l == L - 1) continue;
     const cpfem_sell_t& S = mg.sell[l];
-    const double* V = (l == 0) ? vals0 : mg.values[l];
-    double* X = down_t[l] ? mg.t[l] : mg.x[l];
-    double* T = down_t[l] ? mg.x[l] : mg.t[l];
-    const double* Xc = (l + 1 == L - 1 ? down_t[l + 1] : up_t[l + 1]) ? mg.t[l + 1] : mg.x[l + 1];
+    const R* V = A.values(l);
+    R* X = down_t[l] ? A.t(l) : A.x(l);
+    R* T = down_t[l] ? A.x(l) : A.t(l);
+    const R* Xc = (l + 1 == L - 1 ? down_t[l + 1] : up_t[l + 1]) ? A.t(l + 1) : A.x(l + 1);
     ok = grid_barrier(gs, gen) && ok;
     if (l == 0) mg_prolong(mg, 0, X, Xc, t0, stride);
     else if (q == 0) mg_prolong(mg, l, X, Xc, tq, sq);
     for (int k = 0; k < mg.post_sweeps; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, V, mg.minv[0], in, X, T, om, a);
+        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, V, A.minv(0), in, X, T, om, a);
       } else {
-        mgq_apply<TRANS>(mg, l, X, T, false, tq, sq, q);
+        mgq_apply<TRANS>(mg, A, l, X, T, false, tq, sq, q);
       }
-      double* tmp = X; X = T; T = tmp;
+      R* tmp = X; X = T; T = tmp;
     }
   }
-  const double* X0 = up_t[0] ? mg.t[0] : mg.x[0];
+  const R* X0 = up_t[0] ? A.t(0) : A.x(0);
   for (int64_t a = t0; a < mg.sell[0].num_nodes; a += stride)
 #pragma unroll
-    for (int i = 0; i < 3; ++i) out[3 * a + i] = X0[3 * a + i];
+    for (int i = 0; i < 3; ++i) out[3 * a + i] = (double)X0[3 * a + i];
 }
 
-template <bool TRANS, bool MG>
+// MGP: 0 the point preconditioners of precond 0..2, 1 the FP64 V-cycle, 2 the FP32 V-cycle.
+template <bool TRANS, int MGP>
 __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
                                                         const double* __restrict__ b, double* __restrict__ x,
                                                         KWork w, int precond, double tol, double atol,
                                                         int maxiter, int max_restarts, const cpfem_mg_t mg) {
+  constexpr bool MG = MGP != 0;
+  using MgReal = typename std::conditional<MGP == 2, float, double>::type;
   __shared__ double smem[4 * 32];
   __shared__ double bcast[4];
   const int64_t n = L.num_nodes;
@@ -611,7 +656,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         for (int i = 0; i < 3; ++i) w.phat[3 * a + i] = ph[i];
       }
     }
-    if constexpr (MG) mg_vcycle<TRANS>(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok);
+    if constexpr (MG) mg_vcycle<TRANS, MgReal>(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok);
     ok = grid_barrier(w.sync, gen) && ok;
     // q = A phat ; alpha = rho_new / (rhat . q)
     double v1[1] = {0.0};
@@ -648,7 +693,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
       ok = grid_reduce<1>(vs, parts(), w.sync, gen, smem, bcast) && ok;   // also the shat halo barrier
     } else {
       // the V-cycle starts on this thread's own s; s.s joins the t reduction below
-      mg_vcycle<TRANS>(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
+      mg_vcycle<TRANS, MgReal>(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
       ok = grid_barrier(w.sync, gen) && ok;
     }
     // t = A shat ; omega = (t.s)/(t.t)
@@ -760,7 +805,9 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   memset(&mg, 0, sizeof(mg));
   if (precond == 3) mg = *mgp;
   int per_sm = 0, sms = 0;
-  const void* kfn = (precond == 3) ? (const void*)k_bicgstab<TRANS, true> : (const void*)k_bicgstab<TRANS, false>;
+  const void* kfn = (precond != 3)      ? (const void*)k_bicgstab<TRANS, 0>
+                    : (mg.precision == 1) ? (const void*)k_bicgstab<TRANS, 2>
+                                          : (const void*)k_bicgstab<TRANS, 1>;
   int rc = sm_count_and_blocks(kfn, &per_sm, &sms);
   if (rc) return rc;
   if (per_sm < 1) {
@@ -803,20 +850,26 @@ static int mg_check(const cpfem_mg_t* mg, const cpfem_sell_t* sell) {
   CPFEM_REQUIRE(mg->pre_sweeps >= 1 && mg->post_sweeps >= 0 && mg->coarse_sweeps >= 1, "bad multigrid sweep counts");
   CPFEM_REQUIRE(mg->omega > 0.0 && mg->omega < 2.0, "multigrid omega must lie in (0, 2)");
   CPFEM_REQUIRE(sell == nullptr || mg->sell[0].num_nodes == sell->num_nodes, "level 0 must be the system's layout");
+  CPFEM_REQUIRE(mg->precision == 0 || mg->precision == 1, "multigrid precision must be 0 (FP64) or 1 (FP32)");
+  CPFEM_REQUIRE(mg->local_nodes >= 0, "multigrid local_nodes must be >= 0");
+  const bool single = mg->precision == 1;
   for (int l = 0; l < L; ++l) {
     const int64_t n = (int64_t)mg->dims[l][0] * mg->dims[l][1] * mg->dims[l][2];
     CPFEM_REQUIRE(mg->dims[l][0] >= 1 && mg->dims[l][1] >= 1 && mg->dims[l][2] >= 1 && n == mg->sell[l].num_nodes,
                   "multigrid dims do not match the level's node count");
-    CPFEM_REQUIRE(sell_ok(&mg->sell[l]) && mg->minv[l] && mg->x[l] && mg->t[l], "multigrid level arrays missing");
+    CPFEM_REQUIRE(sell_ok(&mg->sell[l]) && mg->minv[l], "multigrid level arrays missing");
+    CPFEM_REQUIRE(single ? (mg->values32[l] && mg->minv32[l] && mg->x32[l] && mg->t32[l]) : (mg->x[l] && mg->t[l]),
+                  "multigrid work arrays missing");
     CPFEM_REQUIRE(mg->slot[l], "multigrid slot table missing");
     if (l + 1 < L) {
-      CPFEM_REQUIRE(mg->r[l], "multigrid residual array missing");
+      CPFEM_REQUIRE(single ? mg->r32[l] != nullptr : mg->r[l] != nullptr, "multigrid residual array missing");
       const int64_t need = (int64_t)((mg->dims[l][0] - 1) / 2 + 1) * mg->dims[l][1] * mg->dims[l][2];
       CPFEM_REQUIRE(mg->scratch[0] && mg->scratch[1] && mg->scratch_nodes >= need,
                     "multigrid scratch missing or too small");
     }
     if (l >= 1) {
-      CPFEM_REQUIRE(mg->values[l] && mg->b[l], "multigrid coarse arrays missing");
+      CPFEM_REQUIRE(mg->values[l] && (single ? mg->b32[l] != nullptr : mg->b[l] != nullptr),
+                    "multigrid coarse arrays missing");
       for (int d = 0; d < 3; ++d)
         CPFEM_REQUIRE((mg->dims[l - 1][d] - 1) % 2 == 0 && mg->dims[l][d] == (mg->dims[l - 1][d] - 1) / 2 + 1,
                       "each multigrid level must halve the cell counts of the finer one");
@@ -899,6 +952,15 @@ __global__ void __launch_bounds__(256) k_mg_rap_dir(int dir, int ix, int iy, int
   }
 }
 
+// FP32 copy of n values, or of a sliced-ELL value array (9 * group_off[num_groups] values,
+// read on the device) when slots != nullptr.
+__global__ void __launch_bounds__(256) k_to_f32(const double* __restrict__ in, float* __restrict__ out, int64_t n,
+                                                const int64_t* __restrict__ slots) {
+  const int64_t m = slots != nullptr ? 9 * slots[0] : n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
 }  // namespace cpfem
 
 using namespace cpfem;
@@ -953,6 +1015,19 @@ int cpfem_mg_setup(const cpfem_mg_t* mg, const double* values0, void* stream) {
     k_precond_setup<false><<<(unsigned)ceil_div(C.num_nodes, 128), 128, 0, s>>>(C, mg->values[l + 1], 2,
                                                                                 mg->minv[l + 1]);
     CPFEM_CUDA_TRY(cudaGetLastError());
+  }
+  if (mg->precision == 1) {
+    // the FP32 V-cycle's operators: rounded copies of the FP64 ones
+    for (int l = 0; l < mg->num_levels; ++l) {
+      const cpfem_sell_t& S = mg->sell[l];
+      k_to_f32<<<1216, 256, 0, s>>>((l == 0) ? values0 : mg->values[l], mg->values32[l], 0,
+                                    S.group_off + S.num_groups);
+      CPFEM_CUDA_TRY(cudaGetLastError());
+      const int64_t nm = 9 * (int64_t)S.num_nodes;
+      k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div(nm, 256), 1216), 256, 0, s>>>(mg->minv[l], mg->minv32[l], nm,
+                                                                                   nullptr);
+      CPFEM_CUDA_TRY(cudaGetLastError());
+    }
   }
   return CPFEM_OK;
 }

@@ -273,3 +273,15 @@ extern "C" int cpfem_mg_slot_table(int32_t num_nodes, const int32_t* dims, const
   }
   return CPFEM_OK;
 }
+
+extern "C" size_t cpfem_struct_size(int32_t which) {
+  switch (which) {
+    case 0: return sizeof(cpfem_material_t);
+    case 1: return sizeof(cpfem_gp_args_t);
+    case 2: return sizeof(cpfem_vjp_args_t);
+    case 3: return sizeof(cpfem_sell_t);
+    case 4: return sizeof(cpfem_mg_t);
+    case 5: return sizeof(cpfem_krylov_opts_t);
+    default: return 0;
+  }
+}

@@ -286,14 +286,22 @@ class CrystalPlasticity:
         sell = _capi.Sell(n, ng, *(a.data_ptr() for a in arrays))
         return rowptr, cols, goff, sell, arrays, 9 * int(slots[0])
 
-    def multigrid(self, max_levels=5, pre_sweeps=1, post_sweeps=1, coarse_sweeps=8, omega=0.45):
+    def multigrid(self, max_levels=5, pre_sweeps=1, post_sweeps=1, coarse_sweeps=8, omega=0.45, precision="fp64",
+                  local_nodes=256):
         """Geometric multigrid hierarchy of a structured box mesh for the BiCGSTAB
         preconditioner ``precond=3`` (built once; coarse operators by ``mg_setup``).
-        Levels halve the cell counts while every count stays even, up to max_levels."""
+        Levels halve the cell counts while every count stays even, up to max_levels.
+        precision="fp32" runs the V-cycle in single precision on rounded copies of the
+        operators (the Krylov iteration and its stop rule stay FP64); levels from the
+        third on with at most ``local_nodes`` nodes are smoothed inside one block."""
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("multigrid precision must be 'fp64' or 'fp32'")
         if getattr(self, "_mg", None) is not None and self._mg_key == max_levels:
             mg = self._mg   # same levels: only the smoother settings may change
             mg.pre_sweeps, mg.post_sweeps, mg.coarse_sweeps = pre_sweeps, post_sweeps, coarse_sweeps
             mg.omega = float(omega)
+            mg.local_nodes = int(local_nodes)
+            self._mg_precision(mg, precision)
             return mg
         dims = structured_dims(self.mesh.points)
         if dims is None:
@@ -352,7 +360,33 @@ class CrystalPlasticity:
         self._mg, self._mg_keep, self._mg_free, self._mg_key = mg, keep, free, max_levels
         self._mg_bc_token = None
         self.mg_levels = levels
+        mg.local_nodes = int(local_nodes)
+        self._mg_precision(mg, precision)
         return mg
+
+    def _mg_precision(self, mg, precision):
+        """Select the V-cycle precision; the FP32 arrays are made on first use (they are
+        filled by the next ``mg_setup``)."""
+        mg.precision = 1 if precision == "fp32" else 0
+        if mg.precision == 0 or mg.values32[0]:
+            return
+        keep = self._mg_keep
+
+        def buf(n):
+            t = torch.zeros(n, dtype=torch.float32, device=self.device)
+            keep.append(t)
+            return t.data_ptr()
+
+        L = mg.num_levels
+        for l, d in enumerate(self.mg_levels):
+            n = d[0] * d[1] * d[2]
+            mg.values32[l] = buf(9 * int(self.mg_layouts[l][2][-1]))
+            mg.minv32[l] = buf(9 * n)
+            mg.x32[l], mg.t32[l] = buf(3 * n), buf(3 * n)
+            if l + 1 < L:
+                mg.r32[l] = buf(3 * n)
+            if l >= 1:
+                mg.b32[l] = buf(3 * n)
 
     def mg_setup(self, values, refresh="newton", **kw):
         """Coarse operators and smoother blocks of the hierarchy for the current
@@ -366,13 +400,14 @@ class CrystalPlasticity:
             if fe.bc_dofs.numel():
                 self._mg_free[fe.bc_dofs.long()] = 0
             self._mg_bc_token = fe.bc_token
-        if refresh == "step" and getattr(self, "_mg_setup_key", None) == (fe.bc_token, self._state_token):
+        key = (fe.bc_token, self._state_token, mg.precision)
+        if refresh == "step" and getattr(self, "_mg_setup_key", None) == key:
             return mg
         if refresh not in ("newton", "step"):
             raise ValueError("mg refresh must be 'newton' or 'step'")
         with self.region("mg_setup"):
             _capi.check(self.lib.cpfem_mg_setup(ctypes.byref(mg), _dev_ptr(values), _stream()))
-        self._mg_setup_key = (fe.bc_token, self._state_token)
+        self._mg_setup_key = key
         return mg
 
     def csr_map(self):

@@ -7,7 +7,8 @@ SpMVs, fewer make each grid barrier cheaper).  ``tune_linear_solver`` times comp
 solves of a real Newton system (CUDA events on the solve's stream, after one untimed
 solve per configuration) with a coordinate search over those settings, and returns the
 fastest configuration that converged.  Every candidate solves the same system to the
-same stop rule, so the choice changes only the time, not the accuracy contract.  The
+same stop rule, so the choice changes only the time, not the accuracy contract.  The V-cycle
+may run in FP32 (the Krylov iteration stays FP64, so the stop rule is the same).  The
 damping stays at or below 0.45: block-Jacobi smoothing of these tangents diverges near
 0.7, and a tuned value must stay safe for the later, more plastic, Newton systems.
 """
@@ -18,17 +19,21 @@ import torch
 from . import solver as _solver
 
 DEFAULT = {"max_levels": 5, "pre_sweeps": 1, "post_sweeps": 1, "coarse_sweeps": 8, "omega": 0.45,
-           "grid_blocks": 0}
-SEARCH = (("omega", (0.35, 0.4, 0.45)),
+           "precision": "fp64", "local_nodes": 256, "grid_blocks": 0}
+# the keys that go to CrystalPlasticity.multigrid (grid_blocks goes to the launch)
+MG_KEYS = ("max_levels", "pre_sweeps", "post_sweeps", "coarse_sweeps", "omega", "precision", "local_nodes")
+SEARCH = (("precision", ("fp64", "fp32")),
+          ("omega", (0.35, 0.4, 0.45)),
           ("pre_sweeps", (1, 2)),
           ("post_sweeps", (0, 1, 2)),
           ("coarse_sweeps", (4, 8, 12)),
           ("max_levels", (3, 4, 5)),
+          ("local_nodes", (256, 1024)),
           ("grid_blocks", (0, 76, 104, 152, 304)))
 
 
 def _time_solve(problem, A, b, x0, cfg, reps):
-    mg = {k: cfg[k] for k in ("max_levels", "pre_sweeps", "post_sweeps", "coarse_sweeps", "omega")}
+    mg = {k: cfg[k] for k in MG_KEYS}
     _solver.bicgstab(problem, A, b, x0, precond=3, mg_options=mg, grid_blocks=cfg["grid_blocks"])
     best, its, ok = float("inf"), None, True
     for _ in range(reps):
@@ -64,5 +69,5 @@ def tune_linear_solver(problem, A, b, x0, reps=2, search=SEARCH, start=None):
             if t_ok and t_ms < best_ms:
                 best_ms, cfg = t_ms, trial
     # leave the problem's hierarchy in the chosen configuration
-    problem.multigrid(**{k: cfg[k] for k in ("max_levels", "pre_sweeps", "post_sweeps", "coarse_sweeps", "omega")})
+    problem.multigrid(**{k: cfg[k] for k in MG_KEYS})
     return cfg, table

@@ -40,6 +40,19 @@ def test_library_exports_every_declared_symbol(lib):
     assert lib.cpfem_abi_version() == 1
 
 
+def test_struct_layouts_match_the_library(lib):
+    import ctypes
+    from importlib import import_module
+    capi = import_module("jax-cpfem_gb300._capi")
+    for which, st in enumerate(capi.STRUCTS):
+        assert lib.cpfem_struct_size(which) == ctypes.sizeof(st), st.__name__
+    assert lib.cpfem_struct_size(len(capi.STRUCTS)) == 0
+    # field offsets the kernels depend on: the FP32 V-cycle arrays follow the FP64 ones
+    mg = capi.MGHierarchy
+    assert mg.precision.offset == mg.scratch_nodes.offset + 8
+    assert mg.b32.offset + 8 * capi.MG_MAX_LEVELS == ctypes.sizeof(mg)
+
+
 def _pattern(lib, cells, n_nodes):
     cells = np.ascontiguousarray(cells, dtype=np.int32)
     nb = np.zeros(1, np.int64)

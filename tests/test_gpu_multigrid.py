@@ -97,9 +97,47 @@ def test_multigrid_bicgstab_solves_the_tangent(pkg, gpu):
     assert float(r.norm()) <= 1e-10 * max(float(res.norm()), 1.0) * 10
 
 
-def test_load_steps_with_multigrid_match_oracle(pkg, gpu):
+@pytest.mark.parametrize("local_nodes", [256, 1024])
+def test_fp32_vcycle_solves_the_tangent(pkg, gpu, local_nodes):
+    """The single-precision V-cycle (local_nodes 1024 also smooths the 9^3 level inside one
+    block): the FP64 Krylov iteration still meets the FP64 stop rule, and the solution
+    agrees with the Jacobi and FP64-multigrid solves."""
+    problem_mod, solver_mod = gpu
+    _, _, _, _, _, prob, u = _plastic_case(pkg, problem_mod, n=16)
+    res, A = solver_mod.newton_update_helper(prob, u)
+    x0 = solver_mod.initial_increment(prob, u)
+    xj, kj, okj = solver_mod.bicgstab(prob, A, -res, x0, precond=1)
+    xd, kd, okd = solver_mod.bicgstab(prob, A, -res, x0, precond=3)
+    xs, ks, oks = solver_mod.bicgstab(prob, A, -res, x0, precond=3,
+                                      mg_options={"precision": "fp32", "local_nodes": local_nodes})
+    assert prob._mg.precision == 1 and prob._mg.local_nodes == local_nodes
+    assert okj and okd and oks and 0 < ks <= kd + 3, (kj, kd, ks)
+    assert float((xs - xj).abs().max() / xj.abs().max()) < 1e-8
+    r = A.matvec(xs) + res
+    assert float(r.norm()) <= 1e-10 * max(float(res.norm()), 1.0) * 10
+    # back to FP64 on the same hierarchy: the same iterates as the first FP64 solve
+    xd2, kd2, _ = solver_mod.bicgstab(prob, A, -res, x0, precond=3, mg_options={"local_nodes": 256})
+    assert kd2 == kd and torch.equal(xd2, xd)
+
+
+def test_fp32_vcycle_transposed_solve(pkg, gpu):
+    problem_mod, solver_mod = gpu
+    _, _, _, _, _, prob, u = _plastic_case(pkg, problem_mod, n=16)
+    res, A = solver_mod.newton_update_helper(prob, u)
+    f = torch.randn_like(res)
+    f[prob.fes[0].bc_dofs.long()] = 0.0
+    x0 = torch.zeros_like(res)
+    xj, kj, okj = solver_mod.bicgstab(prob, A.T, f, x0, precond=1)
+    xs, ks, oks = solver_mod.bicgstab(prob, A.T, f, x0, precond=3, mg_options={"precision": "fp32"})
+    assert okj and oks and 0 < ks < kj / 4, (kj, ks)
+    assert float((xs - xj).abs().max() / xj.abs().max()) < 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_load_steps_with_multigrid_match_oracle(pkg, gpu, precision):
     """Three tension steps of a 4^3, 4-grain polycrystal with the multigrid-preconditioned
-    linear solve: per-cell stress and u against the oracle (Jacobi BiCGSTAB)."""
+    linear solve (FP64 or FP32 V-cycle): per-cell stress and u against the oracle (Jacobi
+    BiCGSTAB)."""
     problem_mod, solver_mod = gpu
     spec = pkg.material.BENCH_STEEL
     mesh = pkg.box_mesh(4, 4, 4)
@@ -117,7 +155,8 @@ def test_load_steps_with_multigrid_match_oracle(pkg, gpu):
         bcs = bcf(float(disps[i + 1]))
         prob.fes[0].set_dirichlet_lists([b[0] for b in bcs], [b[1] for b in bcs], [b[2] for b in bcs])
         prob.set_params(params)
-        sol = solver_mod.solver(prob, {"jax_solver": {"precond": "mg"}, "tol": 1e-9, "rel_tol": 1e-12,
+        sol = solver_mod.solver(prob, {"jax_solver": {"precond": "mg", "mg_options": {"precision": precision}},
+                                       "tol": 1e-9, "rel_tol": 1e-12,
                                        "initial_guess": [sol.reshape(-1, 3)]})[0].reshape(-1)
         out.append(prob.compute_avg_stress(sol.reshape(-1, 3), params).cpu().numpy())
         params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
@@ -136,7 +175,7 @@ def test_autotuner_picks_a_converging_configuration(pkg, gpu):
     cfg, table = tuning.tune_linear_solver(prob, A, -res, x0, reps=1,
                                            search=(("omega", (0.4, 0.5)), ("grid_blocks", (0, 8))))
     assert len(table) >= 3 and set(cfg) == set(tuning.DEFAULT)
-    mg = {k: cfg[k] for k in ("max_levels", "pre_sweeps", "post_sweeps", "coarse_sweeps", "omega")}
+    mg = {k: cfg[k] for k in tuning.MG_KEYS}
     x, k, ok = solver_mod.bicgstab(prob, A, -res, x0, precond=3, mg_options=mg, grid_blocks=cfg["grid_blocks"])
     xj, kj, okj = solver_mod.bicgstab(prob, A, -res, x0, precond=1)
     assert ok and okj and float((x - xj).abs().max() / xj.abs().max()) < 1e-8
