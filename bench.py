@@ -401,8 +401,10 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
     disps = STRAIN_STEP * np.arange(nsteps + 1)
     ts = DT * np.arange(nsteps + 1)
     # forward and transposed (adjoint) solves with the same preconditioner
-    h = adjoint.LoadHistory(prob, disps, ts, bc_fn, quat, solver_options={"jax_solver": {"precond": args.precond}},
-                            adjoint_options={"precond": args.precond})
+    mg = {"precision": args.mg_precision} if args.mg_precision else None
+    h = adjoint.LoadHistory(prob, disps, ts, bc_fn, quat,
+                            solver_options={"jax_solver": {"precond": args.precond, "mg_options": mg}},
+                            adjoint_options={"precond": args.precond, "mg_options": mg})
     theta = np.array([spec.h, spec.gss_initial, spec.t_sat, spec.gss_a, spec.xm])
     euler = np.zeros((N_GRAINS, 3))
     # synthetic target: h0, g0, gs scaled by 1.1 under the same seed
@@ -422,7 +424,8 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
            "n_gpus": 1, "steps": nsteps, "warmup": 0, "dtype": "f64", "data": "synthetic",
            "config": dict(workload_config(n), workload=f"adjoint-fcc-polycrystal-{n}^3-{N_GRAINS}grains",
                           load_steps=nsteps, params="h0,g0,gs,a,m + 64x3 Euler angles",
-                          precond={1: "jacobi", 2: "block-jacobi-3x3", 3: "multigrid-vcycle"}.get(args.precond)),
+                          precond={1: "jacobi", 2: "block-jacobi-3x3", 3: "multigrid-vcycle"}.get(args.precond),
+                          mg_precision=(args.mg_precision or "fp64") if args.precond == 3 else None),
            "forward_s": t_fwd, "backward_s": t_bwd, "gradient_over_forward": (t_fwd + t_bwd) / t_fwd,
            "objective": float(((s - target) ** 2).mean()), "theta_grad": tb.tolist(),
            "euler_grad_norm": float(np.linalg.norm(eb)), "adjoint_krylov_iters": h.krylov_iters}
@@ -506,6 +509,8 @@ def main():
     ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
                     help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
     ap.add_argument("--no-tune", action="store_true", help="skip the linear-solver autotuning before warm-up ends")
+    ap.add_argument("--mg-precision", default=None, choices=["fp64", "fp32"],
+                    help="fix the V-cycle precision (default: the autotuner's choice, FP64 untuned)")
     ap.add_argument("--no-jacobi-leg", action="store_true",
                     help="skip the two extra load steps timed with the reference's Jacobi preconditioner")
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"],
@@ -561,6 +566,8 @@ def main():
     st = Stepper(pkg, prob, solver_mod, mesh)
     st.precond = args.precond
     st.mg_options = {"refresh": args.mg_refresh}
+    if args.mg_precision:
+        st.mg_options["precision"] = args.mg_precision
     clk = ClockSampler(local).start()
     time.sleep(1.0)
     # warm-up with the timers on, so every kernel the timed steps use (including torch's
@@ -577,7 +584,12 @@ def main():
             prob.set_params(st.params)
             res, A = solver_mod.newton_update_helper(prob, st.sol)
             x0 = solver_mod.initial_increment(prob, st.sol).clone()
-            cfg, table = tuning.tune_linear_solver(prob, A, -res, x0)
+            search = tuning.SEARCH
+            start = dict(tuning.DEFAULT)
+            if args.mg_precision:   # a fixed precision is not searched
+                start["precision"] = args.mg_precision
+                search = tuple(kv for kv in search if kv[0] != "precision")
+            cfg, table = tuning.tune_linear_solver(prob, A, -res, x0, search=search, start=start)
             st.grid_blocks = cfg["grid_blocks"]
             st.mg_options = dict({k: v for k, v in cfg.items() if k != "grid_blocks"}, refresh=args.mg_refresh)
             tuned = {"chosen": cfg, "candidates": len(table),

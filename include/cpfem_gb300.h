@@ -106,6 +106,12 @@ typedef struct {
                                  evaluates GP order[t].  Ordering GPs by their previous
                                  local-Newton iteration count keeps a warp's lanes busy for
                                  the same number of iterations; results are unchanged. */
+  double* s_warm;             /* [6*num_gp] or NULL: lattice-frame S (11,22,33,23,13,12) of the
+                                 GP's last converged local solve, read and written.  The
+                                 local Newton starts there instead of at S = 0 (the
+                                 reference's start), falling back to S = 0 when that start has
+                                 not converged after 8 iterations; the result is the root of
+                                 the same residual to the same tolerance.  Zeros = S = 0. */
 } cpfem_gp_args_t;
 
 /*
@@ -149,6 +155,9 @@ typedef struct {
   double* theta_bar;
   double* rot_bar;
   int32_t* status;
+  const double* s_start;      /* [6*num_gp] or NULL: lattice-frame S the recomputation of the
+                                 converged state starts from (the forward's converged S of
+                                 this step makes it take no iterations); NULL starts at S = 0 */
 } cpfem_vjp_args_t;
 
 /* Library identity and error text. */

@@ -69,6 +69,7 @@ class GPArgs(ctypes.Structure):
         ("num_listed", ctypes.c_int32),
         ("pad", ctypes.c_int32),
         ("order", ctypes.c_void_p),
+        ("s_warm", ctypes.c_void_p),
     ]
 
 
@@ -85,7 +86,7 @@ class VjpArgs(ctypes.Structure):
     ] + [(name, ctypes.c_void_p) for name in (
         "u", "cells", "shape_grads", "jxw", "fpi", "g", "rot_table", "rot_idx", "param_table", "param_idx",
         "elastic_table", "cell_sig_bar", "fpi_bar", "g_bar", "mu", "f_bar", "fpi_bar_old", "g_bar_old", "theta_bar", "rot_bar",
-        "status")]
+        "status", "s_start")]
 
 
 class Sell(ctypes.Structure):

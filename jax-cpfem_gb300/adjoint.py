@@ -98,6 +98,7 @@ class LoadHistory:
         self.theta = np.asarray(theta, dtype=np.float64)
         self.euler = np.asarray(euler, dtype=np.float64)
         sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
+        p.reset_local_start()
         self.ckpt = []
         out = []
         params = p.internal_vars
@@ -113,12 +114,15 @@ class LoadHistory:
             out.append(sig.mean(0))
             params = p.update_int_vars_gp(sol.reshape(-1, 3), params)
             if checkpoint:
-                self.ckpt[-1] = self.ckpt[-1] + (sol.clone(),)
+                # the converged S of every GP (the last pass ran at sol) starts the backward's
+                # recomputations of this step's local state
+                w = p._warm()
+                self.ckpt[-1] = self.ckpt[-1] + (sol.clone(), None if w is None else w.clone())
         p.set_params(params)
         return torch.stack(out)
 
     # ------------------------------------------------------------------ backward
-    def _vjp(self, mode, u, fpi, g, cell_sig_bar, lam_fp, lam_g, mu=None):
+    def _vjp(self, mode, u, fpi, g, cell_sig_bar, lam_fp, lam_g, mu=None, s_start=None):
         p = self.p
         G, N = p.num_gp, p.num_slip
         a = _capi.VjpArgs()
@@ -136,6 +140,7 @@ class LoadHistory:
         a.cell_sig_bar = _dev_ptr(cell_sig_bar)
         a.fpi_bar, a.g_bar = _dev_ptr(lam_fp), _dev_ptr(lam_g)
         a.mu = _dev_ptr(mu)
+        a.s_start = _dev_ptr(s_start)
         status = torch.zeros(1, dtype=torch.int32, device=p.device)
         a.status = status.data_ptr()
         outs = {}
@@ -168,13 +173,15 @@ class LoadHistory:
         pc = self.adj_opts.get("precond", 1)
         self.krylov_iters = []
         for i in reversed(range(self.n_steps)):
-            fpi, g, u = self.ckpt[i]
+            fpi, g, u, s_conv = self.ckpt[i]
             self._set_step(i)
             p.fpi, p.g = fpi, g
             p._views = None
+            if s_conv is not None and p._warm() is not None:
+                p._warm().copy_(s_conv)
             cell_bar = (stress_bar[i] / E).expand(E, 9).contiguous()
             # 1. F cotangent and its gather into the right-hand side
-            fb = self._vjp(1, u, fpi, g, cell_bar, lam_fp, lam_g)["f_bar"]
+            fb = self._vjp(1, u, fpi, g, cell_bar, lam_fp, lam_g, s_start=s_conv)["f_bar"]
             f_u = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
             fe = p.fes[0]
             p.scatter(fb, None, f_u, None)
@@ -183,13 +190,14 @@ class LoadHistory:
             mu0 = torch.zeros_like(f_u)
             mu, k, ok = _solver.bicgstab(p, A.T, f_u, mu0, precond=pc, tol=self.adj_opts.get("tol", 1e-10),
                                          atol=self.adj_opts.get("atol", 1e-14),
-                                         maxiter=self.adj_opts.get("maxiter", 10000))
+                                         maxiter=self.adj_opts.get("maxiter", 10000),
+                                         mg_options=self.adj_opts.get("mg_options"))
             self.krylov_iters.append(k)
             if not ok:
                 raise RuntimeError(f"adjoint solve did not converge (iterations {k})")
             mu[fe.bc_dofs.long()] = 0.0
             # 3. cotangents of the step's inputs
-            o = self._vjp(2, u, fpi, g, cell_bar, lam_fp, lam_g, mu)
+            o = self._vjp(2, u, fpi, g, cell_bar, lam_fp, lam_g, mu, s_start=s_conv)
             lam_fp, lam_g = o["fpi_bar_old"], o["g_bar_old"]
             theta_acc += o["theta_bar"].sum(1)
             rot_acc.index_add_(0, ridx, o["rot_bar"].t())

@@ -243,6 +243,7 @@ def run_serial(instances, disps, dt, device=None, prepared=None):
     for k, (p, nodes) in enumerate(prepared):
         params = p.internal_vars
         sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
+        p.reset_local_start()
         for i, d in enumerate(disps):
             p.dt = float(dt)
             p.fes[0].set_dirichlet_lists(nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, float(d)])

@@ -57,14 +57,22 @@ __global__ void __launch_bounds__(64) k_gp_vjp(const MatDev m, const cpfem_vjp_a
     g[s] = a.g[s * G + gp];
     ig[s] = 1.0 / g[s];
   }
-  // recompute the converged local state (the checkpoint keeps only u, Fp^-1, g)
+  // recompute the converged local state from the checkpoint (u, Fp^-1, g and, if kept,
+  // the converged S as the local Newton's start)
   double A[9], AR[9], Ct[9];
   mm3(F, Fpi, A);
   mm3(A, R, AR);
   mm3_at(AR, AR, Ct);
   const double cdt = m.ao * a.dt;
   GPSolve<NS> st;
-  cp_local_newton<NS>(m, cc, Ct, ig, cdt, 1.0 / th[3], st);
+  if (a.s_start != nullptr) {
+    double s0[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s0[k] = a.s_start[k * G + gp];
+    cp_local_newton<NS>(m, cc, Ct, ig, cdt, 1.0 / th[3], st, s0);
+  } else {
+    cp_local_newton<NS>(m, cc, Ct, ig, cdt, 1.0 / th[3], st);
+  }
   // output cotangents
   constexpr int NY = YOut<NS>::kN;
   double ybar[NY];

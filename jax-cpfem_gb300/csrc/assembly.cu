@@ -126,7 +126,17 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
   mm3_at(AR, AR, Ct);
 
   GPSolve<NS> st;
-  cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
+  if (a.s_warm != nullptr) {
+    double s0[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s0[k] = a.s_warm[k * G + gp];
+    cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st, s0);
+    if (st.rn <= m.local_tol)
+#pragma unroll
+      for (int k = 0; k < 6; ++k) a.s_warm[k * G + gp] = st.s[k];
+  } else {
+    cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
+  }
   if (a.status != nullptr) {
     int bits = 0;
     if (!(st.rn <= m.local_tol)) bits |= CPFEM_GP_MAXITER;

@@ -135,29 +135,50 @@ CPFEM_HD void cp_jacobian(const MatDev& m, const Cub& cc, const double* kk, cons
   }
 }
 
-// Local Newton from s0 = 0 with the cut-half line search of models_copper.py:218-245:
-// trial residuals at s + relax ds, relax = 1, 1/2, ..., until the norm drops below the
-// current one or max_sub_step trials were made; the last trial is taken.
+constexpr int kWarmStartIters = 8;   // a warm start still unconverged after this restarts from 0
+
+// Local Newton with the cut-half line search of models_copper.py:218-245: trial
+// residuals at s + relax ds, relax = 1, 1/2, ..., until the norm drops below the current
+// one or max_sub_step trials were made; the last trial is taken.  It starts from s0 = 0,
+// as the reference does, or -- given s_init, the same GP's last converged stress -- from
+// there, which needs far fewer iterations once the global Newton iterates settle.  A
+// warm start that has not converged after kWarmStartIters iterations (or went
+// non-finite) is abandoned: one step with a single trial evaluates the residual at
+// s0 = 0 and the reference's iteration runs from there with its own max_iter.  Either way the result is the root of the same residual to the
+// same tolerance.  st.iters counts every step, the restart included.
 template <int NS>
 CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, const double* ig,
-                                                double cdt, double pexp, GPSolve<NS>& st) {
+                                                double cdt, double pexp, GPSolve<NS>& st,
+                                                const double* s_init = nullptr) {
   const int ie1 = int_exponent(pexp - 1.0);
   double r[6];
+  bool warm = s_init != nullptr;
 #pragma unroll
-  for (int k = 0; k < 6; ++k) st.s[k] = 0.0;
+  for (int k = 0; k < 6; ++k) st.s[k] = warm ? s_init[k] : 0.0;
   cp_residual<NS>(m, cc, Ct, ig, cdt, pexp, ie1, st.s, r, st.rn, st.dg, st.kk, st.B, st.M);
-  int it = 0;
-  while (st.rn > m.local_tol && it < m.max_iter) {
-    double J[36];
-    int perm[6];
-    double dinv[6];
-    cp_jacobian<NS>(m, cc, st.kk, st.M, J);
-    lu_factor<6>(J, perm, dinv);
+  const int warm_iters = (kWarmStartIters < m.max_iter) ? kWarmStartIters : m.max_iter - 1;
+  int it = 0, it0 = 0;   // it0: the step the s0 = 0 iteration started at
+  while ((st.rn > m.local_tol || (warm && !(st.rn <= m.local_tol))) && it - it0 < m.max_iter) {
     double ds[6];
+    int sub_cap = m.max_sub_step;
+    if (warm && (it >= warm_iters || !isfinite(st.rn))) {
+      // abandon the warm start: the single trial below lands on s = 0 + 1 * 0
 #pragma unroll
-    for (int k = 0; k < 6; ++k) ds[k] = -r[k];
-    lu_solve<6>(J, perm, dinv, ds);
-    const double rn0 = st.rn;
+      for (int k = 0; k < 6; ++k) st.s[k] = ds[k] = 0.0;
+      sub_cap = 1;
+      warm = false;
+      it0 = it + 1;
+    } else {
+      double J[36];
+      int perm[6];
+      double dinv[6];
+      cp_jacobian<NS>(m, cc, st.kk, st.M, J);
+      lu_factor<6>(J, perm, dinv);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) ds[k] = -r[k];
+      lu_solve<6>(J, perm, dinv, ds);
+    }
+    const double rn0 = sub_cap == 1 ? 0.0 : st.rn;
     double relax = 1.0;
     int sub = 0;
     double st_s[6];
@@ -167,7 +188,7 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, 
       cp_residual<NS>(m, cc, Ct, ig, cdt, pexp, ie1, st_s, r, st.rn, st.dg, st.kk, st.B, st.M);
       relax *= 0.5;
       ++sub;
-    } while (st.rn >= rn0 && sub < m.max_sub_step);
+    } while (st.rn >= rn0 && sub < sub_cap);
     // s + 2 relax ds with the halved relax is exactly the last trial point
 #pragma unroll
     for (int k = 0; k < 6; ++k) st.s[k] = st_s[k];

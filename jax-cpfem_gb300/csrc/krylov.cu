@@ -636,6 +636,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
   }
   ok = grid_reduce<2>(v2, parts(), w.sync, gen, smem, bcast) && ok;
   const double atol2 = fmax(tol * tol * v2[0], atol * atol);
+  const double rs0 = fmax(v2[1], atol2);
   double rs = v2[1], rho_new = v2[1], rho = 1.0, alpha = 1.0, omega = 1.0;
   int k = 0, restarts = 0;
 
@@ -745,7 +746,11 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
     rho = rho_new;
     rho_new = vr[1];
     rs = vr[0];
-    if (kn < 0 && restarts < max_restarts && ok && rs > atol2) {
+    // an FP32 V-cycle cannot resolve the near-null modes of a near-singular system (its
+    // rounding, amplified by the condition number, swamps them); a residual that grew by
+    // 1e8 or went non-finite ends the solve with -12 so the caller can re-solve in FP64
+    if (MGP == 2 && !(rs <= 1e16 * rs0)) kn = -12;
+    if (kn < 0 && kn != -12 && restarts < max_restarts && ok && rs > atol2) {
       // restart at the current x: rhat = p = q = r = b - A x (x is complete: the last
       // reduction crossed the grid barrier after every block wrote its part)
       ++restarts;

@@ -205,6 +205,9 @@ class CrystalPlasticity:
         self.timing = False
         self.timers = {}
         self.sort_gps = True     # order each tangent pass by the previous pass's local-Newton counts
+        # start each GP's local Newton from its last converged S instead of S = 0 (same root
+        # to the same tolerance; S = 0 again whenever the warm start does not converge)
+        self.warm_start_local = True
         self.custom_init(*additional_info)
 
     # ------------------------------------------------------------------ set-up
@@ -286,14 +289,16 @@ class CrystalPlasticity:
         sell = _capi.Sell(n, ng, *(a.data_ptr() for a in arrays))
         return rowptr, cols, goff, sell, arrays, 9 * int(slots[0])
 
-    def multigrid(self, max_levels=5, pre_sweeps=1, post_sweeps=1, coarse_sweeps=8, omega=0.45, precision="fp64",
+    def multigrid(self, max_levels=4, pre_sweeps=1, post_sweeps=1, coarse_sweeps=4, omega=0.45, precision="fp64",
                   local_nodes=256):
         """Geometric multigrid hierarchy of a structured box mesh for the BiCGSTAB
         preconditioner ``precond=3`` (built once; coarse operators by ``mg_setup``).
         Levels halve the cell counts while every count stays even, up to max_levels.
         precision="fp32" runs the V-cycle in single precision on rounded copies of the
-        operators (the Krylov iteration and its stop rule stay FP64); levels from the
-        third on with at most ``local_nodes`` nodes are smoothed inside one block."""
+        operators (the Krylov iteration and its stop rule stay FP64): faster, but not for
+        near-singular systems, where ``solver.bicgstab`` falls back to FP64 by itself.
+        Levels from the third on with at most ``local_nodes`` nodes are smoothed inside
+        one block."""
         if precision not in ("fp64", "fp32"):
             raise ValueError("multigrid precision must be 'fp64' or 'fp32'")
         if getattr(self, "_mg", None) is not None and self._mg_key == max_levels:
@@ -614,6 +619,21 @@ class CrystalPlasticity:
     def _state(self):
         return (self.fpi, self.g, self.slip, self.rot_table, self.rot_idx, self.param_table, self.param_idx)
 
+    def _warm(self):
+        """The per-GP lattice-frame S the local Newton starts from (or None)."""
+        if not self.warm_start_local:
+            return None
+        w = self._bufs.get("s_warm")
+        if w is None:
+            w = self._bufs["s_warm"] = torch.zeros((6, self.num_gp), dtype=torch.float64, device=self.device)
+        return w
+
+    def reset_local_start(self):
+        """Local Newton solves start from S = 0 again (a new load history)."""
+        w = self._bufs.get("s_warm")
+        if w is not None:
+            w.zero_()
+
     def region(self, name):
         """Context manager timing the enclosed library calls with CUDA events."""
         return _Region(self, name)
@@ -669,7 +689,7 @@ class CrystalPlasticity:
             trial = self.new_trial()
         trial = trial if need_tangent else {}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its, cell_list=cell_list, order=order, **trial)
+                             iters=its, cell_list=cell_list, order=order, s_warm=self._warm(), **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
         if ordered:
             # the next pass runs the GPs heaviest first, in runs of equal local-Newton counts
@@ -815,7 +835,7 @@ class CrystalPlasticity:
         status = self._buf("status", (1,), torch.int32)
         status.zero_()
         args = self._gp_args(self._state(), self.dt, u=u, stress=sw, fpi_new=fn, g_new=gn, slip_new=sn,
-                             status=status, weight_jxw=True)
+                             status=status, weight_jxw=True, s_warm=self._warm())
         self._run_gp(args, "gp_eval_post")
         sig = torch.empty((self.num_cells, 3, 3), dtype=torch.float64, device=self.device)
         _capi.check(self.lib.cpfem_cell_average(self.num_cells, _dev_ptr(self.fes[0].JxW), _dev_ptr(sw),

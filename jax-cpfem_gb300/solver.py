@@ -51,13 +51,35 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     info = np.zeros(2, dtype=np.int32)
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
                             float(tol), float(atol), None, int(grid_blocks), 0)
+    mg_options = dict(mg_options or {})
     if int(precond) == 3:
+        if getattr(problem, "mg_fp64_only", False):
+            mg_options["precision"] = "fp64"
         # the same hierarchy serves A^T (coarse operators (P^T A P)^T, transposed smoother)
-        opts.mg = ctypes.pointer(problem.mg_setup(A.values, **(mg_options or {})))
+        opts.mg = ctypes.pointer(problem.mg_setup(A.values, **mg_options))
+    b = b.contiguous()
     with problem.region("bicgstab"):
-        _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b.contiguous()), _dev_ptr(x),
+        _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
                                           ctypes.byref(opts), _dev_ptr(ws), info.ctypes.data, _stream()))
-    return x, int(info[0]), bool(info[1])
+    k, ok = int(info[0]), bool(info[1])
+    if int(precond) == 3 and opts.mg.contents.precision == 1 and not _fp32_solve_ok(problem, A, b, x, ok, tol, atol):
+        # the FP32 V-cycle failed on this system (near-singular: see cpfem_mg_t.precision);
+        # solve again with the FP64 V-cycle, and keep FP64 for this problem from now on
+        problem.mg_fp64_only = True
+        problem.stats["mg_fp64_fallbacks"] = problem.stats.get("mg_fp64_fallbacks", 0) + 1
+        return bicgstab(problem, A, b, x0, precond, tol, atol, maxiter, restarts, mg_options, grid_blocks)
+    return x, k, ok
+
+
+def _fp32_solve_ok(problem, A, b, x, converged, tol, atol):
+    """An FP32-preconditioned solve is kept when it converged and its true residual meets
+    the stop rule (with a factor 10 for the drift of the recursive residual)."""
+    if not converged:
+        return False
+    r = A.matvec(x)
+    r.sub_(b)
+    rn, bn = norm(problem, r), norm(problem, b)
+    return math.isfinite(rn) and rn <= 10.0 * max(tol * bn, atol)
 
 
 def jax_solve(problem, A, b, x0, precond=True, opts=None):

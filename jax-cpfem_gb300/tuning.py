@@ -18,7 +18,7 @@ import torch
 
 from . import solver as _solver
 
-DEFAULT = {"max_levels": 5, "pre_sweeps": 1, "post_sweeps": 1, "coarse_sweeps": 8, "omega": 0.45,
+DEFAULT = {"max_levels": 4, "pre_sweeps": 1, "post_sweeps": 1, "coarse_sweeps": 4, "omega": 0.45,
            "precision": "fp64", "local_nodes": 256, "grid_blocks": 0}
 # the keys that go to CrystalPlasticity.multigrid (grid_blocks goes to the launch)
 MG_KEYS = ("max_levels", "pre_sweeps", "post_sweeps", "coarse_sweeps", "omega", "precision", "local_nodes")

@@ -107,7 +107,7 @@ def test_fp32_vcycle_solves_the_tangent(pkg, gpu, local_nodes):
     res, A = solver_mod.newton_update_helper(prob, u)
     x0 = solver_mod.initial_increment(prob, u)
     xj, kj, okj = solver_mod.bicgstab(prob, A, -res, x0, precond=1)
-    xd, kd, okd = solver_mod.bicgstab(prob, A, -res, x0, precond=3)
+    xd, kd, okd = solver_mod.bicgstab(prob, A, -res, x0, precond=3, mg_options={"precision": "fp64"})
     xs, ks, oks = solver_mod.bicgstab(prob, A, -res, x0, precond=3,
                                       mg_options={"precision": "fp32", "local_nodes": local_nodes})
     assert prob._mg.precision == 1 and prob._mg.local_nodes == local_nodes
@@ -116,7 +116,8 @@ def test_fp32_vcycle_solves_the_tangent(pkg, gpu, local_nodes):
     r = A.matvec(xs) + res
     assert float(r.norm()) <= 1e-10 * max(float(res.norm()), 1.0) * 10
     # back to FP64 on the same hierarchy: the same iterates as the first FP64 solve
-    xd2, kd2, _ = solver_mod.bicgstab(prob, A, -res, x0, precond=3, mg_options={"local_nodes": 256})
+    xd2, kd2, _ = solver_mod.bicgstab(prob, A, -res, x0, precond=3,
+                                      mg_options={"precision": "fp64", "local_nodes": 256})
     assert kd2 == kd and torch.equal(xd2, xd)
 
 
@@ -181,10 +182,12 @@ def test_autotuner_picks_a_converging_configuration(pkg, gpu):
     assert ok and okj and float((x - xj).abs().max() / xj.abs().max()) < 1e-8
 
 
-def test_golden_case4_with_multigrid(pkg, gpu):
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_golden_case4_with_multigrid(pkg, gpu, precision):
     """The first 20 steps of calibration_case4 scenario 0 (20^3 Neper voxels, corner BCs with
     a free rigid rotation about z) with the multigrid-preconditioned solve: mean sigma_zz
-    against the reference's curve."""
+    against the reference's curve.  The system is near-singular: an FP32 V-cycle fails on
+    it, and the solver re-solves with the FP64 one."""
     import os
     problem_mod, solver_mod = gpu
     gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
@@ -202,12 +205,16 @@ def test_golden_case4_with_multigrid(pkg, gpu):
         prob.dt = float(ts[i + 1] - ts[i])
         prob.fes[0].set_dirichlet_lists([c, c, bot, top], [0, 1, 2, 2], [0.0, 0.0, 0.0, float(disps[i + 1])])
         prob.set_params(params)
-        sol = solver_mod.solver(prob, {"jax_solver": {"precond": "mg", "restart_on_breakdown": True}, "tol": 1e-7,
-                                       "line_search_flag": True, "initial_guess": [sol.reshape(-1, 3)]})[0].reshape(-1)
+        sol = solver_mod.solver(prob, {"jax_solver": {"precond": "mg", "restart_on_breakdown": True,
+                                                      "mg_options": {"precision": precision}},
+                                       "tol": 1e-7, "line_search_flag": True,
+                                       "initial_guess": [sol.reshape(-1, 3)]})[0].reshape(-1)
         out.append(float(prob.compute_avg_stress(sol.reshape(-1, 3), params)[:, 2, 2].mean()))
         params = prob.update_int_vars_gp(sol.reshape(-1, 3), params)
     rel = np.abs((np.array(out) - gold["case4_szz"][:20]) / gold["case4_szz"][:20])
     assert rel.max() < 1e-5, rel
+    if precision == "fp32":
+        assert prob.stats.get("mg_fp64_fallbacks", 0) >= 1 and prob.mg_fp64_only
 
 
 def test_transposed_multigrid_solve(pkg, gpu):
