@@ -213,7 +213,9 @@ def spmv_roofline(prob, torch, lib, reps=50):
 # profiles/dram_fcc32_loadstep.md, on the 32^3 benchmark matrix: the standalone SpMV and
 # the persistent BiCGSTAB (the matrix is read from HBM once per solve, then from L2).
 SPMV_DRAM_BYTES = {"c1": 72.4e6}
-KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 1): 75.7e6}
+# DRAM bytes of one k_bicgstab launch from ncu captures of the 32^3 bench matrix, by
+# (config, precond, V-cycle precision): Jacobi ~330 iterations, multigrid ~20-30
+KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 1, None): 75.7e6, ("c1", 3, "fp64"): 107.9e6, ("c1", 3, "fp32"): 3.662e9}
 
 
 def krylov_iteration_cost(prob, precond=1):
@@ -677,14 +679,13 @@ def main():
     kr_its = sum(max(k, 0) for k in krylov)
     kb, kf, kf32 = krylov_iteration_cost(prob, args.precond)
     mg_fp32 = args.precond == 3 and getattr(prob, "_mg", None) is not None and prob._mg.precision == 1
+    kr_key = (args.config, args.precond, ("fp32" if mg_fp32 else "fp64") if args.precond == 3 else None)
     kr_roof = None
     if kr_n and kr_ms > 0:
         tflops = kf * kr_its / (kr_ms * 1e-3) / 1e12
         gbs = kb * kr_its / (kr_ms * 1e-3) / 1e9
         kr_roof = {"bound": "fp64", "achieved": tflops, "peak": fp64, "unit": "TFLOP/s", "frac": tflops / fp64,
-                   "traffic": (KRYLOV_DRAM_BYTES_PER_LAUNCH[(args.config, args.precond)]
-                               if (args.config, args.precond) in KRYLOV_DRAM_BYTES_PER_LAUNCH and n == N_EDGE
-                               else None),
+                   "traffic": KRYLOV_DRAM_BYTES_PER_LAUNCH.get(kr_key) if n == N_EDGE else None,
                    "traffic_note": "DRAM bytes per launch (ncu); algorithmic bytes per launch = "
                                    "algorithmic_bytes_per_iteration x iterations, served from L2",
                    "kernel": ("k_bicgstab<0,%d> (persistent multigrid-preconditioned BiCGSTAB, %s V-cycle, one "
@@ -694,6 +695,9 @@ def main():
                    "launches": kr_n, "us_per_iteration": kr_ms * 1e3 / max(kr_its, 1),
                    "algorithmic_bytes_per_iteration": kb, "flops_per_iteration": kf,
                    "fp32_flops_per_iteration": kf32,
+                   "limiter": ("grid barriers and load latency (29 grid barriers per iteration; ncu: barrier "
+                               "and long-scoreboard stalls dominate, FP64 pipe 14-26 %)" if args.precond == 3
+                               else "FP64 pipe (the SpMVs)"),
                    "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm if hbm else None},
                    "peak_source": "cpfem_probe_dfma FP64 (of measured); HBM from MEASURED_PEAKS.json (of measured)"}
     spmv_roof = {"bound": "fp64", "achieved": spmv_flops / t_spmv / 1e12, "peak": fp64, "unit": "TFLOP/s",

@@ -101,7 +101,8 @@ typedef struct {
                                  of each listed cell; every output of other GPs is left
                                  untouched (a ragged batch skips its converged instances) */
   int32_t num_listed;
-  int32_t pad;
+  int32_t warm_mode;          /* with s_warm: 0 start there; 1 start at the linear prediction
+                                 s_warm + ds/dF : (F - s_f) (needs s_dsdf and s_f) */
   const int32_t* order;       /* [num_gp] permutation or NULL (no cell list): thread t
                                  evaluates GP order[t].  Ordering GPs by their previous
                                  local-Newton iteration count keeps a warp's lanes busy for
@@ -112,6 +113,14 @@ typedef struct {
                                  reference's start), falling back to S = 0 when that start has
                                  not converged after 8 iterations; the result is the root of
                                  the same residual to the same tolerance.  Zeros = S = 0. */
+  double* s_dsdf;             /* [54*num_gp] or NULL (with s_warm and s_f): ds/dF of the last
+                                 tangent pass, lattice-frame s by F component, entry
+                                 (6*kl + k)*num_gp + gp; written by tangent passes */
+  double* s_f;                /* [9*num_gp] or NULL (with s_warm and s_dsdf): F at which s_warm
+                                 converged, written with it.  The prediction is worth it once
+                                 ds/dF is that of a plastic state near the new one (not, for
+                                 instance, right after a state commit, when the relaxed
+                                 state's near-elastic ds/dF overshoots the flow stress). */
 } cpfem_gp_args_t;
 
 /*

@@ -172,12 +172,22 @@ class LoadHistory:
         ridx = p.rot_idx.long()
         pc = self.adj_opts.get("precond", 1)
         self.krylov_iters = []
+        predict, p.predict_local = p.predict_local, False   # starts come from the checkpoints
+        try:
+            return self._backward(stress_bar, lam_fp, lam_g, theta_acc, rot_acc, ridx, pc)
+        finally:
+            p.predict_local = predict
+
+    def _backward(self, stress_bar, lam_fp, lam_g, theta_acc, rot_acc, ridx, pc):
+        p = self.p
+        E = p.num_cells
         for i in reversed(range(self.n_steps)):
             fpi, g, u, s_conv = self.ckpt[i]
             self._set_step(i)
             p.fpi, p.g = fpi, g
             p._views = None
             if s_conv is not None and p._warm() is not None:
+                # the step's tangent is re-formed at its converged S: no prediction needed
                 p._warm().copy_(s_conv)
             cell_bar = (stress_bar[i] / E).expand(E, 9).contiguous()
             # 1. F cotangent and its gather into the right-hand side

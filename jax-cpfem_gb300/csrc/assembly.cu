@@ -126,14 +126,28 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
   mm3_at(AR, AR, Ct);
 
   GPSolve<NS> st;
+  const bool predict = a.s_warm != nullptr && a.s_dsdf != nullptr && a.s_f != nullptr;
   if (a.s_warm != nullptr) {
     double s0[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) s0[k] = a.s_warm[k * G + gp];
+    if (predict && a.warm_mode == 1) {
+      // first-order prediction from where s_warm converged: s0 += ds/dF : (F - F_then)
+#pragma unroll
+      for (int kl = 0; kl < 9; ++kl) {
+        const double dF = F[kl] - a.s_f[kl * G + gp];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s0[k] = fma(a.s_dsdf[(6 * kl + k) * G + gp], dF, s0[k]);
+      }
+    }
     cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st, s0);
-    if (st.rn <= m.local_tol)
+    if (st.rn <= m.local_tol) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) a.s_warm[k * G + gp] = st.s[k];
+      if (predict)
+#pragma unroll
+        for (int kl = 0; kl < 9; ++kl) a.s_f[kl * G + gp] = F[kl];
+    }
   } else {
     cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
   }
@@ -191,9 +205,13 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
   if (a.iters != nullptr) a.iters[gp] = st.iters;
   if (TANGENT && a.tangent != nullptr) {
     double* tan = a.tangent;
-    auto store = [&](int kl, const double* col) {
+    const bool keep_dsdf = predict && st.rn <= m.local_tol;
+    auto store = [&](int kl, const double* col, const double* dsdf) {
 #pragma unroll
       for (int c = 0; c < 9; ++c) tan[(int64_t)(9 * c + kl) * G + gp] = col[c] * w;
+      if (keep_dsdf)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a.s_dsdf[(6 * kl + k) * G + gp] = dsdf[k];
     };
     cp_tangent<NS>(m, cc, F, Gm, st, H, W, Y, idet, store);
   }

@@ -221,8 +221,8 @@ CPFEM_HD void cp_stress(const double* F, const double* G /*Fp^-1_old R*/, const 
 // Consistent tangent at the converged state:
 // dP/dF = d_ik Y_lJ + (dP/ds)(ds/dF) with ds/dF = J^-1 C : sym(Fe_l[k,:] (x) H[l,:]),
 // the implicit-function tangent of f_jvp (models_copper.py:251-259).
-// The tangent column for F_kl is handed to store_col(kl, col[9]) as soon as it is
-// known, so the 81 entries never need to be live at once.  Called after every other
+// The tangent column for F_kl is handed to store_col(kl, col[9], ds/dF_kl[6]) as soon as
+// it is known, so the 81 entries never need to be live at once.  Called after every other
 // output of the Gauss point is written, so only what it needs is live.
 template <int NS, class StoreCol>
 CPFEM_HD void cp_tangent(const MatDev& m, const Cub& cc, const double* F, const double* G /*Fp^-1_old R*/,
@@ -300,7 +300,7 @@ CPFEM_HD void cp_tangent(const MatDev& m, const Cub& cc, const double* F, const 
         for (int mm = 0; mm < 6; ++mm) v = fma(dPds[mm][3 * i + j], x[mm], v);
         col[3 * i + j] = v;
       }
-    store_col(kl, col);
+    store_col(kl, col, x);
   }
 }
 

@@ -208,6 +208,9 @@ class CrystalPlasticity:
         # start each GP's local Newton from its last converged S instead of S = 0 (same root
         # to the same tolerance; S = 0 again whenever the warm start does not converge)
         self.warm_start_local = True
+        # ... moved to first order along F: s_warm + ds/dF (F - F_warm), with the ds/dF of the
+        # last tangent pass (no effect on the result, fewer local iterations)
+        self.predict_local = True
         self.custom_init(*additional_info)
 
     # ------------------------------------------------------------------ set-up
@@ -590,7 +593,7 @@ class CrystalPlasticity:
         return [dofs.reshape(self.num_nodes, 3)]
 
     # ------------------------------------------------------------------ GPU passes
-    def _gp_args(self, state, dt, u=None, u_grad=None, num_gp=None, elastic=None, **outs):
+    def _gp_args(self, state, dt, u=None, u_grad=None, num_gp=None, elastic=None, warm_mode=0, **outs):
         a = _capi.GPArgs()
         fpi, g, slip, rot_table, rot_idx, param_table, param_idx = state
         a.num_gp = self.num_gp if num_gp is None else num_gp
@@ -609,6 +612,7 @@ class CrystalPlasticity:
         else:
             a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
         a.weight_jxw = 1 if outs.pop("weight_jxw", False) else 0
+        a.warm_mode = int(warm_mode)
         cl = outs.pop("cell_list", None)
         if cl is not None:
             a.cell_list, a.num_listed = _dev_ptr(cl), int(cl.numel())
@@ -628,11 +632,35 @@ class CrystalPlasticity:
             w = self._bufs["s_warm"] = torch.zeros((6, self.num_gp), dtype=torch.float64, device=self.device)
         return w
 
+    def _warm_args(self, tangent=False):
+        """GP-pass arguments of the local Newton's start: the warm start, and from the third
+        tangent pass under the same committed state on the linear prediction (the first
+        tangent pass after a commit sees the relaxed, near-elastic state, whose ds/dF would
+        overshoot the flow stress on the next pass)."""
+        w = self._warm()
+        if w is None:
+            return {}
+        out = {"s_warm": w}
+        if self.predict_local:
+            for name, rows in (("s_dsdf", 54), ("s_f", 9)):
+                b = self._bufs.get(name)
+                if b is None:
+                    b = self._bufs[name] = torch.zeros((rows, self.num_gp), dtype=torch.float64, device=self.device)
+                out[name] = b
+            token, count = getattr(self, "_tangent_passes", (None, 0))
+            if token != self._state_token:
+                count = 0
+            out["warm_mode"] = 1 if count >= 2 else 0
+            if tangent:
+                self._tangent_passes = (self._state_token, count + 1)
+        return out
+
     def reset_local_start(self):
         """Local Newton solves start from S = 0 again (a new load history)."""
-        w = self._bufs.get("s_warm")
-        if w is not None:
-            w.zero_()
+        for name in ("s_warm", "s_dsdf", "s_f"):
+            w = self._bufs.get(name)
+            if w is not None:
+                w.zero_()
 
     def region(self, name):
         """Context manager timing the enclosed library calls with CUDA events."""
@@ -689,7 +717,8 @@ class CrystalPlasticity:
             trial = self.new_trial()
         trial = trial if need_tangent else {}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its, cell_list=cell_list, order=order, s_warm=self._warm(), **trial)
+                             iters=its, cell_list=cell_list, order=order, **self._warm_args(need_tangent),
+                             **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
         if ordered:
             # the next pass runs the GPs heaviest first, in runs of equal local-Newton counts
@@ -835,7 +864,7 @@ class CrystalPlasticity:
         status = self._buf("status", (1,), torch.int32)
         status.zero_()
         args = self._gp_args(self._state(), self.dt, u=u, stress=sw, fpi_new=fn, g_new=gn, slip_new=sn,
-                             status=status, weight_jxw=True, s_warm=self._warm())
+                             status=status, weight_jxw=True, **self._warm_args())
         self._run_gp(args, "gp_eval_post")
         sig = torch.empty((self.num_cells, 3, 3), dtype=torch.float64, device=self.device)
         _capi.check(self.lib.cpfem_cell_average(self.num_cells, _dev_ptr(self.fes[0].JxW), _dev_ptr(sw),

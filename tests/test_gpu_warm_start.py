@@ -1,7 +1,7 @@
-"""Warm-started local Newton (each GP starts from its last converged S instead of S = 0):
-the abandoned warm start reproduces the S = 0 solve bit for bit, a warm start from a
-nearby state converges to the same root, and load steps with and without it agree and
-match the oracle."""
+"""Warm-started local Newton (each GP starts from its last converged S, moved to first
+order along F, instead of S = 0): the abandoned warm start reproduces the S = 0 solve bit
+for bit, warm and predicted starts converge to the same root, and load steps with and
+without them agree and match the oracle."""
 import numpy as np
 import pytest
 import torch
@@ -61,6 +61,26 @@ def test_warm_start_converges_to_the_same_root(pkg, gpu):
     assert float((rw - rc).abs().max() / rc.abs().max()) < 1e-10
     assert float((vw - vc).abs().max() / vc.abs().max()) < 1e-9
     assert float(iw.double().mean()) < 0.6 * float(ic.double().mean()), (iw.double().mean(), ic.double().mean())
+
+
+def test_linear_predictor_cuts_local_iterations(pkg, gpu):
+    """Starting at s_warm + ds/dF (F - F_warm) instead of at s_warm: the same root, fewer
+    local iterations."""
+    problem_mod, _ = gpu
+    _, _, _, _, prob, u = _case(pkg, problem_mod)
+    prob.reset_local_start()
+    _pass(prob, u)                      # s_warm, its F and ds/dF at u
+    _pass(prob, u)                      # (the prediction is used from the third tangent pass)
+    saved = {k: prob._bufs[k].clone() for k in ("s_warm", "s_dsdf", "s_f")}
+    u2 = u * (1.0 + 2e-2)
+    rp, vp, ip = _pass(prob, u2)
+    for k, v in saved.items():
+        prob._bufs[k].copy_(v)
+    prob.predict_local = False
+    rw, vw, iw = _pass(prob, u2)
+    assert float((rp - rw).abs().max() / rw.abs().max()) < 1e-10
+    assert float((vp - vw).abs().max() / vw.abs().max()) < 1e-9
+    assert float(ip.double().mean()) < float(iw.double().mean()), (ip.double().mean(), iw.double().mean())
 
 
 def test_load_steps_with_warm_start_match_cold_and_oracle(pkg, gpu):
