@@ -410,7 +410,10 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
     theta = np.array([spec.h, spec.gss_initial, spec.t_sat, spec.gss_a, spec.xm])
     euler = np.zeros((N_GRAINS, 3))
     # synthetic target: h0, g0, gs scaled by 1.1 under the same seed
-    target = h.forward(theta * np.array([1.1, 1.1, 1.1, 1.0, 1.0]), euler, checkpoint=False).cpu().numpy()[:, 2, 2]
+    target = h.forward(theta * np.array([1.1, 1.1, 1.1, 1.0, 1.0]), euler).cpu().numpy()[:, 2, 2]
+    # untimed backward of that run: every kernel of the backward path (the library's and
+    # torch's) has run once before the clock starts, as the forward's have
+    h.backward(np.ones((nsteps, 3, 3)))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s = h.forward(theta, euler).cpu().numpy()[:, 2, 2]
@@ -436,9 +439,15 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
         d_t = rng.normal(size=5) * theta * 1e-6
         d_e = rng.normal(size=euler.shape) * 1e-4
         f = lambda th, eu: float(((h.forward(th, eu, checkpoint=False).cpu().numpy()[:, 2, 2] - target) ** 2).mean())
+        # the difference quotient runs the local solves from S = 0, the reference's start: a
+        # warm start stops as soon as the residual is below the local tolerance, so the map
+        # is smooth only to that tolerance (~1e-10 relative), which a 1e-6 step amplifies
+        prob.warm_start_local = False
         fd = (f(theta + d_t, euler + d_e) - f(theta - d_t, euler - d_e)) / 2.0
+        prob.warm_start_local = True
         ad = float(tb @ d_t + (eb * d_e).sum())
-        out["directional_fd_check"] = {"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd)}
+        out["directional_fd_check"] = {"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd),
+                                       "fd_local_start": "S = 0"}
     print(json.dumps(out))
 
 

@@ -168,8 +168,10 @@ class LoadHistory:
         lam_fp = torch.zeros((9, G), dtype=torch.float64, device=p.device)
         lam_g = torch.zeros((N, G), dtype=torch.float64, device=p.device)
         theta_acc = torch.zeros(5, dtype=torch.float64, device=p.device)
-        rot_acc = torch.zeros((p.rot_table.shape[0], 3), dtype=torch.float64, device=p.device)
-        ridx = p.rot_idx.long()
+        # per-GP rotation cotangents summed over the steps on the device; the per-grain sum
+        # happens once on the host at the end
+        rot_acc = torch.zeros((3, G), dtype=torch.float64, device=p.device)
+        ridx = p.rot_idx.cpu().numpy().astype(np.int64)
         pc = self.adj_opts.get("precond", 1)
         self.krylov_iters = []
         predict, p.predict_local = p.predict_local, False   # starts come from the checkpoints
@@ -210,12 +212,15 @@ class LoadHistory:
             o = self._vjp(2, u, fpi, g, cell_bar, lam_fp, lam_g, mu, s_start=s_conv)
             lam_fp, lam_g = o["fpi_bar_old"], o["g_bar_old"]
             theta_acc += o["theta_bar"].sum(1)
-            rot_acc.index_add_(0, ridx, o["rot_bar"].t())
+            rot_acc += o["rot_bar"]
         # parameters: (gss_a, h, t_sat, xm) -> (a, h0, gs, m); g0 through the initial state
         th = theta_acc.cpu().numpy()
         theta_bar = np.array([th[1], float(lam_g.sum()), th[2], th[0], th[3]])
         gen = _euler_generators(self.euler)                       # (n_grains, 3 angles, 3)
-        euler_bar = np.einsum("gkj,gj->gk", gen, rot_acc.cpu().numpy())
+        per_gp = rot_acc.cpu().numpy()
+        n_rot = p.rot_table.shape[0]
+        per_grain = np.stack([np.bincount(ridx, weights=per_gp[c], minlength=n_rot) for c in range(3)], axis=1)
+        euler_bar = np.einsum("gkj,gj->gk", gen, per_grain)
         return theta_bar, euler_bar
 
 

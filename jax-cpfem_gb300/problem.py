@@ -693,11 +693,13 @@ class CrystalPlasticity:
         if s & _capi.CPFEM_GP_MAXITER:
             raise RuntimeError(f"local Newton did not converge within max_iter={self.material.max_iter}")
 
-    def assemble(self, u, need_tangent=True, cell_list=None, trial=None):
+    def assemble(self, u, need_tangent=True, cell_list=None, trial=None, keep_trial=False):
         """Residual int P:grad(v) (ndof) and, if asked, the CSR tangent values, before BCs.
         ``cell_list`` (device int32) restricts the constitutive pass to those cells: the
         other GPs keep their P, dP/dF and trial outputs from an earlier pass (``trial``, a
-        dict of persistent trial buffers, keeps them across passes).
+        dict of persistent trial buffers, keeps them across passes).  Tangent passes, and
+        residual passes with ``keep_trial``, also write the trial state and stress that
+        become the step's post-processing if ``u`` turns out to be converged.
         Returns (res, values or None, status tensor)."""
         G = self.num_gp
         res = self._buf("res", (self.num_total_dofs_all_vars,))
@@ -710,12 +712,13 @@ class CrystalPlasticity:
             values = self._buf("values", (self.num_values,))
             values.zero_()
             dw = self._buf("tangent_w", (81, G))
-        ordered = self.sort_gps and need_tangent and cell_list is None
+        with_trial = need_tangent or keep_trial
+        ordered = self.sort_gps and with_trial and cell_list is None
         its = self._buf("iters", (G,), torch.int32) if (self.timing or ordered) else None
         order = self._bufs.get("gp_order") if ordered else None
-        if need_tangent and trial is None:
+        if with_trial and trial is None:
             trial = self.new_trial()
-        trial = trial if need_tangent else {}
+        trial = trial if with_trial else {}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
                              iters=its, cell_list=cell_list, order=order, **self._warm_args(need_tangent),
                              **trial)
@@ -769,12 +772,13 @@ class CrystalPlasticity:
         self.A_values = values
         return [res.reshape(self.num_nodes, 3)]
 
-    def compute_residual(self, sol_list, check=True):
+    def compute_residual(self, sol_list, check=True, keep_trial=False):
         """Residual only.  ``check=False`` lets non-finite or unconverged local solves
         through as values (the global line search compares their norms the way the
-        reference does, ``solver.py:258-272``)."""
+        reference does, ``solver.py:258-272``); ``keep_trial`` also keeps the pass's trial
+        state for the post-processing (a Newton iterate expected to be the last)."""
         u = _flat(sol_list, self.device)
-        res, _, status = self.assemble(u, need_tangent=False)
+        res, _, status = self.assemble(u, need_tangent=False, keep_trial=keep_trial)
         if check:
             self._check_status(status)
         return [res.reshape(self.num_nodes, 3)]

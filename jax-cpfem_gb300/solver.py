@@ -123,10 +123,19 @@ def newton_update_helper(problem, dofs):
     return res, DeviceCSR(problem, problem.A_values)
 
 
-def residual_bc(problem, dofs, check=True):
-    res = problem.compute_residual(problem.unflatten_fn_sol_list(dofs), check=check)[0].reshape(-1)
+def residual_bc(problem, dofs, check=True, keep_trial=False):
+    res = problem.compute_residual(problem.unflatten_fn_sol_list(dofs), check=check,
+                                   keep_trial=keep_trial)[0].reshape(-1)
     problem.apply_dirichlet(res, dofs, None)
     return res
+
+
+def _expect_converged(history, limit):
+    """Newton converges quadratically near the root, r_{k+1} ~ r_k^3 / r_{k-1}^2: True when
+    that predicts the next residual well (4x) below the stop limit."""
+    if len(history) < 2 or not (history[-2] > 0.0 and history[-1] < history[-2]):
+        return False
+    return history[-1] ** 3 / history[-2] ** 2 < 0.25 * limit
 
 
 def initial_increment(problem, dofs):
@@ -190,12 +199,27 @@ def solver(problem, solver_options=None):
     rel_res_val = res_val / res_val_initial if res_val_initial > 0 else float("nan")
     history = [res_val]
     it = 0
+    limit = max(tol, rel_tol * res_val_initial)
+    skip = getattr(problem, "skip_final_tangent", True)
     while (rel_res_val > rel_tol) and (res_val > tol):
         if it >= max_newton:
             raise RuntimeError(f"global Newton did not converge in {max_newton} iterations (res = {res_val})")
         dofs = linear_incremental_solver(problem, res_vec, A, dofs, solver_options)
-        res_vec, A = newton_update_helper(problem, dofs)
-        res_val = norm(problem, res_vec)
+        res_vec = None
+        if skip and _expect_converged(history, limit):
+            # the last iterate needs no tangent: residual (and trial state) only, and the
+            # tangent pass after all if the residual is not below the limit yet (its local
+            # solves then start at their roots)
+            res_vec = residual_bc(problem, dofs, keep_trial=True)
+            res_val = norm(problem, res_vec)
+            if (res_val / res_val_initial > rel_tol) and (res_val > tol):
+                problem.stats["final_tangent_mispredicted"] = problem.stats.get("final_tangent_mispredicted", 0) + 1
+                res_vec = None
+            else:
+                problem.stats["final_tangent_skipped"] = problem.stats.get("final_tangent_skipped", 0) + 1
+        if res_vec is None:
+            res_vec, A = newton_update_helper(problem, dofs)
+            res_val = norm(problem, res_vec)
         rel_res_val = res_val / res_val_initial
         history.append(res_val)
         it += 1
