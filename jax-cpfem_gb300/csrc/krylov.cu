@@ -251,10 +251,12 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* partials, G
 // the trilinear weight prod_d (1 if i_d = 2 I_d else 1/2).
 
 __device__ __forceinline__ void mg_xyz(int64_t a, const int32_t* dims, int& x, int& y, int& z) {
-  x = (int)(a % dims[0]);
-  const int64_t q = a / dims[0];
-  y = (int)(q % dims[1]);
-  z = (int)(q / dims[1]);
+  // node counts fit 32 bits (cpfem_sell_t.num_nodes is int32): 32-bit divisions
+  const unsigned ua = (unsigned)a, d0 = (unsigned)dims[0], d1 = (unsigned)dims[1];
+  const unsigned q = ua / d0;
+  x = (int)(ua - q * d0);
+  z = (int)(q / d1);
+  y = (int)(q - (unsigned)z * d1);
 }
 
 // z = D^-1 v with the stored inverse diagonal block; TRANS uses its transpose, which is
@@ -287,7 +289,23 @@ __device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const R* V, cons
 
 // Rows of node a of A x (A^T x when TRANS) restricted to the slots j = q (mod 4) (one
 // lane of a quad).
-template <bool TRANS, typename R>
+// A vector element written earlier in the launch: an L2 load from global memory (other
+// blocks may have written it), a plain load from shared memory (SH).
+template <bool SH, typename R>
+__device__ __forceinline__ R ldv(const R* p) {
+  if constexpr (SH) return *p;
+  else return __ldcg(p);
+}
+
+// A value of a level operator: read-only for the whole launch, so through the read-only
+// cache from global memory, or a plain load from shared memory (SH).
+template <bool SH, typename R>
+__device__ __forceinline__ R ldc(const R* p) {
+  if constexpr (SH) return *p;
+  else return __ldg(p);
+}
+
+template <bool TRANS, bool SH, typename R, bool SHV = false>
 __device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const R* __restrict__ vals, const R* x,
                                                int64_t a, int q, R* acc) {
   const int64_t g = a >> 5;
@@ -299,18 +317,57 @@ __device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const R* _
 #pragma unroll 2
   for (int j = q; j < w; j += 4) {
     const int64_t b = __ldg(&L.cols[c0 + 32 * j]);
-    const R x0 = __ldcg(&x[3 * b]), x1 = __ldcg(&x[3 * b + 1]), x2 = __ldcg(&x[3 * b + 2]);
+    const R x0 = ldv<SH>(&x[3 * b]), x1 = ldv<SH>(&x[3 * b + 1]), x2 = ldv<SH>(&x[3 * b + 2]);
     if (!TRANS) {
       const R* vb = v0 + 288 * j;
-      a0 = mad(__ldg(&vb[0]), x0, mad(__ldg(&vb[32]), x1, mad(__ldg(&vb[64]), x2, a0)));
-      a1 = mad(__ldg(&vb[96]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[160]), x2, a1)));
-      a2 = mad(__ldg(&vb[192]), x0, mad(__ldg(&vb[224]), x1, mad(__ldg(&vb[256]), x2, a2)));
+      a0 = mad(ldc<SHV>(&vb[0]), x0, mad(ldc<SHV>(&vb[32]), x1, mad(ldc<SHV>(&vb[64]), x2, a0)));
+      a1 = mad(ldc<SHV>(&vb[96]), x0, mad(ldc<SHV>(&vb[128]), x1, mad(ldc<SHV>(&vb[160]), x2, a1)));
+      a2 = mad(ldc<SHV>(&vb[192]), x0, mad(ldc<SHV>(&vb[224]), x1, mad(ldc<SHV>(&vb[256]), x2, a2)));
     } else {
       const int64_t tp = __ldg(&L.tpos[c0 + 32 * j]);
       const R* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
-      a0 = mad(__ldg(&vb[0]), x0, mad(__ldg(&vb[96]), x1, mad(__ldg(&vb[192]), x2, a0)));
-      a1 = mad(__ldg(&vb[32]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[224]), x2, a1)));
-      a2 = mad(__ldg(&vb[64]), x0, mad(__ldg(&vb[160]), x1, mad(__ldg(&vb[256]), x2, a2)));
+      a0 = mad(ldc<SHV>(&vb[0]), x0, mad(ldc<SHV>(&vb[96]), x1, mad(ldc<SHV>(&vb[192]), x2, a0)));
+      a1 = mad(ldc<SHV>(&vb[32]), x0, mad(ldc<SHV>(&vb[128]), x1, mad(ldc<SHV>(&vb[224]), x2, a1)));
+      a2 = mad(ldc<SHV>(&vb[64]), x0, mad(ldc<SHV>(&vb[160]), x1, mad(ldc<SHV>(&vb[256]), x2, a2)));
+    }
+  }
+  acc[0] = a0;
+  acc[1] = a1;
+  acc[2] = a2;
+}
+
+constexpr int kMgMaxWidth = 27;                 // neighbour slots of a structured-box node
+
+// sell_rows_quad on a level staged in shared memory: values, x and the index tables
+// (group offsets, widths, columns, transposed slots as int32, mg_stage) all there.
+template <bool TRANS, typename R>
+__device__ __forceinline__ void sell_rows_quad_st(const int* ix, int ng, const R* vals, const R* x, int64_t a,
+                                                  int q, R* acc) {
+  const int* goff = ix;
+  const int* gw = ix + ng + 1;
+  const int* cols = gw + ng;
+  const int* tpos = cols + 32 * kMgMaxWidth * ng;
+  const int g = (int)(a >> 5);
+  const int lane = (int)(a & 31);
+  const int c0 = goff[g] + lane;
+  const R* v0 = vals + 9 * goff[g] + lane;
+  const int w = gw[g];
+  R a0 = R(0), a1 = R(0), a2 = R(0);
+#pragma unroll 2
+  for (int j = q; j < w; j += 4) {
+    const int b = cols[c0 + 32 * j];
+    const R x0 = x[3 * b], x1 = x[3 * b + 1], x2 = x[3 * b + 2];
+    if (!TRANS) {
+      const R* vb = v0 + 288 * j;
+      a0 = mad(vb[0], x0, mad(vb[32], x1, mad(vb[64], x2, a0)));
+      a1 = mad(vb[96], x0, mad(vb[128], x1, mad(vb[160], x2, a1)));
+      a2 = mad(vb[192], x0, mad(vb[224], x1, mad(vb[256], x2, a2)));
+    } else {
+      const int tp = tpos[c0 + 32 * j];
+      const R* vb = vals + 9 * goff[b >> 5] + (b & 31) + 288 * tp;
+      a0 = mad(vb[0], x0, mad(vb[96], x1, mad(vb[192], x2, a0)));
+      a1 = mad(vb[32], x0, mad(vb[128], x1, mad(vb[224], x2, a1)));
+      a2 = mad(vb[64], x0, mad(vb[160], x1, mad(vb[256], x2, a2)));
     }
   }
   acc[0] = a0;
@@ -357,13 +414,13 @@ __device__ __forceinline__ void quad_sum3(R* v) {
 // Level operations of the V-cycle on a coarse level (l >= 1), one quad of lanes per node:
 // nodes a = tq, tq + sq, ... (tq = this lane's quad, sq = the quads taking part; a warp
 // holds 8 consecutive quads and runs the padded loops in lockstep, so the shuffles always
-// see the whole warp); lane 0 of a node's quad owns its writes.
+// see the whole warp); lane 0 of a node's quad owns its writes.  The level's vectors are
+// passed explicitly: global arrays on the grid-wide levels, shared memory (SH) on the
+// block-local ones.
 template <bool TRANS, typename R>
-__device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, const MgArrays<R>& A, int l, R* X, int64_t tq,
-                                                int64_t sq, int q) {
+__device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, const R* Mi, int l, R* X, const R* B,
+                                                int64_t tq, int64_t sq, int q) {
   if (q != 0) return;
-  const R* B = A.b(l);
-  const R* Mi = A.minv(l);
   const R om = (R)mg.omega;
   for (int64_t a = tq; a < mg.sell[l].num_nodes; a += sq) {
     R v[3] = {B[3 * a], B[3 * a + 1], B[3 * a + 2]}, z[3];
@@ -374,17 +431,19 @@ __device__ __forceinline__ void mgq_first_sweep(const cpfem_mg_t& mg, const MgAr
 }
 
 // T = X + omega Minv (B - A X)  (residual = false)  or  T = B - A X  (residual = true)
-template <bool TRANS, typename R>
-__device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, const MgArrays<R>& A, int l, const R* X, R* T,
-                                          bool residual, int64_t tq, int64_t sq, int q) {
+template <bool TRANS, bool SH, bool SHV = false, typename R>
+__device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, const R* V, const R* Mi, int l, const R* X, R* T,
+                                          const R* B, bool residual, int64_t tq, int64_t sq, int q,
+                                          const int* sidx = nullptr) {
   const cpfem_sell_t& S = mg.sell[l];
-  const R* B = A.b(l);
-  const R* V = A.values(l);
   const R om = (R)mg.omega;
   const int64_t n = S.num_nodes, npad = (n + 7) / 8 * 8;
   for (int64_t a = tq; a < npad; a += sq) {
     R acc[3] = {R(0), R(0), R(0)};
-    if (a < n) sell_rows_quad<TRANS>(S, V, X, a, q, acc);
+    if (a < n) {
+      if constexpr (SHV) sell_rows_quad_st<TRANS>(sidx, S.num_groups, V, X, a, q, acc);
+      else sell_rows_quad<TRANS, SH, R>(S, V, X, a, q, acc);
+    }
     quad_sum3(acc);
     if (a < n && q == 0) {
       R r[3];
@@ -395,7 +454,7 @@ __device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, const MgArrays<R
         for (int i = 0; i < 3; ++i) T[3 * a + i] = r[i];
       } else {
         R z[3];
-        mg_apply_minv<TRANS>(A.minv(l), a, r, z);
+        mg_apply_minv<TRANS>(Mi, a, r, z);
 #pragma unroll
         for (int i = 0; i < 3; ++i) T[3 * a + i] = mad(om, z[i], X[3 * a + i]);
       }
@@ -403,27 +462,31 @@ __device__ __forceinline__ void mgq_apply(const cpfem_mg_t& mg, const MgArrays<R
   }
 }
 
-// b_{l+1} = P^T Res_l: the 27 fine nodes of a coarse node split over its quad.
-template <typename R>
-__device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, const MgArrays<R>& A, int l, const R* Res,
-                                             int64_t tq, int64_t sq, int q) {
+// Bc = P^T Res_l (the level l+1 right-hand side): the 27 fine nodes of a coarse node
+// split over its quad.  SH: Res is in shared memory.
+template <bool SH, typename R>
+__device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, int l, const R* Res, R* Bc, int64_t tq,
+                                             int64_t sq, int q) {
   const int32_t* df = mg.dims[l];
   const int32_t* dc = mg.dims[l + 1];
-  R* Bc = A.b(l + 1);
   const int64_t nc = mg.sell[l + 1].num_nodes, ncpad = (nc + 7) / 8 * 8;
   for (int64_t I = tq; I < ncpad; I += sq) {
     R acc[3] = {R(0), R(0), R(0)};
     if (I < nc) {
       int cx, cy, cz;
       mg_xyz(I, dc, cx, cy, cz);
-      for (int k = q; k < 27; k += 4) {
-        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-        const int ix = 2 * cx + dx, iy = 2 * cy + dy, iz = 2 * cz + dz;
-        if (ix < 0 || ix >= df[0] || iy < 0 || iy >= df[1] || iz < 0 || iz >= df[2]) continue;
-        const R w = (dx ? R(0.5) : R(1)) * (dy ? R(0.5) : R(1)) * (dz ? R(0.5) : R(1));
-        const int64_t i = ix + (int64_t)df[0] * (iy + (int64_t)df[1] * iz);
+      // the lane's fine neighbours k = q, q+4, ... < 27, unrolled and predicated (an absent
+      // neighbour reads node 0 with weight 0), so all their loads are in flight together
 #pragma unroll
-        for (int c = 0; c < 3; ++c) acc[c] = mad(w, __ldcg(&Res[3 * i + c]), acc[c]);
+      for (int kk = 0; kk < 7; ++kk) {
+        const int k = q + 4 * kk;
+        const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+        const int ix = 2 * cx + dx, iy = 2 * cy + dy, iz = 2 * cz + dz;
+        const bool in = k < 27 && ix >= 0 && ix < df[0] && iy >= 0 && iy < df[1] && iz >= 0 && iz < df[2];
+        const R w = in ? (dx ? R(0.5) : R(1)) * (dy ? R(0.5) : R(1)) * (dz ? R(0.5) : R(1)) : R(0);
+        const int64_t i = in ? ix + (int64_t)df[0] * (iy + (int64_t)df[1] * iz) : 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) acc[c] = mad(w, ldv<SH>(&Res[3 * i + c]), acc[c]);
       }
     }
     quad_sum3(acc);
@@ -434,8 +497,8 @@ __device__ __forceinline__ void mgq_restrict(const cpfem_mg_t& mg, const MgArray
 }
 
 // X_l += P X_{l+1} at the nodes a = first, first + step, ... (masked on Dirichlet dofs of
-// level 0).
-template <typename R>
+// level 0).  SH: Xc is in shared memory.
+template <bool SH, typename R>
 __device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, R* X, const R* Xc, int64_t first,
                                            int64_t step) {
   const int32_t* df = mg.dims[l];
@@ -447,12 +510,20 @@ __device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, R* X, co
     const int nxc = (ix & 1) + 1, nyc = (iy & 1) + 1, nzc = (iz & 1) + 1;
     const R w = ((ix & 1) ? R(0.5) : R(1)) * ((iy & 1) ? R(0.5) : R(1)) * ((iz & 1) ? R(0.5) : R(1));
     R acc[3] = {R(0), R(0), R(0)};
-    for (int kz = 0; kz < nzc; ++kz)
-      for (int ky = 0; ky < nyc; ++ky)
-        for (int kx = 0; kx < nxc; ++kx) {
-          const int64_t I = (cx0 + kx) + (int64_t)dc[0] * ((cy0 + ky) + (int64_t)dc[1] * (cz0 + kz));
+    // the 1, 2, 4 or 8 coarse parents, unrolled over 2x2x2 and predicated (an absent one
+    // reads its first parent with weight 0), so all their loads are in flight together
 #pragma unroll
-          for (int c = 0; c < 3; ++c) acc[c] = mad(w, __ldcg(&Xc[3 * I + c]), acc[c]);
+    for (int kz = 0; kz < 2; ++kz)
+#pragma unroll
+      for (int ky = 0; ky < 2; ++ky)
+#pragma unroll
+        for (int kx = 0; kx < 2; ++kx) {
+          const bool in = kx < nxc && ky < nyc && kz < nzc;
+          const int64_t I = (cx0 + (in ? kx : 0)) +
+                            (int64_t)dc[0] * ((cy0 + (in ? ky : 0)) + (int64_t)dc[1] * (cz0 + (in ? kz : 0)));
+          const R wk = in ? w : R(0);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) acc[c] = mad(wk, ldv<SH>(&Xc[3 * I + c]), acc[c]);
         }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -464,26 +535,158 @@ __device__ __forceinline__ void mg_prolong(const cpfem_mg_t& mg, int l, R* X, co
 
 constexpr int64_t kMgLocalNodes = 256;   // default: levels this small run inside block 0
 
+// The first block-local level: the coarsest levels, from level 2 on, with at most
+// local_nodes nodes (host and device agree on it).
+__host__ __device__ inline int mg_first_local(const cpfem_mg_t& mg) {
+  const int64_t local_nodes = mg.local_nodes > 0 ? (int64_t)mg.local_nodes : kMgLocalNodes;
+  int lb = mg.num_levels;
+  for (int l = mg.num_levels - 1; l >= 2 && mg.sell[l].num_nodes <= local_nodes; --l) lb = l;
+  return lb;
+}
+
+constexpr size_t kMgMaxLocalBytes = 220 * 1024; // shared memory of the block-local levels, at most
+constexpr size_t kMgStageBytes = kMgMaxLocalBytes;   // ... also when it holds staged operators
+
+// Shared memory of the block-local levels, in elements of R: x, t, r, b of each level (3
+// values per node) and, when everything fits in kMgStageBytes and the V-cycle is FP32, the
+// levels' operators (sliced-ELL, at most kMgMaxWidth slots per node) and inverse diagonal
+// blocks, staged once per launch.  Host and device derive the same layout.
+struct MgShared {
+  size_t vec[CPFEM_MG_MAX_LEVELS];
+  size_t val[CPFEM_MG_MAX_LEVELS];
+  size_t minv[CPFEM_MG_MAX_LEVELS];
+  size_t idx[CPFEM_MG_MAX_LEVELS];   // int32: group offsets, group widths, columns, transposed slots
+  size_t total;
+  bool staged;
+};
+
+// int32 entries of a staged level's layout: ng+1 group offsets, ng widths, and the column
+// and transposed-slot tables of 32 * kMgMaxWidth slots per group
+__host__ __device__ inline size_t mg_idx_words(int32_t ng) { return 2 * (size_t)ng + 1 + 2 * 32 * (size_t)kMgMaxWidth * ng; }
+
+__host__ __device__ inline MgShared mg_shared_layout(const cpfem_mg_t& mg, size_t real_bytes) {
+  MgShared s{};
+  const int lb = mg_first_local(mg);
+  size_t off = 0;
+  for (int m = lb; m < mg.num_levels; ++m) {
+    s.vec[m] = off;
+    off += 12 * (size_t)mg.sell[m].num_nodes;
+  }
+  size_t off_v = off;
+  for (int m = lb; m < mg.num_levels; ++m) {
+    s.val[m] = off_v;
+    off_v += 9 * 32 * (size_t)kMgMaxWidth * (size_t)mg.sell[m].num_groups;
+    s.minv[m] = off_v;
+    off_v += 9 * (size_t)mg.sell[m].num_nodes;
+    s.idx[m] = off_v;   // in 4-byte words, which the staged (FP32) layout's elements are
+    off_v += mg_idx_words(mg.sell[m].num_groups);
+  }
+  s.staged = real_bytes == sizeof(float) && lb < mg.num_levels && off_v * real_bytes <= kMgStageBytes;
+  s.total = (s.staged ? off_v : off) * real_bytes;
+  return s;
+}
+
+extern __shared__ __align__(16) unsigned char mg_shared[];
+
+// Block 0, once per launch: the block-local levels' operators and inverse diagonal blocks
+// to shared memory (when the layout stages them).
+// Returns whether they were staged (every level within kMgMaxWidth slots per node).
+template <typename R>
+__device__ bool mg_stage(const cpfem_mg_t& mg, const MgArrays<R>& A, const MgShared& lay) {
+  if (!lay.staged) return false;
+  for (int m = mg_first_local(mg); m < mg.num_levels; ++m)
+    if (mg.sell[m].group_off[mg.sell[m].num_groups] > 32 * (int64_t)kMgMaxWidth * mg.sell[m].num_groups) return false;
+  R* sh = reinterpret_cast<R*>(mg_shared);
+  for (int m = mg_first_local(mg); m < mg.num_levels; ++m) {
+    const cpfem_sell_t& S = mg.sell[m];
+    const int64_t nv = 9 * S.group_off[S.num_groups];
+    const R* V = A.values(m);
+    const R* Mi = A.minv(m);
+    for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) sh[lay.val[m] + i] = V[i];
+    for (int64_t i = threadIdx.x; i < 9 * (int64_t)S.num_nodes; i += blockDim.x) sh[lay.minv[m] + i] = Mi[i];
+    int* ix = reinterpret_cast<int*>(sh + lay.idx[m]);
+    const int ng = S.num_groups;
+    const int64_t ns = S.group_off[ng];
+    int* cols = ix + 2 * ng + 1;
+    int* tpos = cols + 32 * kMgMaxWidth * ng;
+    for (int64_t i = threadIdx.x; i <= ng; i += blockDim.x) ix[i] = (int)S.group_off[i];
+    for (int64_t i = threadIdx.x; i < ng; i += blockDim.x) ix[ng + 1 + i] = S.group_width[i];
+    for (int64_t i = threadIdx.x; i < ns; i += blockDim.x) {
+      cols[i] = S.cols[i];
+      tpos[i] = (S.tpos != nullptr) ? S.tpos[i] : 0;
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// Block 0: the block-local levels lb .. L-1 on its shared memory -- restriction of the
+// grid-wide level lb-1's residual, down sweeps, the coarsest level, up sweeps -- and level
+// lb's iterate copied to the global array the grid-wide prolongation reads.  SHV: the
+// operators were staged (mg_stage); otherwise they are read from global memory.
+template <bool TRANS, bool SHV, typename R>
+__device__ void mg_local_cycle(const cpfem_mg_t& mg, const MgArrays<R>& A, const MgShared& lay, int lb,
+                               const R* Res, const bool* down_t, const bool* up_t, int q) {
+  const int L = mg.num_levels;
+  const int64_t tqb = threadIdx.x >> 2, sqb = blockDim.x >> 2;   // block-local quads
+  R* sh = reinterpret_cast<R*>(mg_shared);
+  auto vec = [&](int m, int k) { return sh + lay.vec[m] + (size_t)k * 3 * mg.sell[m].num_nodes; };  // x t r b
+  auto V = [&](int m) { return SHV ? (const R*)(sh + lay.val[m]) : A.values(m); };
+  auto Mi = [&](int m) { return SHV ? (const R*)(sh + lay.minv[m]) : A.minv(m); };
+  auto Ix = [&](int m) { return SHV ? reinterpret_cast<const int*>(sh + lay.idx[m]) : (const int*)nullptr; };
+  mgq_restrict<false>(mg, lb - 1, Res, vec(lb, 3), tqb, sqb, q);
+  for (int m = lb; m < L; ++m) {
+    R* Xm = vec(m, 0);
+    R* Tm = vec(m, 1);
+    mgq_first_sweep<TRANS>(mg, Mi(m), m, Xm, vec(m, 3), tqb, sqb, q);
+    const int nswm = (m == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
+    for (int k = 1; k < nswm; ++k) {
+      __syncthreads();
+      mgq_apply<TRANS, true, SHV>(mg, V(m), Mi(m), m, Xm, Tm, vec(m, 3), false, tqb, sqb, q, Ix(m));
+      R* tmp = Xm; Xm = Tm; Tm = tmp;
+    }
+    if (m == L - 1) break;
+    __syncthreads();
+    mgq_apply<TRANS, true, SHV>(mg, V(m), Mi(m), m, Xm, vec(m, 2), vec(m, 3), true, tqb, sqb, q, Ix(m));
+    __syncthreads();
+    mgq_restrict<true>(mg, m, vec(m, 2), vec(m + 1, 3), tqb, sqb, q);
+  }
+  for (int m = L - 2; m >= lb; --m) {
+    R* Xm = down_t[m] ? vec(m, 1) : vec(m, 0);
+    R* Tm = down_t[m] ? vec(m, 0) : vec(m, 1);
+    const R* Xc = (m + 1 == L - 1 ? down_t[m + 1] : up_t[m + 1]) ? vec(m + 1, 1) : vec(m + 1, 0);
+    __syncthreads();
+    if (q == 0) mg_prolong<true>(mg, m, Xm, Xc, tqb, sqb);
+    for (int k = 0; k < mg.post_sweeps; ++k) {
+      __syncthreads();
+      mgq_apply<TRANS, true, SHV>(mg, V(m), Mi(m), m, Xm, Tm, vec(m, 3), false, tqb, sqb, q, Ix(m));
+      R* tmp = Xm; Xm = Tm; Tm = tmp;
+    }
+  }
+  const bool in_t = (lb == L - 1) ? down_t[lb] : up_t[lb];
+  const R* src = in_t ? vec(lb, 1) : vec(lb, 0);
+  R* dst = in_t ? A.t(lb) : A.x(lb);
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < 3 * mg.sell[lb].num_nodes; i += blockDim.x) dst[i] = src[i];
+}
+
 // One V-cycle out = M^-1 in over every block of the cooperative launch, in precision R
 // (in and out are the FP64 Krylov vectors).  Level 0 uses the caller's one-thread-per-node
 // grid-stride mapping (so input written by this thread needs no barrier); coarser levels
 // give every node a quad of lanes, so their few nodes still hide load latency.  The levels
-// (from level 2 on) with at most local_nodes nodes run inside block 0 with block barriers
-// while the other blocks wait at the next grid barrier.  Which of x / t holds a level's
-// iterate follows from the sweep counts alone, so every block knows it.  Returns with out
-// complete for this thread's own nodes.
+// (from level 2 on) with at most local_nodes nodes run inside block 0 on vectors in its
+// shared memory (mg_local_cycle), while the other blocks wait at the next grid barrier.
+// Which of x / t holds a level's iterate follows from the sweep counts alone, so every
+// block knows it.  Returns with out complete for this thread's own nodes.
 template <bool TRANS, typename R>
 __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0, const double* in, double* out,
-                          int64_t t0, int64_t stride, GridSync* gs, unsigned int& gen, bool& ok) {
+                          int64_t t0, int64_t stride, GridSync* gs, unsigned int& gen, bool& ok, bool staged) {
   const MgArrays<R> A{mg, vals0};
   const int L = mg.num_levels;
   const R om = (R)mg.omega;
   const int64_t tq = t0 >> 2, sq = stride >> 2;
   const int q = (int)(t0 & 3);
-  const int64_t tqb = threadIdx.x >> 2, sqb = blockDim.x >> 2;   // block-local quads
-  const int64_t local_nodes = mg.local_nodes > 0 ? (int64_t)mg.local_nodes : kMgLocalNodes;
-  int lb = L;                                                    // first block-local level
-  for (int l = L - 1; l >= 2 && mg.sell[l].num_nodes <= local_nodes; --l) lb = l;
+  const int lb = mg_first_local(mg);                             // first block-local level
   // where each level's iterate lives after its down sweeps / after its up sweeps
   bool down_t[CPFEM_MG_MAX_LEVELS], up_t[CPFEM_MG_MAX_LEVELS];
   for (int l = 0; l < L; ++l) {
@@ -495,26 +698,27 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
   for (int l = 0; l < lb; ++l) {
     const cpfem_sell_t& S = mg.sell[l];
     const R* V = A.values(l);
+    const R* Mi = A.minv(l);
     R* X = A.x(l);
     R* T = A.t(l);
     const int64_t n = S.num_nodes;
     if (l == 0) {
       for (int64_t a = t0; a < n; a += stride) {
         R v[3] = {(R)in[3 * a], (R)in[3 * a + 1], (R)in[3 * a + 2]}, z[3];
-        mg_apply_minv<TRANS>(A.minv(0), a, v, z);
+        mg_apply_minv<TRANS>(Mi, a, v, z);
 #pragma unroll
         for (int i = 0; i < 3; ++i) X[3 * a + i] = om * z[i];
       }
     } else {
-      mgq_first_sweep<TRANS>(mg, A, l, X, tq, sq, q);
+      mgq_first_sweep<TRANS>(mg, Mi, l, X, A.b(l), tq, sq, q);
     }
     const int nsw = (l == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
     for (int k = 1; k < nsw; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, V, A.minv(0), in, X, T, om, a);
+        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, V, Mi, in, X, T, om, a);
       } else {
-        mgq_apply<TRANS>(mg, A, l, X, T, false, tq, sq, q);
+        mgq_apply<TRANS, false>(mg, V, Mi, l, X, T, A.b(l), false, tq, sq, q);
       }
       R* tmp = X; X = T; T = tmp;
     }
@@ -532,42 +736,15 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
         }
       }
     } else {
-      mgq_apply<TRANS>(mg, A, l, X, Res, true, tq, sq, q);
+      mgq_apply<TRANS, false>(mg, V, Mi, l, X, Res, A.b(l), true, tq, sq, q);
     }
     ok = grid_barrier(gs, gen) && ok;
     if (l + 1 < lb) {
-      mgq_restrict(mg, A, l, Res, tq, sq, q);
+      mgq_restrict<false>(mg, l, Res, A.b(l + 1), tq, sq, q);
     } else if (blockIdx.x == 0) {
-      // ---- block-local levels lb .. L-1: down, coarsest, up to lb
-      mgq_restrict(mg, A, l, Res, tqb, sqb, q);
-      for (int m = lb; m < L; ++m) {
-        R* Xm = A.x(m);
-        R* Tm = A.t(m);
-        mgq_first_sweep<TRANS>(mg, A, m, Xm, tqb, sqb, q);
-        const int nswm = (m == L - 1) ? mg.coarse_sweeps : mg.pre_sweeps;
-        for (int k = 1; k < nswm; ++k) {
-          __syncthreads();
-          mgq_apply<TRANS>(mg, A, m, Xm, Tm, false, tqb, sqb, q);
-          R* tmp = Xm; Xm = Tm; Tm = tmp;
-        }
-        if (m == L - 1) break;
-        __syncthreads();
-        mgq_apply<TRANS>(mg, A, m, Xm, A.r(m), true, tqb, sqb, q);
-        __syncthreads();
-        mgq_restrict(mg, A, m, A.r(m), tqb, sqb, q);
-      }
-      for (int m = L - 2; m >= lb; --m) {
-        R* Xm = down_t[m] ? A.t(m) : A.x(m);
-        R* Tm = down_t[m] ? A.x(m) : A.t(m);
-        const R* Xc = (m + 1 == L - 1 ? down_t[m + 1] : up_t[m + 1]) ? A.t(m + 1) : A.x(m + 1);
-        __syncthreads();
-        if (q == 0) mg_prolong(mg, m, Xm, Xc, tqb, sqb);
-        for (int k = 0; k < mg.post_sweeps; ++k) {
-          __syncthreads();
-          mgq_apply<TRANS>(mg, A, m, Xm, Tm, false, tqb, sqb, q);
-          R* tmp = Xm; Xm = Tm; Tm = tmp;
-        }
-      }
+      const MgShared lay = mg_shared_layout(mg, sizeof(R));
+      if (staged) mg_local_cycle<TRANS, true>(mg, A, lay, lb, (const R*)Res, down_t, up_t, q);
+      else mg_local_cycle<TRANS, false>(mg, A, lay, lb, (const R*)Res, down_t, up_t, q);
     }
   }
   // ---- grid-wide levels lb-1 .. 0, up
@@ -575,18 +752,19 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     if (l == L - 1) continue;
     const cpfem_sell_t& S = mg.sell[l];
     const R* V = A.values(l);
+    const R* Mi = A.minv(l);
     R* X = down_t[l] ? A.t(l) : A.x(l);
     R* T = down_t[l] ? A.x(l) : A.t(l);
     const R* Xc = (l + 1 == L - 1 ? down_t[l + 1] : up_t[l + 1]) ? A.t(l + 1) : A.x(l + 1);
     ok = grid_barrier(gs, gen) && ok;
-    if (l == 0) mg_prolong(mg, 0, X, Xc, t0, stride);
-    else if (q == 0) mg_prolong(mg, l, X, Xc, tq, sq);
+    if (l == 0) mg_prolong<false>(mg, 0, X, Xc, t0, stride);
+    else if (q == 0) mg_prolong<false>(mg, l, X, Xc, tq, sq);
     for (int k = 0; k < mg.post_sweeps; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, V, A.minv(0), in, X, T, om, a);
+        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, V, Mi, in, X, T, om, a);
       } else {
-        mgq_apply<TRANS>(mg, A, l, X, T, false, tq, sq, q);
+        mgq_apply<TRANS, false>(mg, V, Mi, l, X, T, A.b(l), false, tq, sq, q);
       }
       R* tmp = X; X = T; T = tmp;
     }
@@ -618,6 +796,11 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
     return p;
   };
   bool ok = true;
+  bool staged = false;
+  if constexpr (MG) {
+    // block 0 keeps the block-local levels' operators in shared memory for the whole solve
+    if (blockIdx.x == 0) staged = mg_stage<MgReal>(mg, MgArrays<MgReal>{mg, vals}, mg_shared_layout(mg, sizeof(MgReal)));
+  }
 
   // r = b - A x0 ; rhat = p = q = r
   double v2[2] = {0.0, 0.0};
@@ -657,7 +840,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
         for (int i = 0; i < 3; ++i) w.phat[3 * a + i] = ph[i];
       }
     }
-    if constexpr (MG) mg_vcycle<TRANS, MgReal>(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok);
+    if constexpr (MG) mg_vcycle<TRANS, MgReal>(mg, vals, w.p, w.phat, t0, stride, w.sync, gen, ok, staged);
     ok = grid_barrier(w.sync, gen) && ok;
     // q = A phat ; alpha = rho_new / (rhat . q)
     double v1[1] = {0.0};
@@ -694,7 +877,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
       ok = grid_reduce<1>(vs, parts(), w.sync, gen, smem, bcast) && ok;   // also the shat halo barrier
     } else {
       // the V-cycle starts on this thread's own s; s.s joins the t reduction below
-      mg_vcycle<TRANS, MgReal>(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok);
+      mg_vcycle<TRANS, MgReal>(mg, vals, w.s, w.shat, t0, stride, w.sync, gen, ok, staged);
       ok = grid_barrier(w.sync, gen) && ok;
     }
     // t = A shat ; omega = (t.s)/(t.t)
@@ -787,13 +970,14 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
   }
 }
 
-static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms) {
+static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms, size_t dyn_smem = 0) {
   int dev = 0;
   CPFEM_CUDA_TRY(cudaGetDevice(&dev));
   CPFEM_CUDA_TRY(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
-  CPFEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kPThreads, 0));
+  CPFEM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kPThreads, dyn_smem));
   return CPFEM_OK;
 }
+
 
 template <bool TRANS>
 static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double* b, double* x, int precond,
@@ -813,7 +997,16 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   const void* kfn = (precond != 3)      ? (const void*)k_bicgstab<TRANS, 0>
                     : (mg.precision == 1) ? (const void*)k_bicgstab<TRANS, 2>
                                           : (const void*)k_bicgstab<TRANS, 1>;
-  int rc = sm_count_and_blocks(kfn, &per_sm, &sms);
+  size_t dyn = 0;
+  if (precond == 3) {
+    dyn = mg_shared_layout(mg, mg.precision == 1 ? sizeof(float) : sizeof(double)).total;
+    if (dyn > kMgMaxLocalBytes) {
+      set_error("multigrid local_nodes too large: the block-local levels do not fit in shared memory");
+      return CPFEM_ERR_ARG;
+    }
+    if (dyn > 48 * 1024) CPFEM_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  }
+  int rc = sm_count_and_blocks(kfn, &per_sm, &sms, dyn);
   if (rc) return rc;
   if (per_sm < 1) {
     set_error("persistent BiCGSTAB kernel cannot be resident");
@@ -829,7 +1022,7 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   double tl = tol, at = atol;
   int mi = maxiter, mr = max_restarts;
   void* args[] = {&Lc, &vals, &bb, &xx, &w, &pc, &tl, &at, &mi, &mr, &mg};
-  CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3((unsigned)blocks), dim3(kPThreads), args, 0, s));
+  CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3((unsigned)blocks), dim3(kPThreads), args, dyn, s));
   SolveOut out;
   CPFEM_CUDA_TRY(cudaMemcpyAsync(&out, w.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, s));
   CPFEM_CUDA_TRY(cudaStreamSynchronize(s));
