@@ -101,8 +101,14 @@ typedef struct {
                                  of each listed cell; every output of other GPs is left
                                  untouched (a ragged batch skips its converged instances) */
   int32_t num_listed;
-  int32_t warm_mode;          /* with s_warm: 0 start there; 1 start at the linear prediction
-                                 s_warm + ds/dF : (F - s_f) (needs s_dsdf and s_f) */
+  int32_t local_flags;        /* local Newton options, OR-ed bits:
+                                 1 (with s_warm, s_dsdf, s_f): start at the linear prediction
+                                   s_warm + ds/dF : (F - s_f) instead of at s_warm;
+                                 2: Newton directions from an FP32 Jacobian / LU while the
+                                   Jacobian's scale max_a d(dgamma_a)/d(tau_a) C11 <= 1e4
+                                   (else FP64); the residual, its stop test and the tangent
+                                   stay FP64, so the converged state is the same root.
+                                 0 with s_warm = NULL: the reference's iterates. */
   const int32_t* order;       /* [num_gp] permutation or NULL (no cell list): thread t
                                  evaluates GP order[t].  Ordering GPs by their previous
                                  local-Newton iteration count keeps a warp's lanes busy for

@@ -67,7 +67,7 @@ class GPArgs(ctypes.Structure):
         ("status", ctypes.c_void_p),
         ("cell_list", ctypes.c_void_p),
         ("num_listed", ctypes.c_int32),
-        ("warm_mode", ctypes.c_int32),
+        ("local_flags", ctypes.c_int32),
         ("order", ctypes.c_void_p),
         ("s_warm", ctypes.c_void_p),
         ("s_dsdf", ctypes.c_void_p),

@@ -44,6 +44,11 @@ int make_matdev(const cpfem_material_t* m, MatDev* o) {
     o->pv[a][3] = d[1] * n[2] + d[2] * n[1];
     o->pv[a][4] = d[0] * n[2] + d[2] * n[0];
     o->pv[a][5] = d[0] * n[1] + d[1] * n[0];
+    for (int i = 0; i < 3; ++i) {
+      o->d32[a][i] = (float)o->d[a][i];
+      o->n32[a][i] = (float)o->n[a][i];
+    }
+    for (int k = 0; k < 6; ++k) o->pv32[a][k] = (float)o->pv[a][k];
   }
   return CPFEM_OK;
 }
@@ -131,7 +136,7 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
     double s0[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) s0[k] = a.s_warm[k * G + gp];
-    if (predict && a.warm_mode == 1) {
+    if (predict && (a.local_flags & 1)) {
       // first-order prediction from where s_warm converged: s0 += ds/dF : (F - F_then)
 #pragma unroll
       for (int kl = 0; kl < 9; ++kl) {
@@ -140,7 +145,7 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
         for (int k = 0; k < 6; ++k) s0[k] = fma(a.s_dsdf[(6 * kl + k) * G + gp], dF, s0[k]);
       }
     }
-    cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st, s0);
+    cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st, s0, (a.local_flags & 2) != 0);
     if (st.rn <= m.local_tol) {
 #pragma unroll
       for (int k = 0; k < 6; ++k) a.s_warm[k * G + gp] = st.s[k];
@@ -149,7 +154,7 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
         for (int kl = 0; kl < 9; ++kl) a.s_f[kl * G + gp] = F[kl];
     }
   } else {
-    cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st);
+    cp_local_newton<NS>(m, cc, Ct, ig, m.ao * a.dt, 1.0 / xm, st, nullptr, (a.local_flags & 2) != 0);
   }
   if (a.status != nullptr) {
     int bits = 0;

@@ -47,6 +47,9 @@ struct MatDev {
   double n[CPFEM_MAX_SLIP][3];   // slip-plane normal, lattice frame
   double pv[CPFEM_MAX_SLIP][6];  // P = d n^T as (P11,P22,P33,P23+P32,P13+P31,P12+P21)
   double p9[CPFEM_MAX_SLIP][9];  // P = d n^T row-major
+  float d32[CPFEM_MAX_SLIP][3];  // FP32 copies for the local Newton's FP32 direction
+  float n32[CPFEM_MAX_SLIP][3];
+  float pv32[CPFEM_MAX_SLIP][6];
 };
 
 int make_matdev(const cpfem_material_t* m, MatDev* out);
@@ -124,19 +127,25 @@ CPFEM_HD void cubic_apply(const Cub& m, const double* e, double* t) {
   t[5] = c2 * e[5];
 }
 
-// In-register LU with partial pivoting of an n x n matrix; all indices are static so
-// the matrix stays in registers.  Row swaps are done with predicated exchanges.
-template <int n>
-CPFEM_HD void lu_factor(double* A, int* perm, double* dinv) {
+CPFEM_HD double cp_fma(double a, double b, double c) { return fma(a, b, c); }
+CPFEM_HD float cp_fma(float a, float b, float c) { return fmaf(a, b, c); }
+CPFEM_HD double cp_abs(double a) { return fabs(a); }
+CPFEM_HD float cp_abs(float a) { return fabsf(a); }
+
+// In-register LU with partial pivoting of an n x n matrix (FP64, or FP32 for a Newton
+// direction that need not be exact); all indices are static so the matrix stays in
+// registers.  Row swaps are done with predicated exchanges.
+template <int n, typename T>
+CPFEM_HD void lu_factor(T* A, int* perm, T* dinv) {
 #pragma unroll
   for (int i = 0; i < n; ++i) perm[i] = i;
 #pragma unroll
   for (int k = 0; k < n; ++k) {
     int p = k;
-    double best = fabs(A[k * n + k]);
+    T best = cp_abs(A[k * n + k]);
 #pragma unroll
     for (int i = k + 1; i < n; ++i) {
-      const double v = fabs(A[i * n + k]);
+      const T v = cp_abs(A[i * n + k]);
       if (v > best) { best = v; p = i; }
     }
 #pragma unroll
@@ -144,7 +153,7 @@ CPFEM_HD void lu_factor(double* A, int* perm, double* dinv) {
       if (p == i) {
 #pragma unroll
         for (int j = 0; j < n; ++j) {
-          const double t = A[k * n + j];
+          const T t = A[k * n + j];
           A[k * n + j] = A[i * n + j];
           A[i * n + j] = t;
         }
@@ -153,25 +162,25 @@ CPFEM_HD void lu_factor(double* A, int* perm, double* dinv) {
         perm[i] = t;
       }
     }
-    const double inv = 1.0 / A[k * n + k];
+    const T inv = T(1) / A[k * n + k];
     dinv[k] = inv;
 #pragma unroll
     for (int i = k + 1; i < n; ++i) {
-      const double l = A[i * n + k] * inv;
+      const T l = A[i * n + k] * inv;
       A[i * n + k] = l;
 #pragma unroll
-      for (int j = k + 1; j < n; ++j) A[i * n + j] = fma(-l, A[k * n + j], A[i * n + j]);
+      for (int j = k + 1; j < n; ++j) A[i * n + j] = cp_fma(-l, A[k * n + j], A[i * n + j]);
     }
   }
 }
 
 // Solve with the factors of lu_factor; b is overwritten by x.
-template <int n>
-CPFEM_HD void lu_solve(const double* LU, const int* perm, const double* dinv, double* b) {
-  double y[n];
+template <int n, typename T>
+CPFEM_HD void lu_solve(const T* LU, const int* perm, const T* dinv, T* b) {
+  T y[n];
 #pragma unroll
   for (int i = 0; i < n; ++i) {
-    double v = 0.0;
+    T v = T(0);
 #pragma unroll
     for (int j = 0; j < n; ++j) v = (perm[i] == j) ? b[j] : v;
     y[i] = v;
@@ -179,11 +188,11 @@ CPFEM_HD void lu_solve(const double* LU, const int* perm, const double* dinv, do
 #pragma unroll
   for (int i = 0; i < n; ++i)
 #pragma unroll
-    for (int j = 0; j < i; ++j) y[i] = fma(-LU[i * n + j], y[j], y[i]);
+    for (int j = 0; j < i; ++j) y[i] = cp_fma(-LU[i * n + j], y[j], y[i]);
 #pragma unroll
   for (int i = n - 1; i >= 0; --i) {
 #pragma unroll
-    for (int j = i + 1; j < n; ++j) y[i] = fma(-LU[i * n + j], y[j], y[i]);
+    for (int j = i + 1; j < n; ++j) y[i] = cp_fma(-LU[i * n + j], y[j], y[i]);
     y[i] = y[i] * dinv[i];
   }
 #pragma unroll

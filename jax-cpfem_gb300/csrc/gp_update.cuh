@@ -135,6 +135,57 @@ CPFEM_HD void cp_jacobian(const MatDev& m, const Cub& cc, const double* kk, cons
   }
 }
 
+// The same Jacobian in FP32, for a Newton direction only (the residual, the stop test and
+// the tangent stay FP64).  Used while the Jacobian's scale max_a kk_a C11 is at most
+// kJ32Scale, where FP32 rounding leaves the direction accurate to ~1e-4 or better.
+constexpr double kJ32Scale = 1e4;
+
+template <int NS>
+CPFEM_HD void cp_jacobian_f32(const MatDev& m, const Cub& cc, const double* kk, const double* M, float* J) {
+  float Mf[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Mf[k] = (float)M[k];
+  float* Q = J;
+#pragma unroll
+  for (int i = 0; i < 36; ++i) Q[i] = 0.0f;
+#pragma unroll
+  for (int a = 0; a < NS; ++a) {
+    const float* d = m.d32[a];
+    const float* n = m.n32[a];
+    float w[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) w[i] = fmaf(Mf[i], d[0], fmaf(Mf[3 + i], d[1], Mf[6 + i] * d[2]));
+    float q[6];
+    q[0] = w[0] * n[0];
+    q[1] = w[1] * n[1];
+    q[2] = w[2] * n[2];
+    q[3] = 0.5f * fmaf(w[1], n[2], w[2] * n[1]);
+    q[4] = 0.5f * fmaf(w[0], n[2], w[2] * n[0]);
+    q[5] = 0.5f * fmaf(w[0], n[1], w[1] * n[0]);
+    const float ka = (float)kk[a];
+    float c[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) c[j] = ka * m.pv32[a][j];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) Q[6 * i + j] = fmaf(q[i], c[j], Q[6 * i + j]);
+  }
+  const float c11 = (float)cc.C11, c12 = (float)cc.C12, c44x2 = (float)(2.0 * cc.C44);
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const float e0 = Q[j], e1 = Q[6 + j], e2 = Q[12 + j];
+    const float t0 = fmaf(c11, e0, c12 * (e1 + e2));
+    const float t1 = fmaf(c11, e1, c12 * (e0 + e2));
+    const float t2 = fmaf(c11, e2, c12 * (e0 + e1));
+    J[j] = (j == 0 ? 1.0f : 0.0f) + t0;
+    J[6 + j] = (j == 1 ? 1.0f : 0.0f) + t1;
+    J[12 + j] = (j == 2 ? 1.0f : 0.0f) + t2;
+#pragma unroll
+    for (int i = 3; i < 6; ++i) J[6 * i + j] = (i == j ? 1.0f : 0.0f) + c44x2 * Q[6 * i + j];
+  }
+}
+
 constexpr int kWarmStartIters = 8;   // a warm start still unconverged after this restarts from 0
 
 // Local Newton with the cut-half line search of models_copper.py:218-245: trial
@@ -149,7 +200,7 @@ constexpr int kWarmStartIters = 8;   // a warm start still unconverged after thi
 template <int NS>
 CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, const double* ig,
                                                 double cdt, double pexp, GPSolve<NS>& st,
-                                                const double* s_init = nullptr) {
+                                                const double* s_init = nullptr, bool j32 = false) {
   const int ie1 = int_exponent(pexp - 1.0);
   double r[6];
   bool warm = s_init != nullptr;
@@ -169,14 +220,37 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, 
       warm = false;
       it0 = it + 1;
     } else {
-      double J[36];
-      int perm[6];
-      double dinv[6];
-      cp_jacobian<NS>(m, cc, st.kk, st.M, J);
-      lu_factor<6>(J, perm, dinv);
+      bool done = false;
+      if (j32) {
+        double kmax = 0.0;
 #pragma unroll
-      for (int k = 0; k < 6; ++k) ds[k] = -r[k];
-      lu_solve<6>(J, perm, dinv, ds);
+        for (int a = 0; a < NS; ++a) kmax = fmax(kmax, st.kk[a]);
+        if (kmax * cc.C11 <= kJ32Scale) {
+          float J[36], dinv[6], d32[6];
+          int perm[6];
+          cp_jacobian_f32<NS>(m, cc, st.kk, st.M, J);
+          lu_factor<6>(J, perm, dinv);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) d32[k] = (float)(-r[k]);
+          lu_solve<6>(J, perm, dinv, d32);
+          done = true;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            ds[k] = (double)d32[k];
+            done = done && isfinite(ds[k]);
+          }
+        }
+      }
+      if (!done) {
+        double J[36];
+        int perm[6];
+        double dinv[6];
+        cp_jacobian<NS>(m, cc, st.kk, st.M, J);
+        lu_factor<6>(J, perm, dinv);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ds[k] = -r[k];
+        lu_solve<6>(J, perm, dinv, ds);
+      }
     }
     const double rn0 = sub_cap == 1 ? 0.0 : st.rn;
     double relax = 1.0;

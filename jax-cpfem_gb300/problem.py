@@ -211,6 +211,9 @@ class CrystalPlasticity:
         # ... moved to first order along F: s_warm + ds/dF (F - F_warm), with the ds/dF of the
         # last tangent pass (no effect on the result, fewer local iterations)
         self.predict_local = True
+        # Newton directions of the local solve from an FP32 Jacobian while its scale allows
+        # (same residual, stop test and tangent in FP64: same converged state)
+        self.fp32_local_jacobian = True
         self.custom_init(*additional_info)
 
     # ------------------------------------------------------------------ set-up
@@ -593,7 +596,11 @@ class CrystalPlasticity:
         return [dofs.reshape(self.num_nodes, 3)]
 
     # ------------------------------------------------------------------ GPU passes
-    def _gp_args(self, state, dt, u=None, u_grad=None, num_gp=None, elastic=None, warm_mode=0, **outs):
+    def _gp_args(self, state, dt, u=None, u_grad=None, num_gp=None, elastic=None, predict=False, fast_local=False,
+                 **outs):
+        """cpfem_gp_args_t of one constitutive pass.  predict: start the local Newton at the
+        linear prediction (needs the warm-start arrays); fast_local: FP32 Newton directions
+        (the problem's ``fp32_local_jacobian`` decides)."""
         a = _capi.GPArgs()
         fpi, g, slip, rot_table, rot_idx, param_table, param_idx = state
         a.num_gp = self.num_gp if num_gp is None else num_gp
@@ -612,7 +619,7 @@ class CrystalPlasticity:
         else:
             a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
         a.weight_jxw = 1 if outs.pop("weight_jxw", False) else 0
-        a.warm_mode = int(warm_mode)
+        a.local_flags = (1 if predict else 0) | (2 if (fast_local and self.fp32_local_jacobian) else 0)
         cl = outs.pop("cell_list", None)
         if cl is not None:
             a.cell_list, a.num_listed = _dev_ptr(cl), int(cl.numel())
@@ -650,7 +657,7 @@ class CrystalPlasticity:
             token, count = getattr(self, "_tangent_passes", (None, 0))
             if token != self._state_token:
                 count = 0
-            out["warm_mode"] = 1 if count >= 2 else 0
+            out["predict"] = count >= 2
             if tangent:
                 self._tangent_passes = (self._state_token, count + 1)
         return out
@@ -720,8 +727,8 @@ class CrystalPlasticity:
             trial = self.new_trial()
         trial = trial if with_trial else {}
         args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its, cell_list=cell_list, order=order, **self._warm_args(need_tangent),
-                             **trial)
+                             iters=its, cell_list=cell_list, order=order, fast_local=True,
+                             **self._warm_args(need_tangent), **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
         if ordered:
             # the next pass runs the GPs heaviest first, in runs of equal local-Newton counts
@@ -868,7 +875,7 @@ class CrystalPlasticity:
         status = self._buf("status", (1,), torch.int32)
         status.zero_()
         args = self._gp_args(self._state(), self.dt, u=u, stress=sw, fpi_new=fn, g_new=gn, slip_new=sn,
-                             status=status, weight_jxw=True, **self._warm_args())
+                             status=status, weight_jxw=True, fast_local=True, **self._warm_args())
         self._run_gp(args, "gp_eval_post")
         sig = torch.empty((self.num_cells, 3, 3), dtype=torch.float64, device=self.device)
         _capi.check(self.lib.cpfem_cell_average(self.num_cells, _dev_ptr(self.fes[0].JxW), _dev_ptr(sw),

@@ -116,3 +116,19 @@ def test_load_steps_with_warm_start_match_cold_and_oracle(pkg, gpu):
     s_o, u_o = O.run_load_steps(orc, disps, ts, bcf, {"tol": 1e-9, "rel_tol": 1e-12})
     assert np.abs(sw - s_o).max() / np.abs(s_o).max() < 1e-8
     assert np.abs(uw - u_o).max() / np.abs(u_o).max() < 1e-8
+
+
+def test_fp32_local_newton_direction_converges_to_the_same_root(pkg, gpu):
+    """Newton directions from the FP32 local Jacobian (the residual, stop test and tangent in
+    FP64): the pass agrees with the FP64-direction pass to the local tolerance, at about the
+    same iteration counts."""
+    problem_mod, _ = gpu
+    _, _, _, _, prob, u = _case(pkg, problem_mod)
+    prob.warm_start_local = False
+    prob.fp32_local_jacobian = False
+    r64, v64, i64 = _pass(prob, u)
+    prob.fp32_local_jacobian = True
+    r32, v32, i32 = _pass(prob, u)
+    assert float((r32 - r64).abs().max() / r64.abs().max()) < 1e-10
+    assert float((v32 - v64).abs().max() / v64.abs().max()) < 1e-9
+    assert float(i32.double().mean()) <= float(i64.double().mean()) + 0.5, (i32.double().mean(), i64.double().mean())
