@@ -253,21 +253,23 @@ def krylov_iteration_cost(prob, precond=1):
     return bytes_it, flops_it, flops32_it
 
 
-def gp_flops_per_eval(num_slip, iters_mean, tangent=True):
-    """Algorithmic FP64 flops of one GP update (FMA = 2; pow, div, sqrt = 1 each):
-    per local iteration one residual (tau 12N, power/slip 6N, L_p 18N, 3x3 products and
-    strain 130) + one 6x6 Jacobian (per slip M^T d 18, sym(. (x) n) 15, kk pv 6, rank-one
-    update 72; the cubic stiffness once on six columns, ~100) + LU/solve (~230); the
-    tangent adds a Jacobian + LU, 6 dP/ds directions (20N+220 each) and 9 columns (~220
-    each)."""
+def gp_flops_per_eval(num_slip, iters_mean, tangent=True, fp32_direction=True):
+    """Algorithmic flops of one GP update (FMA = 2; pow, div, sqrt = 1 each), returned as
+    (FP64, FP32): per local iteration one residual (tau 12N, power/slip 6N, L_p 18N, 3x3
+    products and strain 130) in FP64, and one 6x6 Jacobian (per slip M^T d 18,
+    sym(. (x) n) 15, kk pv 6, rank-one update 72; the cubic stiffness once on six columns,
+    ~100) + LU/solve (~230), in FP32 when the local Newton takes FP32 directions (counted
+    so for every iteration: a lower bound of the FP64 work); the tangent (FP64) adds a
+    Jacobian + LU, 6 dP/ds directions (20N+220 each) and 9 columns (~220 each)."""
     N = num_slip
     residual = 36 * N + 130
     jac = 111 * N + 100
     lu = 230
-    per_iter = residual + jac + lu
     setup = 120 + residual
     tan = (jac + lu + 6 * (20 * N + 220) + 9 * 220) if tangent else 0
-    return setup + iters_mean * per_iter + tan + 60
+    direction = iters_mean * (jac + lu)
+    fp64 = setup + iters_mean * residual + tan + 60 + (0 if fp32_direction else direction)
+    return fp64, (direction if fp32_direction else 0.0)
 
 
 def _oracle_pass_worker(job):
@@ -683,7 +685,8 @@ def main():
     its_t = prob.stats.get("local_iters_mean", 6.0)
     gp_n, gp_ms = regions.get("gp_eval_tangent", (0, 0.0))
     gp_t = gp_ms * 1e-3 / max(gp_n, 1)
-    gp_flops = G * gp_flops_per_eval(prob.num_slip, its_t)
+    gp64, gp32 = gp_flops_per_eval(prob.num_slip, its_t, fp32_direction=prob.fp32_local_jacobian)
+    gp_flops = G * gp64
     kr_n, kr_ms = regions.get("bicgstab", (0, 0.0))
     kr_its = sum(max(k, 0) for k in krylov)
     kb, kf, kf32 = krylov_iteration_cost(prob, args.precond)
@@ -717,7 +720,9 @@ def main():
                  "peak_source": "cpfem_probe_dfma FP64 (of measured); HBM from MEASURED_PEAKS.json (of measured)"}
     gp_roof = {"bound": "fp64", "achieved": gp_flops / gp_t / 1e12 if gp_t else None, "peak": fp64,
                "unit": "TFLOP/s", "frac": (gp_flops / gp_t / 1e12) / fp64 if gp_t else None, "traffic": None,
-               "kernel": "k_gp_eval<N,tangent>", "peak_source": "cpfem_probe_dfma (of measured)"}
+               "kernel": "k_gp_eval<N,tangent>", "peak_source": "cpfem_probe_dfma (of measured)",
+               "local_iters_mean": its_t, "fp64_flops_per_gp": gp64, "fp32_flops_per_gp": gp32,
+               "note": "FP64 flops counted with every local Newton direction in FP32 (a lower bound)"}
     shares = {"bicgstab": kr_ms / (t * 1e3), "gp_eval_tangent": gp_ms / (t * 1e3),
               "elem_assemble": regions.get("elem_assemble", (0, 0.0))[1] / (t * 1e3)}
     dominant = kr_roof if (kr_roof is not None and shares["bicgstab"] >= shares["gp_eval_tangent"]) else gp_roof
