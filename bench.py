@@ -215,7 +215,7 @@ def spmv_roofline(prob, torch, lib, reps=50):
 SPMV_DRAM_BYTES = {"c1": 72.4e6}
 # DRAM bytes of one k_bicgstab launch from ncu captures of the 32^3 bench matrix, by
 # (config, precond, V-cycle precision): Jacobi ~330 iterations, multigrid ~20-30
-KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 1, None): 75.7e6, ("c1", 3, "fp64"): 107.9e6, ("c1", 3, "fp32"): 3.662e9}
+KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 1, None): 75.7e6, ("c1", 3, "fp64"): 107.9e6, ("c1", 3, "fp32"): 3.684e9}
 
 
 def krylov_iteration_cost(prob, precond=1):
