@@ -89,9 +89,10 @@ __device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const R* __rest
   const int64_t c0 = L.group_off[g] + lane;
   const R* v0 = vals + 9 * L.group_off[g] + lane;
   const int w = L.group_width[g];
-  R a0 = R(0), a1 = R(0), a2 = R(0);
-#pragma unroll 3
-  for (int j = 0; j < w; ++j) {
+  // two accumulators per row (even / odd slots): six independent FMA chains keep the FP64
+  // pipe fed at one thread per node
+  R e0 = R(0), e1 = R(0), e2 = R(0), o0 = R(0), o1 = R(0), o2 = R(0);
+  auto slot = [&](int j, R& a0, R& a1, R& a2) {
     const int64_t b = __ldg(&L.cols[c0 + 32 * j]);
     R x0, x1, x2;
     if (COHERENT) {
@@ -112,10 +113,17 @@ __device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const R* __rest
       a1 = mad(__ldg(&vb[32]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[224]), x2, a1)));
       a2 = mad(__ldg(&vb[64]), x0, mad(__ldg(&vb[160]), x1, mad(__ldg(&vb[256]), x2, a2)));
     }
+  };
+  int j = 0;
+#pragma unroll 2
+  for (; j + 1 < w; j += 2) {
+    slot(j, e0, e1, e2);
+    slot(j + 1, o0, o1, o2);
   }
-  acc[0] = a0;
-  acc[1] = a1;
-  acc[2] = a2;
+  if (j < w) slot(j, e0, e1, e2);
+  acc[0] = e0 + o0;
+  acc[1] = e1 + o1;
+  acc[2] = e2 + o2;
 }
 
 template <bool TRANS>
