@@ -79,6 +79,7 @@ def _fp32_solve_ok(problem, A, b, x, converged, tol, atol):
     r = A.matvec(x)
     r.sub_(b)
     rn, bn = norm(problem, r), norm(problem, b)
+    problem._true_res = (x, b, rn)   # jax_solve's ||Ax - b|| check reuses it
     return math.isfinite(rn) and rn <= 10.0 * max(tol * bn, atol)
 
 
@@ -94,9 +95,14 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
                         atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000), restarts=rs,
                         mg_options=opts.get("mg_options"), grid_blocks=opts.get("grid_blocks", 0))
     problem.stats["krylov_iters"].append(k)
-    r = A.matvec(x)
-    r.sub_(b)
-    err = norm(problem, r)
+    last = getattr(problem, "_true_res", None)
+    if last is not None and last[0] is x and last[1] is b:
+        err = last[2]
+    else:
+        r = A.matvec(x)
+        r.sub_(b)
+        err = norm(problem, r)
+    problem._true_res = None
     if not err < 0.1:
         raise RuntimeError(f"linear solver failed to converge with err = {err} (iterations {k})")
     return x
