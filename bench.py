@@ -103,7 +103,7 @@ class Stepper:
 
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled every 200 ms.  Started before the
-    warm-up (its start-up stalls the driver for a moment), and summarised over the samples
+    warm-up (its start-up stalls the GPU driver for a moment), and summarised over the samples
     whose timestamps fall inside the timed region."""
     Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"

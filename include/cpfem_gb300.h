@@ -467,7 +467,7 @@ int cpfem_bicgstab_batched(const cpfem_sell_t* sell, const double* values, const
  * blocks of 256 threads, each running 8 independent FMA chains of `iters` steps; *flops
  * receives the FP64 flop count of the launch (an FMA counts 2).  Time it with events on
  * `stream`.  No reference counterpart: it supplies the roofline denominator of the
- * constitutive kernel, which the measured peaks do not include.
+ * constitutive kernel (the measured copy-bandwidth and bf16-GEMM peaks do not cover FP64).
  */
 int cpfem_probe_dfma(int64_t iters, int32_t blocks, double* out, double* flops, void* stream);
 
