@@ -1,6 +1,6 @@
 """CPU FP64 oracle for the CPFEM hot path -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
 
-This module is the checker.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+Results of the CUDA path are checked against it.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
 legs of ``bench.py`` (``cpu_baseline`` and ``--impl reference``) may import it; the
 product package never does, and it is never the thing measured as the GPU result.
 
