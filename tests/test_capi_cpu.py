@@ -243,3 +243,45 @@ def test_multiphase_spec_and_golden_dp_fixture(pkg):
     assert g["dp_ori"].max() >= g["dp_quat"].shape[0]          # clamped indices occur
     assert np.abs(np.linalg.norm(g["dp_quat"], axis=1) - 1).max() < 1e-12
     assert g["dp_sig"].shape == (50, 3, 1000)
+
+
+def _fake_hierarchy(capi):
+    """A two-level cpfem_mg_t whose pointers are non-null placeholders: enough for the
+    argument checks, which run before any device access."""
+    import ctypes
+    mg = capi.MGHierarchy()
+    mg.num_levels, mg.pre_sweeps, mg.post_sweeps, mg.coarse_sweeps, mg.omega = 2, 1, 1, 4, 0.45
+    fake = 4096
+    for l, d in enumerate((3, 2)):
+        for k in range(3):
+            mg.dims[l][k] = d
+        s = mg.sell[l]
+        s.num_nodes, s.num_groups = d ** 3, (d ** 3 + 31) // 32
+        s.group_off = s.group_width = s.cols = s.tpos = s.diag_slot = fake
+        mg.values[l] = mg.minv[l] = mg.slot[l] = mg.x[l] = mg.t[l] = mg.r[l] = mg.b[l] = fake
+    mg.scratch[0] = mg.scratch[1] = fake
+    mg.scratch_nodes = 1 << 20
+    return mg
+
+
+@pytest.mark.parametrize("field,value,message", [("precision", 7, "precision"), ("local_nodes", -1, "local_nodes"),
+                                                 ("omega", 2.5, "omega")])
+def test_multigrid_argument_checks(lib, field, value, message):
+    import ctypes
+    from importlib import import_module
+    capi = import_module("jax-cpfem_gb300._capi")
+    mg = _fake_hierarchy(capi)
+    setattr(mg, field, value)
+    rc = lib.cpfem_mg_setup(ctypes.byref(mg), ctypes.c_void_p(4096), None)
+    assert rc == 1 and message in lib.cpfem_last_error().decode()
+
+
+def test_fp32_multigrid_needs_its_arrays(lib):
+    """precision = 1 without the FP32 copies is an argument error, not a device fault."""
+    import ctypes
+    from importlib import import_module
+    capi = import_module("jax-cpfem_gb300._capi")
+    mg = _fake_hierarchy(capi)
+    mg.precision = 1
+    rc = lib.cpfem_mg_setup(ctypes.byref(mg), ctypes.c_void_p(4096), None)
+    assert rc == 1 and "arrays missing" in lib.cpfem_last_error().decode()
