@@ -441,15 +441,16 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
         d_t = rng.normal(size=5) * theta * 1e-6
         d_e = rng.normal(size=euler.shape) * 1e-4
         f = lambda th, eu: float(((h.forward(th, eu, checkpoint=False).cpu().numpy()[:, 2, 2] - target) ** 2).mean())
-        # the difference quotient runs the local solves from S = 0, the reference's start: a
-        # warm start stops as soon as the residual is below the local tolerance, so the map
-        # is smooth only to that tolerance (~1e-10 relative), which a 1e-6 step amplifies
-        prob.warm_start_local = False
+        # the difference quotient runs the reference's local iterates (S = 0 start, FP64
+        # directions): a warm start or an FP32 direction ends the local solve as soon as the
+        # residual is below the tolerance, so the map is smooth only to that tolerance (~1e-10
+        # relative), which a 1e-6 step amplifies
+        prob.warm_start_local = prob.fp32_local_jacobian = False
         fd = (f(theta + d_t, euler + d_e) - f(theta - d_t, euler - d_e)) / 2.0
-        prob.warm_start_local = True
+        prob.warm_start_local = prob.fp32_local_jacobian = True
         ad = float(tb @ d_t + (eb * d_e).sum())
         out["directional_fd_check"] = {"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd),
-                                       "fd_local_start": "S = 0"}
+                                       "fd_local_solve": "S = 0 start, FP64 directions (the reference's iterates)"}
     print(json.dumps(out))
 
 
