@@ -32,6 +32,8 @@ METRIC = "GP updates/s; 32³ RVE s/load-step; grad÷fwd & batched÷serial time a
 UNIT = "GP updates/s"
 N_EDGE, N_GRAINS, SEED = 32, 64, 0
 STRAIN_STEP, DT = 1e-3, 0.1
+# Newton stop rule of both arms: the reference's (crystal_plasticity_OR_design/solver.py:384-385)
+NEWTON = {"tol": 1e-6, "rel_tol": 1e-8}
 
 
 def workload_config(n=N_EDGE, config="c1"):
@@ -42,7 +44,8 @@ def workload_config(n=N_EDGE, config="c1"):
     return {"workload": name,
             "cells": n ** 3, "gauss_points": 8 * n ** 3, "dofs": 3 * (n + 1) ** 3, "grains": grains,
             "strain_per_step": STRAIN_STEP, "dt_s": DT, "bcs": "rollers x=0,y=0,z=0; u_z(top)",
-            "linear_solver": "BiCGSTAB tol=atol=1e-10", "newton": "tol 1e-6 / rel_tol 1e-8",
+            "linear_solver": "BiCGSTAB tol=atol=1e-10",
+            "newton": f"tol {NEWTON['tol']:g} / rel_tol {NEWTON['rel_tol']:g}",
             "l2": "working set > L2 (state+tangent+CSR ~0.4 GB per step)"}
 
 
@@ -50,55 +53,80 @@ def _pkg():
     return importlib.import_module("jax-cpfem_gb300")
 
 
-def make_case(pkg, n=N_EDGE):
-    mesh = pkg.box_mesh(n, n, n)
-    ori, rng = pkg.mesh.voronoi_grains(mesh, N_GRAINS, SEED)
-    quat = pkg.material.random_quaternions(rng, N_GRAINS)
-    return mesh, quat, ori
+def _workloads():
+    return importlib.import_module("jax-cpfem_gb300.workloads")
 
 
-def roller_lists(pkg, mesh, disp):
-    p = mesh.points
-    fn = pkg.mesh.face_nodes
-    nodes = [fn(p, 0, 0.0), fn(p, 1, 0.0), fn(p, 2, 0.0), fn(p, 2, 1.0)]
-    return nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, disp]
+def make_workload(config="c1", n=N_EDGE):
+    W = _workloads()
+    if config == "c0":
+        return W.copper_single_crystal()
+    if config == "c2":
+        return W.tantalum_polycrystal()
+    return W.steel_polycrystal(n, N_GRAINS, SEED)
 
 
-class Stepper:
-    """Device-resident load-step loop through the public API."""
+# ---------------------------------------------------------------------------------------
+# CPU path: the compiled oracle (the reference's algorithm, OpenMP on all host cores)
+# ---------------------------------------------------------------------------------------
+def host_cpu():
+    import platform
+    model = platform.processor() or platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"cpu_count": os.cpu_count(), "model": model, "machine": platform.machine()}
 
-    def __init__(self, pkg, prob, solver_mod, mesh):
-        self.pkg, self.prob, self.solver, self.mesh = pkg, prob, solver_mod, mesh
-        self.i = 0
-        self.precond = 1
-        self.mg_options = None
-        self.grid_blocks = 0
-        self.params = prob.internal_vars
-        import torch
-        self.sol = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64, device="cuda")
 
-    def step(self, host_io=None):
-        prob = self.prob
-        self.i += 1
-        prob.dt = DT
-        nodes, comps, vals = roller_lists(self.pkg, self.mesh, STRAIN_STEP * self.i)
-        prob.fes[0].set_dirichlet_lists(nodes, comps, vals)
-        prob.set_params(self.params)
-        if host_io is not None:
-            sol_h, sig_h = host_io
-            guess = sol_h.to("cuda", non_blocking=True)
-        else:
-            guess = self.sol
-        sol = self.solver.solver(prob, {"jax_solver": {"precond": self.precond, "mg_options": self.mg_options,
-                                                       "grid_blocks": self.grid_blocks},
-                                        "initial_guess": [guess.reshape(-1, 3)]})[0]
-        sig = prob.compute_avg_stress(sol, self.params)
-        self.params = prob.update_int_vars_gp(sol, self.params)
-        self.sol = sol.reshape(-1)
-        if host_io is not None:
-            sol_h.copy_(self.sol, non_blocking=True)
-            sig_h.copy_(sig.reshape(-1), non_blocking=True)
-        return sig
+def oracle_problem(w):
+    """The compiled oracle on workload ``w`` with one OpenMP thread per host core."""
+    from oracle import coracle
+    from oracle import cpfem_oracle as O
+    coracle.set_threads(os.cpu_count() or 1)
+    s = w.spec
+    return coracle.FastOracleProblem(w.mesh.points, w.mesh.cells, O.SLIP_TABLES[s.slip], s.C11, s.C12, s.C44,
+                                     w.quat, w.ori, gss_initial=s.gss_initial, h=s.h, t_sat=s.t_sat,
+                                     gss_a=s.gss_a, xm=s.xm, r=s.r, ao=s.ao, coplanar=s.coplanar_q,
+                                     local_tol=s.local_tol, max_sub_step=s.max_sub_step)
+
+
+def oracle_load_step(orc, w, i, sol, params):
+    """Load step ``i`` (1-based) of the reference driver loop on the oracle
+    (``singlecrystal_copper/singlecrystal_copper.py:179-233``): set dt and the top
+    displacement, global Newton with Jacobi BiCGSTAB, ``compute_avg_stress``,
+    ``update_int_vars_gp``.  Returns (sol, params, cell stresses, solver info)."""
+    from oracle import cpfem_oracle as O
+    orc.dt = w.dt
+    orc.set_bcs(w.bc_triples(w.strain_step * i))
+    orc.set_params(params)
+    sol, info = O.solver(orc, dict(NEWTON, initial_guess=sol))
+    sig = orc.compute_avg_stress(sol, params)
+    params = orc.update_int_vars_gp(sol, params)
+    return sol, params, sig, info
+
+
+def cpu_baseline_step(w, i, sol, params4):
+    """One full load step (step ``i``) of the oracle on the host cores, started from a
+    committed state (``sol``, the four state arrays) of the GPU run: the bounded CPU sample
+    of the same workload."""
+    from oracle import coracle
+    orc = oracle_problem(w)
+    params = [np.ascontiguousarray(p) for p in params4] + orc.internal_vars[4:9]
+    t0 = time.perf_counter()
+    _, _, _, info = oracle_load_step(orc, w, i, np.ascontiguousarray(sol), params)
+    t = time.perf_counter() - t0
+    kr = [int(k) for k in info["krylov_iters"]]
+    threads = coracle.num_threads()
+    return {"value": w.num_gp / t, "unit": UNIT, "cores": threads, "kind": "port", "s_per_load_step": t,
+            "sample": (f"load step {i} of this workload run end to end by the compiled oracle (the reference's "
+                       f"algorithm in C) from the GPU run's committed state at the start of that step: global "
+                       f"Newton ({info['newton_iters']} iterations) with Jacobi BiCGSTAB ({sum(kr)} iterations), "
+                       f"then compute_avg_stress and update_int_vars_gp, {threads} OpenMP threads"),
+            "host": host_cpu(), "newton_iters": info["newton_iters"], "krylov_iters": kr}
 
 
 class ClockSampler:
@@ -272,119 +300,48 @@ def gp_flops_per_eval(num_slip, iters_mean, tangent=True, fp32_direction=True):
     return fp64, (direction if fp32_direction else 0.0)
 
 
-def _oracle_pass_worker(job):
-    """One host process: the oracle's constitutive + tangent + element pass on a chunk of
-    cells, started at a common wall-clock instant; returns (start, end)."""
-    points, cells, quat, ori, spec, start_at = job
-    from oracle import cpfem_oracle as O
-    used, inv = np.unique(cells, return_inverse=True)
-    orc = O.OracleProblem(points[used], inv.reshape(cells.shape), O.FCC12, spec["C11"], spec["C12"], spec["C44"],
-                          quat, ori, gss_initial=spec["gss_initial"], h=spec["h"], t_sat=spec["t_sat"],
-                          gss_a=spec["gss_a"], xm=spec["xm"], r=spec["r"], coplanar=True)
-    orc.dt = DT
-    u = np.zeros(orc.ndof)
-    u[2::3] = STRAIN_STEP * orc.points[:, 2]
-    while time.time() < start_at:
-        time.sleep(0.001)
-    t0 = time.time()
-    orc.newton_update(u)
-    return t0, time.time()
-
-
-def _spmv_worker(job):
-    """One host process: `reps` products of its row block of the tangent pattern with the
-    full vector (plus the iteration's vector updates on its rows), from a common start."""
-    blk, ndof, reps, start_at = job
-    x = np.ones(ndof)
-    y = np.empty(blk.shape[0])
-    while time.time() < start_at:
-        time.sleep(0.001)
-    t0 = time.time()
-    for _ in range(reps):
-        y = blk @ x
-        y = blk @ x
-        for _k in range(5):        # p, s, x, r updates and the six dots on the block's rows
-            y = y + 0.5 * y
-    return t0, time.time()
-
-
-def cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters, cores=None, budget_s=20.0):
-    """The oracle (numpy/scipy) on the host cores, on a bounded sample of the workload,
-    scaled to s per load step.  Constitutive+tangent+assembly: `cores` spawned processes
-    each run the oracle pass on 2048 cells at the same time (wall time of the slowest, x the
-    passes per step, scaled to all cells).  Krylov: each process multiplies its row block
-    of the full 32^3 tangent pattern (two SpMVs + vector updates per iteration); the
-    iteration time is the slowest block's (synchronisation between iterations is not
-    charged, which favours the CPU)."""
-    import multiprocessing as mp
-    import scipy.sparse as sp
-    cores = cores or os.cpu_count() or 1
-    spec = pkg.material.BENCH_STEEL
-    sd = {k: getattr(spec, k) for k in ("C11", "C12", "C44", "gss_initial", "h", "t_sat", "gss_a", "xm", "r")}
-    E = mesh.cells.shape[0]
-    sub = 2048
-    nchunk = max(1, min(cores, E // sub))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(nchunk) as pool:
-        pool.map(abs, range(nchunk))        # start the workers before the common instant
-        start = time.time() + 3.0
-        jobs = [(mesh.points, mesh.cells[k * sub:(k + 1) * sub], quat, ori[k * sub:(k + 1) * sub], sd, start)
-                for k in range(nchunk)]
-        spans = pool.map(_oracle_pass_worker, jobs)
-        t_pass = max(b for _, b in spans) - min(a for a, _ in spans)
-        t_asm = t_pass * E / (sub * nchunk)
-        # Krylov on the full pattern, split into row blocks
-        dof = (3 * mesh.cells[:, :, None] + np.arange(3)).reshape(E, 24)
-        I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
-        J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
-        ndof = 3 * mesh.points.shape[0]
-        A = sp.csr_array((np.random.default_rng(0).random(I.size), (I, J)), shape=(ndof, ndof))
-        A.sum_duplicates()
-        rows = np.linspace(0, ndof, nchunk + 1).astype(np.int64)
-        reps = 40
-        start = time.time() + 3.0
-        spans = pool.map(_spmv_worker, [(A[rows[k]:rows[k + 1]], ndof, reps, start) for k in range(nchunk)])
-        t_it = (max(b for _, b in spans) - min(a for a, _ in spans)) / reps
-    t_step = newton_passes * t_asm + krylov_iters * t_it
-    return {"value": 8 * E / t_step, "unit": UNIT, "cores": nchunk, "kind": "port",
-            "s_per_load_step": t_step,
-            "sample": (f"oracle newton_update on {nchunk} processes x {sub} cells at once ({t_pass:.2f} s wall, "
-                       f"scaled to {E} cells: {t_asm:.2f} s/pass) x {newton_passes} passes + row-block "
-                       f"BiCGSTAB iterations of the full {ndof}-dof pattern on {nchunk} processes "
-                       f"({t_it * 1e3:.2f} ms/it, {reps} timed) x {krylov_iters} iterations")}
-
-
 def run_reference(args):
-    """The reference's CPU path is JAX; JAX is not installed, so the reference arm times
-    the CPU restatement of the same algorithm (the oracle port) on the host cores."""
+    """The reference's CPU path is JAX, which is not installed; this arm runs the reference's
+    algorithm as the compiled oracle, full load steps end to end on all host cores: W
+    untimed load steps, then K timed ones (the same load steps the GPU arm times)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    pkg = _pkg()
-    mesh, quat, ori = make_case(pkg)
-    # counts of this workload's load steps measured on the GPU path (same algorithm)
-    newton_passes, krylov_iters = REF_COUNTS["passes_per_step"], REF_COUNTS["krylov_iters_per_step"]
-    vals = []
-    for k in range(max(1, min(args.steps, 2))):
-        vals.append(cpu_baseline_sample(pkg, mesh, quat, ori, newton_passes, krylov_iters))
-    v = float(np.median([r["value"] for r in vals]))
-    cb = dict(vals[-1])
-    cb["value"] = v
-    cb["sample"] += "; counts per step from the GPU path on this workload"
+    from oracle import coracle
+    w = make_workload("c1", args.edge)
+    t_setup = time.perf_counter()
+    orc = oracle_problem(w)
+    t_setup = time.perf_counter() - t_setup
+    sol, params = np.zeros(orc.ndof), orc.internal_vars
+    for i in range(1, args.warmup + 1):
+        sol, params, _, _ = oracle_load_step(orc, w, i, sol, params)
+    per_step, newton, krylov = [], [], []
+    t0 = time.perf_counter()
+    for i in range(args.warmup + 1, args.warmup + args.steps + 1):
+        ts = time.perf_counter()
+        sol, params, sig, info = oracle_load_step(orc, w, i, sol, params)
+        per_step.append(time.perf_counter() - ts)
+        newton.append(info["newton_iters"])
+        krylov.append([int(k) for k in info["krylov_iters"]])
+    t = time.perf_counter() - t0
+    v = w.num_gp * args.steps / t
+    threads = coracle.num_threads()
+    cb = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "s_per_load_step": t / args.steps,
+          "sample": (f"load steps {args.warmup + 1}-{args.warmup + args.steps} of this workload (after "
+                     f"{args.warmup} untimed ones), each run end to end by the compiled oracle: global Newton with "
+                     f"Jacobi BiCGSTAB, compute_avg_stress, update_int_vars_gp; {threads} OpenMP threads"),
+          "host": host_cpu()}
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 8 * N_EDGE ** 3 / v * 1e3, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": workload_config(), "impl": "reference",
+           "config": dict(workload_config(args.edge), precond="jacobi"), "impl": "reference",
            "cpu_baseline": cb,
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "note": "reference JAX/JAX-FEM path not installable offline; oracle port of the same algorithm"}
+           "s_per_load_step": per_step, "newton_iters_per_step": newton, "krylov_iters": krylov,
+           "setup_s": t_setup, "mean_sigma_zz_last": float(sig[:, 2, 2].mean()),
+           "note": ("the reference's JAX/JAX-FEM path is not installable offline (no jax, jax_fem, meshio); "
+                    "this is its algorithm restated in C (oracle/cpfem_oracle_c.c), timed, not modelled")}
     print(json.dumps(out))
-
-
-# Per-load-step counts of this workload on the GPU path (tension steps 1..20):
-# constitutive+tangent passes (Newton iterations + 1) and BiCGSTAB iterations summed over
-# the step's linear solves.  Refreshed from the GPU bench run.
-REF_COUNTS = {"passes_per_step": 6, "krylov_iters_per_step": 2630}
 
 
 def run_adjoint_config(args, pkg, problem_mod, torch):
@@ -393,14 +350,13 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
     from importlib import import_module
     adjoint = import_module("jax-cpfem_gb300.adjoint")
     n = args.edge
-    mesh, quat, ori = make_case(pkg, n)
-    spec = pkg.material.BENCH_STEEL
+    w = make_workload("c1", n)
+    mesh, quat, ori, spec = w.mesh, w.quat, w.ori, w.spec
     prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=spec)
     nsteps = args.load_steps or 20
 
     def bc_fn(i, d):
-        nodes, comps, vals = roller_lists(pkg, mesh, d)
-        return nodes, comps, vals
+        return w.bc_lists(d)
 
     disps = STRAIN_STEP * np.arange(nsteps + 1)
     ts = DT * np.arange(nsteps + 1)
@@ -560,41 +516,34 @@ def main():
     if args.config == "c4":
         run_batch_config(args, pkg, torch)
         return
-    n = args.edge
-    spec = pkg.material.BENCH_STEEL
-    if args.config == "c0":
-        n = 10
-        mesh, quat, ori = pkg.box_mesh(n, n, n), np.array([[1.0, 0.0, 0.0, 0.0]]), np.zeros(n ** 3, dtype=np.int64)
-        spec = pkg.material.BENCH_COPPER
-    elif args.config == "c2":
-        n = 64
-        mesh = pkg.box_mesh(n, n, n)
-        ori, rng = pkg.mesh.voronoi_grains(mesh, 512, SEED)
-        quat = pkg.material.random_quaternions(rng, 512)
-        spec = pkg.material.BENCH_TANTALUM
-    else:
-        mesh, quat, ori = make_case(pkg, n)
-    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(quat, ori), material=spec)
+    w = make_workload(args.config, args.edge)
+    n = round(w.mesh.cells.shape[0] ** (1.0 / 3.0))
+    mesh = w.mesh
+    prob = problem_mod.CrystalPlasticity(mesh, additional_info=(w.quat, w.ori), material=w.spec)
     counter = CountingLib(prob.lib)
     prob.lib = counter
-    st = Stepper(pkg, prob, solver_mod, mesh)
-    st.precond = args.precond
-    st.mg_options = {"refresh": args.mg_refresh}
+    W = _workloads()
+    st = W.LoadStepper(prob, solver_mod, w)
+    mg_options = {"refresh": args.mg_refresh}
     if args.mg_precision:
-        st.mg_options["precision"] = args.mg_precision
+        mg_options["precision"] = args.mg_precision
+
+    def set_solver(precond, mg, grid_blocks):
+        st.options = dict(NEWTON, jax_solver={"precond": precond, "mg_options": mg, "grid_blocks": grid_blocks})
+
+    set_solver(args.precond, mg_options, 0)
     clk = ClockSampler(local).start()
     time.sleep(1.0)
     # warm-up with the timers on, so every kernel the timed steps use (including torch's
     # small reductions) has run once before the clock starts
     prob.timing = True
     tuned = None
-    for w in range(args.warmup):
+    for wi in range(args.warmup):
         st.step()
-        if w == 0 and args.precond == 3 and not args.no_tune:
+        if wi == 0 and args.precond == 3 and not args.no_tune:
             # autotune the multigrid / launch settings on the next step's first Newton system
             tuning = import_module("jax-cpfem_gb300.tuning")
-            nodes, comps, vals = roller_lists(pkg, mesh, STRAIN_STEP * (st.i + 1))
-            prob.fes[0].set_dirichlet_lists(nodes, comps, vals)
+            prob.fes[0].set_dirichlet_lists(*w.bc_lists(w.strain_step * (st.i + 1)))
             prob.set_params(st.params)
             res, A = solver_mod.newton_update_helper(prob, st.sol)
             x0 = solver_mod.initial_increment(prob, st.sol).clone()
@@ -604,8 +553,8 @@ def main():
                 start["precision"] = args.mg_precision
                 search = tuple(kv for kv in search if kv[0] != "precision")
             cfg, table = tuning.tune_linear_solver(prob, A, -res, x0, search=search, start=start)
-            st.grid_blocks = cfg["grid_blocks"]
-            st.mg_options = dict({k: v for k, v in cfg.items() if k != "grid_blocks"}, refresh=args.mg_refresh)
+            mg_options = dict({k: v for k, v in cfg.items() if k != "grid_blocks"}, refresh=args.mg_refresh)
+            set_solver(args.precond, mg_options, cfg["grid_blocks"])
             tuned = {"chosen": cfg, "candidates": len(table),
                      "default_ms": round(table[0][1], 3), "chosen_ms": round(min(t[1] for t in table
                                                                                    if t[0] == cfg), 3)}
@@ -620,6 +569,11 @@ def main():
     prob.stats["krylov_iters"] = []
     passes0 = prob.stats["gp_passes"]
     newton = []
+    # the committed state at the start of the first timed step (copied before the clock
+    # starts): the CPU baseline runs that same load step from it
+    snap = None
+    if rank == 0 and not args.no_cpu_baseline and args.config == "c1":
+        snap = (st.i + 1, st.sol.cpu().numpy().copy(), [p.cpu().numpy().copy() for p in st.params[:4]])
     barrier()
     torch.cuda.synchronize()
     wall0 = time.time()
@@ -662,8 +616,8 @@ def main():
     # the same load steps with the reference's Jacobi-preconditioned BiCGSTAB, for comparison
     jacobi = None
     if args.precond != 1 and not args.no_jacobi_leg:
-        st.precond, gb = 1, st.grid_blocks
-        st.grid_blocks = 0
+        saved = st.options
+        set_solver(1, None, 0)
         st.step()
         torch.cuda.synchronize()
         k0 = len(prob.stats["krylov_iters"])
@@ -676,7 +630,7 @@ def main():
         jacobi = {"precond": "jacobi (the reference's)", "steps": 2,
                   "ms_per_step": max_over_ranks(j0.elapsed_time(j1) * 1e-3, world, "cuda") / 2 * 1e3,
                   "krylov_iters": [int(k) for k in prob.stats["krylov_iters"][k0:]]}
-        st.precond, st.grid_blocks = args.precond, gb
+        st.options = saved
 
     # roofline of the dominant kernel (the persistent BiCGSTAB) and of the constitutive pass
     peaks = measured_peaks()
@@ -729,20 +683,8 @@ def main():
     dominant = kr_roof if (kr_roof is not None and shares["bicgstab"] >= shares["gp_eval_tangent"]) else gp_roof
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline and args.config == "c1":
-        # the CPU path is the reference's algorithm: Jacobi-preconditioned BiCGSTAB, so its
-        # Krylov count per step comes from the Jacobi leg of this run (else the stored one)
-        if jacobi is not None:
-            kps = sum(max(k, 0) for k in jacobi["krylov_iters"]) / jacobi["steps"]
-            src = "Jacobi-leg Krylov counts of this GPU run"
-        elif args.precond == 1:
-            kps = sum(max(k, 0) for k in krylov) / args.steps
-            src = "Krylov counts of this GPU run"
-        else:
-            kps = REF_COUNTS["krylov_iters_per_step"]
-            src = "stored Jacobi Krylov count of this workload"
-        cpu = cpu_baseline_sample(pkg, mesh, quat, ori, passes / args.steps, kps)
-        cpu["sample"] += f"; constitutive passes per step from this GPU run, {src}"
+    if snap is not None:
+        cpu = cpu_baseline_step(w, *snap)
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,

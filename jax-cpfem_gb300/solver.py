@@ -116,7 +116,8 @@ def linear_solver(problem, A, b, x0, solver_options):
         o = solver_options["jax_solver"] or {}
         return jax_solve(problem, A, b, x0, o.get("precond", True), o)
     if "custom_solver" in solver_options:
-        return solver_options["custom_solver"](A, b, x0, solver_options)
+        x = solver_options["custom_solver"](A, b, x0, solver_options)
+        return torch.as_tensor(x, dtype=torch.float64, device=problem.device).reshape(-1).contiguous()
     raise NotImplementedError("only 'jax_solver' (device BiCGSTAB) and 'custom_solver' run on the GPU; "
                               "UMFPACK/PETSc host solvers are not part of the device path")
 

@@ -527,9 +527,12 @@ def solver(problem, solver_options=None):
         res[bc_dofs] -= bc_vals
         return res
 
+    # a problem may bring compiled row elimination and BiCGSTAB (coracle.FastOracleProblem)
+    zero_rows = getattr(problem, "zero_rows", apply_bc_rows)
+
     def helper(d):
         res, A = problem.newton_update(d)
-        return res_bc(d, res), apply_bc_rows(A, bc_dofs)
+        return res_bc(d, res), zero_rows(A, bc_dofs)
 
     res, A = helper(dofs)
     rv = np.linalg.norm(res)
@@ -539,8 +542,11 @@ def solver(problem, solver_options=None):
         x0 = np.zeros(problem.ndof)
         x0[bc_dofs] = bc_vals
         x0[bc_dofs] -= dofs[bc_dofs]
-        diag = A.diagonal()
-        inc, kk = bicgstab(A, -res, x0, lambda v: v * (1.0 / diag))
+        if hasattr(problem, "linear_solve"):
+            inc, kk = problem.linear_solve(A, -res, x0)
+        else:
+            diag = A.diagonal()
+            inc, kk = bicgstab(A, -res, x0, lambda v: v * (1.0 / diag))
         err = np.linalg.norm(A @ inc + res)
         if not err < 0.1:
             raise RuntimeError(f"oracle linear solver failed, err={err}")

@@ -47,3 +47,35 @@ def random_gp_inputs(rng, n, N, strain=1e-3, plastic=True):
     q /= np.linalg.norm(q, axis=1)[:, None]
     R = O.rot_mat(q)
     return ug, fpi, g, slip, R
+
+
+def fast_oracle_problem(spec, mesh, quat, ori, bcs=()):
+    """The compiled oracle (same algorithm as ``oracle_problem``, for the large cases)."""
+    from oracle import coracle as C
+    return C.FastOracleProblem(mesh.points, mesh.cells, ORACLE_SLIP[spec.slip], spec.C11, spec.C12, spec.C44,
+                               quat, ori, gss_initial=spec.gss_initial, h=spec.h, t_sat=spec.t_sat,
+                               gss_a=spec.gss_a, xm=spec.xm, r=spec.r, ao=spec.ao, coplanar=spec.coplanar_q,
+                               local_tol=spec.local_tol, max_sub_step=spec.max_sub_step, bcs=bcs)
+
+
+def oracle_history(orc, workload, steps, solver_options=None):
+    """The reference driver loop on the oracle (``singlecrystal_copper.py:179-233``): per
+    step the volume-averaged Cauchy stress (3,3), the solution, and Newton / Krylov counts;
+    the final internal variables."""
+    sol = np.zeros(orc.ndof)
+    params = orc.internal_vars
+    vol = orc.jxw.sum(1)
+    sig, us, info = [], [], []
+    for i in range(steps):
+        orc.dt = workload.dt
+        orc.set_bcs(workload.bc_triples(workload.strain_step * (i + 1)))
+        orc.set_params(params)
+        opts = dict(solver_options or {})
+        opts["initial_guess"] = sol
+        sol, inf = O.solver(orc, opts)
+        s = orc.compute_avg_stress(sol, params)
+        sig.append(np.einsum("eij,e->ij", s, vol) / vol.sum())
+        us.append(sol.copy())
+        info.append(inf)
+        params = orc.update_int_vars_gp(sol, params)
+    return np.array(sig), np.array(us), params, info

@@ -2,6 +2,7 @@
 autotuner's coordinate search (with a stand-in for the timed solve)."""
 import importlib
 
+import numpy as np
 import pytest
 
 
@@ -52,3 +53,26 @@ def test_tuner_coordinate_search_keeps_the_fastest_converging(tuning, monkeypatc
     assert cfg["grid_blocks"] == 152
     assert all(t[0]["grid_blocks"] != 76 for t in table)      # the rejected one is left out
     assert prob.kw == {k: cfg[k] for k in tuning.MG_KEYS}      # the hierarchy ends in the choice
+
+
+def test_custom_solver_node_block_pattern(pkg):
+    """The custom_solver binding recovers the node-block pattern of a HEX8 scalar CSR matrix
+    (scipy's COO->CSR of the element triplets) and refuses other patterns."""
+    import importlib
+    import scipy.sparse as sp
+    cs = importlib.import_module("jax-cpfem_gb300.custom_solver")
+    mesh = pkg.box_mesh(3, 2, 2)
+    E = mesh.cells.shape[0]
+    dof = (3 * mesh.cells[:, :, None] + np.arange(3)).reshape(E, 24)
+    I = np.repeat(dof[:, :, None], 24, axis=2).ravel()
+    J = np.repeat(dof[:, None, :], 24, axis=1).ravel()
+    A = sp.csr_array((np.ones(I.size), (I, J)))
+    A.sum_duplicates()
+    A.sort_indices()
+    rowptr, cols, node_of = cs.node_block_pattern(A.indptr.astype(np.int64), A.indices.astype(np.int64))
+    n = mesh.points.shape[0]
+    B = sp.csr_array((np.ones(cols.size), cols, rowptr), shape=(n, n))
+    assert (sp.kron(B, np.ones((3, 3))).tocsr() != A.astype(bool)).nnz == 0
+    with pytest.raises(ValueError):
+        R = sp.random(9, 9, density=0.5, format="csr", random_state=0) + sp.eye(9)
+        cs.node_block_pattern(R.indptr.astype(np.int64), R.indices.astype(np.int64))

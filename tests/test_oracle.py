@@ -149,3 +149,68 @@ def test_euler_generators_match_finite_differences(pkg):
         skew[:, 0, 1], skew[:, 0, 2], skew[:, 1, 2] = -w[:, 2], w[:, 1], -w[:, 0]
         skew = skew - np.swapaxes(skew, -1, -2)
         assert np.abs(skew - Wfd).max() < 1e-8
+
+
+@pytest.mark.parametrize("slip,coplanar", [("fcc12", True), ("bcc24", False)])
+def test_compiled_oracle_matches_numpy_oracle(slip, coplanar):
+    """The compiled oracle (cpfem_oracle_c.c, the large-case checker and the timed CPU
+    baseline) against the numpy oracle it restates: per-GP outputs, the assembled residual
+    and CSR tangent (pattern exact), and three load steps of a 3^3 polycrystal."""
+    from oracle import coracle as C
+    table = {"fcc12": O.FCC12, "bcc24": O.BCC24}[slip]
+    pts, cells = O.box_mesh(3, 3, 3)
+    rng = np.random.default_rng(5)
+    quat = rng.normal(size=(4, 4))
+    quat /= np.linalg.norm(quat, axis=1)[:, None]
+    ori = rng.integers(0, 4, size=cells.shape[0])
+    kw = dict(gss_initial=90.0, h=200.0, t_sat=300.0, gss_a=2.0, xm=0.05, r=1.4, coplanar=coplanar)
+    mats = (204.6e3, 137.7e3, 126.2e3)
+    a = O.OracleProblem(pts, cells, table, *mats, quat, ori, **kw)
+    b = C.FastOracleProblem(pts, cells, table, *mats, quat, ori, **kw)
+    for p in (a, b):
+        p.dt = 0.1
+    u = np.zeros(a.ndof)
+    u[2::3] = 3e-3 * pts[:, 2]
+    u += 2e-4 * rng.normal(size=u.size)
+    r1, A1 = a.newton_update(u)
+    r2, A2 = b.newton_update(u)
+    A2 = A2.tocsr()
+    assert np.array_equal(A1.indptr, A2.indptr) and np.array_equal(A1.indices, A2.indices)
+    assert np.abs(r1 - r2).max() < 1e-11 * np.abs(r1).max()
+    assert np.abs(A1.data - A2.data).max() < 1e-11 * np.abs(A1.data).max()
+    new_a = a.update_int_vars_gp(u, a.internal_vars)
+    new_b = b.update_int_vars_gp(u, b.internal_vars)
+    for x, y in zip(new_a[:3], new_b[:3]):
+        assert np.abs(x - y).max() < 1e-12 * np.abs(x).max()
+    sa, sb = a.compute_avg_stress(u, a.internal_vars), b.compute_avg_stress(u, b.internal_vars)
+    assert np.abs(sa - sb).max() < 1e-11 * np.abs(sa).max()
+
+    def bcs(d):
+        return [(O.face_nodes(pts, 0, 0.0), 0, 0.0), (O.face_nodes(pts, 1, 0.0), 1, 0.0),
+                (O.face_nodes(pts, 2, 0.0), 2, 0.0), (O.face_nodes(pts, 2, 1.0), 2, d)]
+    ts, disps = 0.1 * np.arange(4), 1e-3 * np.arange(4)
+    s1, u1 = O.run_load_steps(a, disps, ts, bcs)
+    s2, u2 = O.run_load_steps(b, disps, ts, bcs)
+    assert np.abs(s1 - s2).max() < 1e-10 * np.abs(s1).max()
+    assert np.abs(u1 - u2).max() < 1e-10 * np.abs(u1).max()
+
+
+def test_compiled_bicgstab_matches_restatement():
+    """The compiled BiCGSTAB runs the numpy restatement's recurrences: same iteration count
+    and iterate on a non-symmetric system."""
+    from oracle import coracle as C
+    rng = np.random.default_rng(3)
+    n = 300
+    A = sp.random(n, n, density=0.03, random_state=4, format="csr") + sp.diags(4.0 + rng.random(n))
+    A = sp.csr_array(A)
+    A.sort_indices()
+    b = rng.normal(size=n)
+    x_ref, k_ref = O.bicgstab(A, b, np.zeros(n), lambda v: v / A.diagonal())
+    M = C.CSR(A.indptr.astype(np.int64), A.indices.astype(np.int32), A.data.copy(), n)
+    x = np.zeros(n)
+    k = np.zeros(1, dtype=np.int32)
+    minv = 1.0 / A.diagonal()
+    C.load().orc_bicgstab(n, M.indptr.ctypes.data, M.indices.ctypes.data, M.data.ctypes.data, b.ctypes.data,
+                          x.ctypes.data, minv.ctypes.data, 1e-10, 1e-10, 10000, k.ctypes.data)
+    assert int(k[0]) == k_ref
+    assert np.abs(x - x_ref).max() < 1e-9 * np.abs(x_ref).max()
