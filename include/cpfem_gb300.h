@@ -421,8 +421,11 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
  * through their own pool, or loops that must not allocate.  Limit: num_nodes <=
  * CPFEM_NOALLOC_MAX_NODES, else CPFEM_ERR_SIZE with a message.  The first call on a
  * device resolves the array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  Every call shares the one array, so calls that overlap on
- * the GPU (other streams or threads) race; serialise them.  Calls no cudaMalloc/cudaFree.
+ * before any stream capture.  The address is kept per device index and belongs to the
+ * device's primary context (the one the CUDA runtime API uses): after cudaDeviceReset, or
+ * from a context made current through the driver API, it is stale, and such callers are not
+ * supported.  Every call shares the one array, so calls that overlap on the GPU (other
+ * streams or threads) race; serialise them.  Calls no cudaMalloc/cudaFree.
  */
 #define CPFEM_NOALLOC_MAX_NODES 65536
 #define CPFEM_NOALLOC_SCRATCH_BYTES (20u * 1024u * 1024u)

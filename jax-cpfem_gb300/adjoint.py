@@ -246,3 +246,211 @@ class SimulationFunction(torch.autograd.Function):
 def simulate(history, theta, euler):
     """Differentiable forward: ``SimulationFunction.apply``."""
     return SimulationFunction.apply(theta, euler, history)
+
+
+# --------------------------------------------------------------------------------------
+# The reference's differentiation interface: ad_wrapper / implicit_vjp
+# (crystal_plasticity_OR_design/solver.py:801-874) as torch autograd nodes.
+#
+# fwd_pred(params) -> sol_list is one load step's global solve as a function of the
+# internal-variable list; its backward is implicit_vjp: A^T lambda = v with the step's
+# row-eliminated tangent, then -lambda^T dc/dparams.  compute_avg_stress and
+# update_int_vars_gp become differentiable in (sol, params) whenever an input requires
+# grad, so a reference driver's load loop under torch autograd gives the gradient jax.grad
+# gives the reference.  Cotangents: Fp^-1, g and the five per-GP parameters (gss_a, h,
+# t_sat, xm, r) exactly; rotation matrices through their component tangent to SO(3),
+# R_bar = 1/2 [w_bar]x R (what any chain through rotation parameters -- Euler angles,
+# quaternions -- sees); slip enters no residual, and a nonzero cotangent of the new slip
+# (an objective that reads slip) is refused.
+# --------------------------------------------------------------------------------------
+def _snap(p):
+    fe = p.fes[0]
+    return float(p.dt), fe.bc_dofs.clone(), fe.bc_vals.clone()
+
+
+def _restore(p, snap):
+    fe = p.fes[0]
+    p.dt = snap[0]
+    fe.bc_dofs, fe.bc_vals = snap[1], snap[2]
+    fe.bc_token += 1
+
+
+def _adopt_detached(p, params):
+    p.set_params([t.detach() if isinstance(t, torch.Tensor) else t for t in params])
+
+
+def _gp_vjp_state(p, mode, u, cell_bar=None, lam_fp=None, lam_g=None, mu=None):
+    """cpfem_gp_vjp at the problem's adopted state (its Fp^-1, g and tables)."""
+    G, N = p.num_gp, p.num_slip
+    z = lambda rows: torch.zeros((rows, G), dtype=torch.float64, device=p.device)
+    a = _capi.VjpArgs()
+    a.num_gp, a.num_cells, a.mode, a.dt = G, p.num_cells, mode, float(p.dt)
+    a.num_nodes, a.num_rot = p.num_nodes, int(p.rot_table.shape[0])
+    a.num_param = int(p.param_table.shape[0])
+    fe = p.fes[0]
+    u = u.reshape(-1).contiguous()
+    cell_bar = torch.zeros((p.num_cells, 9), dtype=torch.float64, device=p.device) if cell_bar is None \
+        else cell_bar.reshape(p.num_cells, 9).contiguous()
+    lam_fp = z(9) if lam_fp is None else lam_fp
+    lam_g = z(N) if lam_g is None else lam_g
+    mu = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device) if mu is None else mu
+    a.u, a.cells, a.shape_grads, a.jxw = u.data_ptr(), fe.cells.data_ptr(), fe.shape_grads.data_ptr(), \
+        fe.JxW.data_ptr()
+    a.fpi, a.g = p.fpi.data_ptr(), p.g.data_ptr()
+    a.rot_table, a.rot_idx = p.rot_table.data_ptr(), p.rot_idx.data_ptr()
+    a.param_table, a.param_idx = p.param_table.data_ptr(), _dev_ptr(p.param_idx)
+    a.elastic_table = _dev_ptr(p.elastic_table)
+    a.cell_sig_bar, a.fpi_bar, a.g_bar, a.mu = cell_bar.data_ptr(), lam_fp.data_ptr(), lam_g.data_ptr(), \
+        mu.data_ptr()
+    status = torch.zeros(1, dtype=torch.int32, device=p.device)
+    a.status = status.data_ptr()
+    out = {}
+    if mode == 1:
+        out["f_bar"] = z(9)
+        a.f_bar = out["f_bar"].data_ptr()
+    else:
+        out.update(fpi_bar_old=z(9), g_bar_old=z(N), theta_bar=z(5), rot_bar=z(3))
+        for k in ("fpi_bar_old", "g_bar_old", "theta_bar", "rot_bar"):
+            setattr(a, k, out[k].data_ptr())
+    with p.region(f"gp_vjp{mode}"):
+        _capi.check(p.lib.cpfem_gp_vjp(p.mat_c, a, _stream()))
+    p._check_status(status)
+    return out
+
+
+def _sol_cotangent(p, f_bar):
+    """The assembly backward: u_bar_a = sum_q F_bar_q grad N_a (the coloured scatter)."""
+    ub = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
+    p.scatter(f_bar, None, ub, None)
+    return ub.reshape(p.num_nodes, 3)
+
+
+def _param_cotangents(p, params, o):
+    """Mode-2 outputs in the shapes of the reference's internal-variable list (None for an
+    entry that does not require grad)."""
+    E, N = p.num_cells, p.num_slip
+    out = [o["fpi_bar_old"].t().reshape(E, 8, 3, 3), o["g_bar_old"].t().reshape(E, 8, N), None]
+    R = torch.as_tensor(params[3], dtype=torch.float64, device=p.device).reshape(-1, 3, 3)
+    w = o["rot_bar"].t()
+    W = torch.zeros((w.shape[0], 3, 3), dtype=torch.float64, device=p.device)
+    W[:, 0, 1], W[:, 0, 2], W[:, 1, 2] = -w[:, 2], w[:, 1], -w[:, 0]
+    W[:, 1, 0], W[:, 2, 0], W[:, 2, 1] = w[:, 2], -w[:, 1], w[:, 0]
+    out.append((0.5 * W @ R).reshape(E, 8, 3, 3))
+    if len(params) >= 9:
+        out += [o["theta_bar"][k].reshape(E, 8) for k in range(5)]
+    if len(params) >= 10:
+        out.append(None)   # the per-GP stiffness of the multi-phase layout is not differentiated
+    return [None if (g is None or not (isinstance(t, torch.Tensor) and t.requires_grad)) else g
+            for g, t in zip(out, params)]
+
+
+class _FwdPred(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, p, solver_options, adjoint_options, *params):
+        _adopt_detached(p, params)
+        opts = dict(solver_options)
+        if opts.get("initial_guess") is None and getattr(p, "initial_guess", None) is not None:
+            opts["initial_guess"] = p.initial_guess
+        sol = _solver.solver(p, opts)[0]
+        ctx.p, ctx.adj, ctx.snap, ctx.raw = p, dict(adjoint_options), _snap(p), params
+        ctx.save_for_backward(sol)
+        return sol
+
+    @staticmethod
+    def backward(ctx, v):
+        p, o, params = ctx.p, ctx.adj, ctx.raw
+        sol = ctx.saved_tensors[0]
+        _restore(p, ctx.snap)
+        _adopt_detached(p, params)
+        _, A = _solver.newton_update_helper(p, sol.reshape(-1))
+        lam, k, ok = _solver.bicgstab(p, A.T, v.reshape(-1).contiguous(),
+                                      torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device),
+                                      precond=o.get("precond", 1), tol=o.get("tol", 1e-10),
+                                      atol=o.get("atol", 1e-14), maxiter=o.get("maxiter", 10000),
+                                      mg_options=o.get("mg_options"))
+        if not ok:
+            raise RuntimeError(f"adjoint solve did not converge (iterations {k})")
+        lam[p.fes[0].bc_dofs.long()] = 0.0     # the Dirichlet rows of c do not depend on params
+        out = _gp_vjp_state(p, 2, sol, mu=lam)
+        return (None, None, None, *_param_cotangents(p, params, out))
+
+
+def ad_wrapper(problem, solver_options=None, adjoint_solver_options=None):
+    """``solver.py:856-874``: returns ``fwd_pred(params) -> sol_list`` whose gradient with
+    respect to the internal-variable list runs the adjoint (``implicit_vjp``, :801-853).
+    ``problem.initial_guess`` (``set_initial_guess``) seeds the solve when the options give
+    none, and the solution becomes the next guess, as the calibration drivers' copy does
+    (``calibration_case1_singleCrystalCopper_GB.py:73-94``)."""
+    so = dict(solver_options or {})
+    ao = dict(adjoint_solver_options or {})
+
+    def fwd_pred(params):
+        sol = _FwdPred.apply(problem, so, ao, *params)
+        problem.set_initial_guess([sol.detach()])
+        return [sol]
+    return fwd_pred
+
+
+class _AvgStress(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, p, sol, *params):
+        _adopt_detached(p, params)
+        sig = p._post_pass(sol.detach(), p.internal_vars)[0].clone()
+        ctx.p, ctx.snap, ctx.raw = p, _snap(p), params
+        ctx.save_for_backward(sol)
+        return sig
+
+    @staticmethod
+    def backward(ctx, sig_bar):
+        p, params = ctx.p, ctx.raw
+        sol = ctx.saved_tensors[0]
+        _restore(p, ctx.snap)
+        _adopt_detached(p, params)
+        cb = sig_bar.reshape(p.num_cells, 9).contiguous()
+        u_bar = _sol_cotangent(p, _gp_vjp_state(p, 1, sol, cell_bar=cb)["f_bar"])
+        out = _gp_vjp_state(p, 2, sol, cell_bar=cb)
+        return (None, u_bar.reshape(sol.shape), *_param_cotangents(p, params, out))
+
+
+class _UpdateIntVars(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, p, sol, *params):
+        _adopt_detached(p, params)
+        new = p._post_pass(sol.detach(), p.internal_vars)[1]
+        ctx.p, ctx.snap, ctx.raw = p, _snap(p), params
+        ctx.save_for_backward(sol)
+        return tuple(t.clone() for t in new[:3]) + tuple(
+            t.detach().clone() if isinstance(t, torch.Tensor) else torch.as_tensor(t) for t in params[3:])
+
+    @staticmethod
+    def backward(ctx, *bars):
+        p, params = ctx.p, ctx.raw
+        sol = ctx.saved_tensors[0]
+        if bars[2] is not None and bool((bars[2] != 0).any()):
+            raise NotImplementedError("the gradient of an objective that reads the slip variables is not "
+                                      "implemented (slip enters no residual of the model)")
+        _restore(p, ctx.snap)
+        _adopt_detached(p, params)
+        G, N = p.num_gp, p.num_slip
+        lam_fp = None if bars[0] is None else bars[0].reshape(G, 9).t().contiguous()
+        lam_g = None if bars[1] is None else bars[1].reshape(G, N).t().contiguous()
+        u_bar = _sol_cotangent(p, _gp_vjp_state(p, 1, sol, lam_fp=lam_fp, lam_g=lam_g)["f_bar"])
+        out = _param_cotangents(p, params, _gp_vjp_state(p, 2, sol, lam_fp=lam_fp, lam_g=lam_g))
+        # the entries from rot on pass through unchanged
+        for k in range(3, len(params)):
+            if bars[k] is not None and isinstance(params[k], torch.Tensor) and params[k].requires_grad:
+                out[k] = bars[k] if out[k] is None else out[k] + bars[k]
+        if bars[2] is not None and isinstance(params[2], torch.Tensor) and params[2].requires_grad:
+            out[2] = bars[2]
+        return (None, u_bar.reshape(sol.shape), *out)
+
+
+def avg_stress(problem, sol, params):
+    """``compute_avg_stress`` as an autograd node in (sol, params)."""
+    return _AvgStress.apply(problem, torch.as_tensor(sol, dtype=torch.float64, device=problem.device), *params)
+
+
+def update_int_vars(problem, sol, params):
+    """``update_int_vars_gp`` as an autograd node in (sol, params)."""
+    return list(_UpdateIntVars.apply(problem, torch.as_tensor(sol, dtype=torch.float64, device=problem.device),
+                                     *params))

@@ -53,7 +53,14 @@ struct KWork {
   double *r, *rhat, *p, *q, *s, *t, *phat, *shat, *minv;
 };
 
-static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+static constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Bytes carve() lays out for n_nodes nodes, as a compile-time expression (the fixed scratch
+// of the allocation-free entry point is checked against it when the library is built).
+static constexpr size_t carve_bytes(int64_t n_nodes) {
+  return align256(sizeof(GridSync)) + align256(sizeof(SolveOut)) + align256(sizeof(double) * 2 * 4 * kMaxBlocks) +
+         8 * align256(sizeof(double) * 3 * (size_t)n_nodes) + align256(sizeof(double) * 9 * (size_t)n_nodes);
+}
 
 static size_t carve(void* base, int64_t n_nodes, KWork* w) {
   const int64_t n = 3 * n_nodes;
@@ -1690,12 +1697,15 @@ static size_t noalloc_bytes_needed() { return carve(nullptr, kNoAllocMaxNodes, n
 // 256-byte aligned scratch; its size is fixed at compile time from the carve layout of
 // kNoAllocMaxNodes nodes (checked again at run time).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[CPFEM_NOALLOC_SCRATCH_BYTES];
+static_assert(carve_bytes(kNoAllocMaxNodes) <= CPFEM_NOALLOC_SCRATCH_BYTES,
+              "the allocation-free scratch is smaller than the solver's layout for CPFEM_NOALLOC_MAX_NODES");
 
 static std::mutex g_noalloc_mutex;
 static void* g_noalloc_ptr[256] = {nullptr};
 
 // Device address of the scratch on the current device.  Host code must not use the
-// symbol's name as an address: it is a host-side stand-in.  Resolved once per device.
+// symbol's name as an address: it is a host-side stand-in.  Resolved once per device index
+// and kept: the address belongs to that device's primary context (the runtime API's).
 static int noalloc_scratch(void** out) {
   int dev = 0;
   CPFEM_CUDA_TRY(cudaGetDevice(&dev));
@@ -1726,7 +1736,9 @@ extern "C" int cpfem_bicgstab_noalloc(const cpfem_sell_t* sell, const double* va
               std::to_string((long long)kNoAllocMaxNodes) + " nodes; use cpfem_bicgstab with a caller workspace");
     return CPFEM_ERR_SIZE;
   }
-  CPFEM_REQUIRE(noalloc_bytes_needed() <= sizeof(g_noalloc_scratch), "scratch smaller than its layout");
+  CPFEM_REQUIRE(noalloc_bytes_needed() == carve_bytes(kNoAllocMaxNodes) &&
+                    noalloc_bytes_needed() <= sizeof(g_noalloc_scratch),
+                "scratch smaller than its layout");
   void* ws = nullptr;
   int rc = noalloc_scratch(&ws);
   if (rc != CPFEM_OK) return rc;

@@ -525,7 +525,8 @@ class CrystalPlasticity:
     def set_params(self, params):
         """Adopt a reference-shaped internal-variable list (``models_copper.py:284-285``)."""
         if not self._is_adopted(params):
-            self._adopt(params)
+            with torch.no_grad():
+                self._adopt(params)
 
     def _is_adopted(self, params):
         """True when ``params`` are the very objects (unchanged) last adopted or handed out."""
@@ -888,11 +889,19 @@ class CrystalPlasticity:
         return sig, new
 
     def update_int_vars_gp(self, sol, params):
-        """New internal variables at the converged ``sol`` (``models_copper.py:273-282``)."""
+        """New internal variables at the converged ``sol`` (``models_copper.py:273-282``);
+        an autograd node when ``sol`` or a parameter requires grad."""
+        if _wants_grad(sol, params):
+            from . import adjoint
+            return adjoint.update_int_vars(self, sol, params)
         return list(self._post_pass(sol, params)[1])
 
     def compute_avg_stress(self, sol, params):
-        """JxW-weighted per-cell Cauchy stress (E,3,3) (``models_copper.py:297-319``)."""
+        """JxW-weighted per-cell Cauchy stress (E,3,3) (``models_copper.py:297-319``); an
+        autograd node when ``sol`` or a parameter requires grad."""
+        if _wants_grad(sol, params):
+            from . import adjoint
+            return adjoint.avg_stress(self, sol, params)
         return self._post_pass(sol, params)[0]
 
     def inspect_interval_vars(self, params):
@@ -922,6 +931,11 @@ class _Region:
             e1.record()
             self.p.timers.setdefault(self.name, []).append((self.e0, e1))
         return False
+
+
+def _wants_grad(sol, params):
+    return torch.is_grad_enabled() and any(isinstance(t, torch.Tensor) and t.requires_grad
+                                           for t in [sol, *params])
 
 
 def _flat(sol_list, device):

@@ -137,7 +137,8 @@ class GPBatch:
 
     def __init__(self, F, Fpi, g, Pr, Cr, xm, ao, dt):
         self.F, self.Fpi, self.g, self.Pr, self.Cr = F, Fpi, g, Pr, Cr
-        self.xm = np.broadcast_to(np.asarray(xm, dtype=np.float64), (F.shape[0],))
+        xm = np.asarray(xm)
+        self.xm = np.broadcast_to(xm.astype(np.result_type(xm, np.float64)), (F.shape[0],))
         self.ao, self.dt = ao, dt
         self.A = F @ Fpi
 
@@ -146,16 +147,26 @@ class GPBatch:
                        self.xm[idx], self.ao, self.dt)
 
 
+def _sign(x):
+    """np.sign of the real part: the branch, which a complex-step perturbation never flips."""
+    return np.sign(np.real(x))
+
+
+def _abs(x):
+    """|x|, continued analytically for complex-step derivatives (x sign(Re x))."""
+    return x * _sign(x) if np.iscomplexobj(x) else np.abs(x)
+
+
 def _slip_increment(b, S):
     """tau, Delta gamma and d(Delta gamma)/d tau (``models_copper.py:173-174``)."""
     tau = np.einsum("gij,gaij->ga", S, b.Pr)
     x = tau / b.g
     p = 1.0 / b.xm[:, None]
-    ax = np.abs(x)
-    dgam = b.ao * b.dt * ax ** p * np.sign(tau)
+    ax = _abs(x)
+    dgam = b.ao * b.dt * ax ** p * _sign(tau)
     # derivative as JAX differentiates |x|**p * sign(tau): p |x|^(p-1) sign(x) sign(tau) / g
     with np.errstate(divide="ignore", invalid="ignore"):
-        kd = np.where(ax > 0, b.ao * b.dt * p * ax ** (p - 1.0) / b.g * np.sign(x) * np.sign(tau), 0.0)
+        kd = np.where(np.real(ax) > 0, b.ao * b.dt * p * ax ** (p - 1.0) / b.g * _sign(x) * _sign(tau), 0.0)
     return tau, dgam, kd
 
 
@@ -196,7 +207,7 @@ def local_newton(b, tol, max_sub_step, max_it=200):
     safety cap the reference does not have; lanes that hit it report not-converged.
     """
     G = b.F.shape[0]
-    y = np.zeros((G, 3, 3))
+    y = np.zeros((G, 3, 3), dtype=np.result_type(b.F, b.Fpi, b.g, b.Pr, b.Cr, b.xm))
     r = residual(b, y)
     rn = np.linalg.norm(r.reshape(G, 9), axis=1)
     its = np.zeros(G, dtype=np.int64)
@@ -259,7 +270,7 @@ def tangent(b, S):
     D = np.einsum("ik,glj->gijkl", I3, X).reshape(G, 9, 9)
     # dP/dS for the 9 basis directions e_mn of S
     Finv_pi = np.linalg.inv(Fpi_new)
-    dPdS = np.empty((G, 9, 9))
+    dPdS = np.empty((G, 9, 9), dtype=X.dtype)
     for m in range(3):
         for n in range(3):
             dL = np.einsum("ga,ga,gaij->gij", kd, b.Pr[:, :, m, n], b.Pr)
@@ -280,12 +291,19 @@ def hardening_update(S, b, g, slip, h, t_sat, gss_a, r, coplanar):
     _, dgam, _ = _slip_increment(b, S)
     Fpi_new, _ = _kinematics(b, dgam)
     ratio = 1.0 - g / t_sat[:, None]
-    tmp = h[:, None] * np.abs(dgam) * np.abs(ratio) ** gss_a[:, None] * np.sign(ratio)
+    tmp = h[:, None] * _abs(dgam) * _abs(ratio) ** gss_a[:, None] * _sign(ratio)
     N = g.shape[1]
     qs = np.stack([q_matrix(N, ri, coplanar) for ri in np.unique(r)])
     ridx = np.searchsorted(np.unique(r), r)
     g_inc = np.einsum("gab,gb->ga", qs[ridx], tmp)
     return Fpi_new, g + g_inc, slip + dgam
+
+
+def _bincount(idx, w, n):
+    """np.bincount with weights, for real or complex weights."""
+    if np.iscomplexobj(w):
+        return np.bincount(idx, weights=w.real, minlength=n) + 1j * np.bincount(idx, weights=w.imag, minlength=n)
+    return np.bincount(idx, weights=w, minlength=n)
 
 
 # ----------------------------------------------------------------------------------
@@ -417,7 +435,7 @@ class OracleProblem:
         P = first_pk_stress(b, S).reshape(E, 8, 3, 3)
         res_e = np.einsum("eqij,eqaj,eq->eai", P, self.sg, self.jxw)
         dof = (3 * self.cells[:, :, None] + np.arange(3)[None, None, :]).reshape(E, 24)
-        res = np.bincount(dof.ravel(), weights=res_e.ravel(), minlength=self.ndof)
+        res = _bincount(dof.ravel(), res_e.ravel(), self.ndof)
         if not need_tangent:
             return res, None
         D = tangent(b, S).reshape(E, 8, 3, 3, 3, 3)
@@ -517,7 +535,8 @@ def solver(problem, solver_options=None):
     rel_tol = opts.get("rel_tol", 1e-8)
     tol = opts.get("tol", 1e-6)
     ls_flag = opts.get("line_search_flag", False)
-    dofs = np.array(opts["initial_guess"], dtype=np.float64).reshape(-1) if opts.get("initial_guess") is not None \
+    guess = opts.get("initial_guess")
+    dofs = np.array(guess, dtype=np.result_type(guess, np.float64)).reshape(-1) if guess is not None \
         else np.zeros(problem.ndof)
     bc_dofs, bc_vals = problem.bc_dofs_vals()
 
@@ -538,8 +557,11 @@ def solver(problem, solver_options=None):
     rv = np.linalg.norm(res)
     r0 = rv
     info = {"newton_iters": 0, "krylov_iters": [], "res_history": [rv]}
+    max_newton = opts.get("max_newton", 100)     # a safety cap the reference does not have
     while (rv / r0 > rel_tol if r0 > 0 else False) and rv > tol:
-        x0 = np.zeros(problem.ndof)
+        if info["newton_iters"] >= max_newton:
+            raise RuntimeError(f"oracle Newton did not converge in {max_newton} iterations (res = {rv})")
+        x0 = np.zeros(problem.ndof, dtype=np.result_type(dofs, res))
         x0[bc_dofs] = bc_vals
         x0[bc_dofs] -= dofs[bc_dofs]
         if hasattr(problem, "linear_solve"):
@@ -610,3 +632,57 @@ def run_load_steps(problem, disps, ts, make_bcs, solver_options=None, stress_fn=
         params = problem.update_int_vars_gp(sol, params)
     problem.set_params(params)
     return np.array(out), sol
+
+
+# ----------------------------------------------------------------------------------
+# Derivatives of a load history (the quantity the reference differentiates with jax.grad
+# through ad_wrapper / implicit_vjp, ``crystal_plasticity_OR_design/solver.py:801-874``,
+# in the calibration and orientation-design drivers)
+# ----------------------------------------------------------------------------------
+def euler_zyx_deg(angles):
+    """Lowercase 'zyx' Euler angles in degrees, i.e. extrinsic rotations about z, then y,
+    then x: R = Rx(c) Ry(b) Rz(a) -- what ``Rotation.from_euler('zyx', ..., degrees=True)``
+    returns at ``poly_sensitivity_rot_mesh2.py:41-55``; written out so that complex angles
+    (complex-step derivatives) pass through."""
+    ang = np.asarray(angles) * (np.pi / 180.0)
+    a, b, c = ang[..., 0], ang[..., 1], ang[..., 2]
+    ca, sa, cb, sb, cc, sc = np.cos(a), np.sin(a), np.cos(b), np.sin(b), np.cos(c), np.sin(c)
+    z, o = np.zeros_like(a), np.ones_like(a)
+    Rz = np.stack([ca, -sa, z, sa, ca, z, z, z, o], -1).reshape(ang.shape[:-1] + (3, 3))
+    Ry = np.stack([cb, z, sb, z, o, z, -sb, z, cb], -1).reshape(ang.shape[:-1] + (3, 3))
+    Rx = np.stack([o, z, z, z, cc, -sc, z, sc, cc], -1).reshape(ang.shape[:-1] + (3, 3))
+    return Rx @ Ry @ Rz
+
+
+def history_stress(points, cells, slip_table, C, grain_quat, cell_grain, theta, euler, disps, ts, make_bcs,
+                   r=1.4, coplanar=True, ao=1e-3, local_tol=1e-8, max_sub_step=5, solver_options=None):
+    """Per-step mean cell Cauchy stress (n_steps, 3, 3) of a load history as a function of
+    the Kalidindi parameters theta = (h0, g0, gs, a, m) and per-grain Euler angles
+    (degrees, 'zyx', composed as R = R_euler R_quat, ``poly_sensitivity_rot_mesh2.py:41-65,
+    186-203``).  Complex theta / euler give complex-step derivatives: every operation on the
+    path is complex-analytic on the branch the real iterate takes, the local and global
+    Newton solves use their exact complex Jacobians, and the linear solves are direct, so
+    Im(f(x + i h d)) / h is the directional derivative of the discrete load history to
+    rounding."""
+    h0, g0, gs, a, m = theta
+    R = euler_zyx_deg(euler) @ rot_mat(grain_quat)
+    prob = OracleProblem(points, cells, slip_table, *C, grain_quat, cell_grain, gss_initial=1.0, h=1.0,
+                         t_sat=1.0, gss_a=1.0, xm=1.0, r=r, ao=ao, coplanar=coplanar, local_tol=local_tol,
+                         max_sub_step=max_sub_step)
+    E, N = prob.E, prob.N
+    ones = np.ones((E, 8))
+    rot = np.repeat(R[np.asarray(cell_grain)][:, None], 8, axis=1)
+    prob.internal_vars = [np.broadcast_to(np.eye(3), (E, 8, 3, 3)).astype(rot.dtype), g0 * np.ones((E, 8, N)),
+                          np.zeros((E, 8, N)), rot, a * ones, h0 * ones, gs * ones, m * ones, r * ones]
+
+    def direct(A, b, x0):
+        import scipy.sparse.linalg as spla
+        return spla.spsolve(sp.csc_matrix(A), b), 0
+    prob.linear_solve = direct
+    sig, _ = run_load_steps(prob, disps, ts, make_bcs, solver_options)
+    return sig.mean(axis=1)
+
+
+def complex_step(fn, x, d, h=1e-30):
+    """Directional derivative Im(fn(x + i h d)) / h of a real function (no cancellation)."""
+    return np.imag(fn(np.asarray(x, dtype=np.complex128) + 1j * h * np.asarray(d))) / h

@@ -214,3 +214,36 @@ def test_compiled_bicgstab_matches_restatement():
                           x.ctypes.data, minv.ctypes.data, 1e-10, 1e-10, 10000, k.ctypes.data)
     assert int(k[0]) == k_ref
     assert np.abs(x - x_ref).max() < 1e-9 * np.abs(x_ref).max()
+
+
+def test_complex_step_history_derivative_matches_central_differences():
+    """The oracle's complex-step derivative of a load history (the independent check of the
+    GPU adjoint) against central differences of the same oracle, on 2 cells and 2 steps."""
+    pts, cells = O.box_mesh(2, 1, 1)
+    rng = np.random.default_rng(4)
+    q = rng.normal(size=(2, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    ori = np.array([0, 1])
+    theta = np.array([200.0, 90.0, 300.0, 2.0, 0.05])
+    euler = rng.uniform(-20, 20, size=(2, 3))
+    disps, ts = 1e-3 * np.arange(3), 0.1 * np.arange(3)
+
+    def bcs(d):
+        return [(O.face_nodes(pts, 0, 0.0), 0, 0.0), (O.face_nodes(pts, 1, 0.0), 1, 0.0),
+                (O.face_nodes(pts, 2, 0.0), 2, 0.0), (O.face_nodes(pts, 2, 1.0), 2, d)]
+
+    def f(th, eu):
+        return O.history_stress(pts, cells, O.FCC12, (204.6e3, 137.7e3, 126.2e3), q, ori, th, eu, disps, ts, bcs,
+                                local_tol=1e-10, solver_options={"tol": 1e-10, "rel_tol": 1e-13,
+                                                                 "max_newton": 40})[:, 2, 2]
+    for k in (1, 4):                       # g0 and m
+        d = np.eye(5)[k]
+        cs = O.complex_step(lambda th: f(th, euler), theta, d)
+        h = 1e-6 * theta[k]
+        fd = (f(theta + h * d, euler) - f(theta - h * d, euler)) / (2 * h)
+        assert np.abs(cs - fd).max() < 1e-5 * np.abs(cs).max(), (k, cs, fd)
+    d = np.zeros_like(euler)
+    d[1, 0] = 1.0
+    cs = O.complex_step(lambda eu: f(theta, eu), euler, d)
+    fd = (f(theta, euler + 1e-4 * d) - f(theta, euler - 1e-4 * d)) / 2e-4
+    assert np.abs(cs - fd).max() < 1e-5 * np.abs(cs).max(), (cs, fd)

@@ -16,7 +16,10 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_bicgstab_matches_workspace_solver_twice(pkg, gpu):
+@pytest.mark.parametrize("precond", [1, 2])
+def test_noalloc_bicgstab_matches_workspace_solver_twice(pkg, gpu, precond):
+    """Jacobi (1) and 3x3 block-Jacobi (2): both carve their preconditioner out of the
+    fixed scratch."""
     problem_mod, solver_mod = gpu
     capi = importlib.import_module("jax-cpfem_gb300._capi")
     lib = capi.load()
@@ -34,13 +37,13 @@ def test_noalloc_bicgstab_matches_workspace_solver_twice(pkg, gpu):
     res, A = solver_mod.newton_update_helper(prob, u)
     b = torch.neg(res)
     x0 = solver_mod.initial_increment(prob, u).clone()
-    x_ref, k_ref, ok_ref = solver_mod.bicgstab(prob, A, b, x0, precond=1)
+    x_ref, k_ref, ok_ref = solver_mod.bicgstab(prob, A, b, x0, precond=precond)
     assert ok_ref and k_ref > 0
     stream = torch.cuda.current_stream().cuda_stream
     for call in range(2):
         x = x0.clone()
         info = np.zeros(2, dtype=np.int32)
-        rc = lib.cpfem_bicgstab_noalloc(prob.sell, A.values.data_ptr(), b.data_ptr(), x.data_ptr(), 1, 0,
+        rc = lib.cpfem_bicgstab_noalloc(prob.sell, A.values.data_ptr(), b.data_ptr(), x.data_ptr(), precond, 0,
                                         1e-10, 1e-10, 10000, info.ctypes.data, stream)
         capi.check(rc)
         assert info[1] == 1 and info[0] == k_ref, (call, info, k_ref)
