@@ -17,47 +17,43 @@ and writes ``golden.npz``.  The Neper meshes (20^3 of case 4, 16^3 of the 304-st
 10^3 of the tantalum VTUs) are checked to be structured boxes with x-fastest node
 numbering, so only per-cell grain ids are stored.  The VTU fields are float32 (meshio).
 
-Usage: python tests/golden/make_golden.py [reference_root]
+The Neper mesh is read with the package's own gmsh 2.2 reader (``mesh.read_gmsh22``).
+
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT
+       (or set CPFEM_REFERENCE_ROOT to the reference checkout)
 """
+import importlib
 import os
 import sys
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 
-def read_msh(path):
-    lines = open(path).read().split("\n")
-    i = lines.index("$Nodes")
-    n = int(lines[i + 1])
-    pts = np.array([[float(v) for v in lines[i + 2 + k].split()[1:4]] for k in range(n)])
-    i = lines.index("$Elements")
-    m = int(lines[i + 1])
-    cells, tags = [], []
-    for k in range(m):
-        p = [int(v) for v in lines[i + 2 + k].split()]
-        if p[1] == 5:
-            tags.append(p[3])
-            cells.append(p[3 + p[2]:3 + p[2] + 8])
-    return pts, np.array(cells) - 1, np.array(tags) - 1
+def reference_root():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CPFEM_REFERENCE_ROOT")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set CPFEM_REFERENCE_ROOT): the reference checkout")
+    return ref
 
 
 def main():
+    REF = reference_root()
+    mesh_mod = importlib.import_module("jax-cpfem_gb300.mesh")
     c = os.path.join(REF, "calibration/data/csv")
     case1 = np.loadtxt(os.path.join(c, "calibration_case1/stress_strain_curve_copper.txt"))
     case2 = np.loadtxt(os.path.join(c, "calibration_case2/ss_curve_e-2.txt"))
     c4zz = np.loadtxt(os.path.join(c, "calibration_case4/UQ/stress_zz_curve_scenario0.txt"))
     c4xx = np.loadtxt(os.path.join(c, "calibration_case4/UQ/stress_xx_curve_scenario1.txt"))
     quat = np.loadtxt(os.path.join(c, "calibration_case4/quat.txt"))[:50, 1:]
-    pts, cells, grains = read_msh(os.path.join(REF, "calibration/data/neper/calibration_case4/UQ/n50-id0.msh"))
-    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    msh, grains = mesh_mod.read_gmsh22(os.path.join(REF, "calibration/data/neper/calibration_case4/UQ/n50-id0.msh"))
+    pts, cells = msh.points, msh.cells
     from oracle.cpfem_oracle import box_mesh
     bp, bc = box_mesh(20, 20, 20, 0.0295, 0.0295, 0.0295)
     assert np.abs(bp - pts).max() < 1e-9, "case4 mesh is not the structured box"
     assert (bc == cells).all(), "case4 connectivity differs from the structured box"
-    import importlib
     vtu = importlib.import_module("jax-cpfem_gb300.vtu")
     vdir = os.path.join(REF, "polycrystal_304steel/data/vtk/polycrystal_304steel")
     st = [vtu.read_vtu(os.path.join(vdir, f"u_{i:03d}.vtu")) for i in range(16)]

@@ -1,6 +1,7 @@
 """Mesh and result file formats on the host: the gmsh 2.2 reader (Neper voxel meshes) and
 the VTU writer/reader (meshio's inline-binary layout)."""
 import importlib
+import os
 
 import numpy as np
 import pytest
@@ -63,3 +64,34 @@ def test_vtu_round_trip(io, tmp_path, compress):
     text = f.read_text()
     assert text.startswith('<?xml version="1.0"?>') and 'type="UnstructuredGrid"' in text
     assert ("vtkZLibDataCompressor" in text) == compress
+
+
+# The reference's own Neper meshes, read where the reference checkout is available (set
+# CPFEM_REFERENCE_ROOT to it; the golden fixtures were generated the same way).
+_REF = os.environ.get("CPFEM_REFERENCE_ROOT")
+NEPER_MESHES = [("calibration/data/neper/calibration_case4/UQ/n50-id0.msh", 20, 0.0295, 50),
+                ("singlecrystal_tantalum/data/neper/singlecrystal_tantalum/mesh10.msh", 10, None, 1),
+                ("polycrystal_DPsteel/data/neper/polycrystal_DPsteel/n1-id0-mesh16.msh", 16, None, 1),
+                ("crystal_plasticity_OR_design/data/neper/sensitivity/mesh2.msh", 2, None, None)]
+
+
+@pytest.mark.skipif(not (_REF and os.path.isdir(_REF)), reason="CPFEM_REFERENCE_ROOT is not set")
+@pytest.mark.parametrize("rel,n,L,grains", NEPER_MESHES)
+def test_gmsh22_reader_on_reference_neper_meshes(io, rel, n, L, grains):
+    """Neper voxel meshes of the reference: a structured n^3 box numbered x fastest with
+    gmsh-ordered HEX8 cells (what the multigrid levels and the golden fixtures assume), and
+    the physical tag minus one as the grain (``calibration_case4_..._1D_GB.py:116``)."""
+    mesh_mod, _ = io
+    m, g = mesh_mod.read_gmsh22(os.path.join(_REF, rel))
+    assert m.cells.shape == (n ** 3, 8)
+    assert mesh_mod.structured_dims(m.points) == (n + 1, n + 1, n + 1)
+    Lx = float(m.points[:, 0].max()) if L is None else L
+    box = mesh_mod.box_mesh(n, n, n, Lx, Lx, Lx)
+    assert np.abs(box.points - m.points).max() < 1e-9 * max(Lx, 1.0)
+    assert np.array_equal(box.cells, m.cells)
+    assert g.min() >= 0
+    if grains is not None:
+        assert g.max() + 1 == grains
+    if rel.startswith("calibration"):
+        gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden.npz"))
+        assert np.array_equal(g, gold["case4_grain"])
