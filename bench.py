@@ -32,8 +32,16 @@ METRIC = "GP updates/s; 32³ RVE s/load-step; grad÷fwd & batched÷serial time a
 UNIT = "GP updates/s"
 N_EDGE, N_GRAINS, SEED = 32, 64, 0
 STRAIN_STEP, DT = 1e-3, 0.1
-# Newton stop rule of both arms: the reference's (crystal_plasticity_OR_design/solver.py:384-385)
-NEWTON = {"tol": 1e-6, "rel_tol": 1e-8}
+# Newton stop rule.  The CPU arm runs the reference's (tol 1e-6, rel_tol 1e-8,
+# crystal_plasticity_OR_design/solver.py:384-385).  The GPU arm stops at an absolute residual
+# of 1e-8 instead (same rel_tol): its Newton loop starts from an extrapolated guess and can
+# stop after a different iterate than the reference's, and at the tighter limit its solution
+# stays within 1e-8 of the discrete solution (the oracle converged to 1e-12), which the
+# reference's own limit does not guarantee; in the steady state the last iterate is already
+# far below either limit, so this costs no Newton iteration there.
+NEWTON_REF = {"tol": 1e-6, "rel_tol": 1e-8}
+BENCH = importlib.import_module("jax-cpfem_gb300.workloads").BENCH_SETTINGS
+NEWTON = dict(BENCH["newton"])
 
 
 def workload_config(n=N_EDGE, config="c1"):
@@ -103,7 +111,7 @@ def oracle_load_step(orc, w, i, sol, params):
     orc.dt = w.dt
     orc.set_bcs(w.bc_triples(w.strain_step * i))
     orc.set_params(params)
-    sol, info = O.solver(orc, dict(NEWTON, initial_guess=sol))
+    sol, info = O.solver(orc, dict(NEWTON_REF, initial_guess=sol))
     sig = orc.compute_avg_stress(sol, params)
     params = orc.update_int_vars_gp(sol, params)
     return sol, params, sig, info
@@ -334,7 +342,9 @@ def run_reference(args):
     out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": dict(workload_config(args.edge), precond="jacobi"), "impl": "reference",
+           "config": dict(workload_config(args.edge), precond="jacobi", initial_guess="last solution",
+                          newton=f"tol {NEWTON_REF['tol']:g} / rel_tol {NEWTON_REF['rel_tol']:g}"),
+           "impl": "reference",
            "cpu_baseline": cb,
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "s_per_load_step": per_step, "newton_iters_per_step": newton, "krylov_iters": krylov,
@@ -486,6 +496,15 @@ def main():
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"],
                     help="c1 (default): 32^3 FCC polycrystal; c0: 10^3 copper single crystal; "
                          "c2: 64^3 BCC24 polycrystal; c3: adjoint on c1; c4: 256-RVE batch")
+    ap.add_argument("--fp32-tangent", default=int(BENCH["fp32_tangent"]), type=int, choices=[0, 1],
+                    help="consistent tangent (the global Newton's Jacobian) in FP32 where the local Jacobian's scale "
+                         "allows (1, default) or FP64 (0); the residual and the converged state are FP64 either way")
+    ap.add_argument("--predictor", default=BENCH["predictor"], choices=["linear", "previous"],
+                    help="initial guess of each load step's Newton solve: linear extrapolation of the last two "
+                         "solutions (default) or the last solution (the reference driver's)")
+    ap.add_argument("--krylov-tol", type=float, default=BENCH["krylov_tol"],
+                    help="relative tolerance of each Newton step's BiCGSTAB (the reference's: 1e-10; atol stays "
+                         "1e-10): an inexact Newton step with the same Newton stop rule")
     ap.add_argument("--load-steps", type=int, default=0)
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--fd-check", action="store_true")
@@ -523,13 +542,15 @@ def main():
     counter = CountingLib(prob.lib)
     prob.lib = counter
     W = _workloads()
-    st = W.LoadStepper(prob, solver_mod, w)
+    st = W.LoadStepper(prob, solver_mod, w, predictor=args.predictor)
+    prob.fp32_tangent = bool(args.fp32_tangent)
     mg_options = {"refresh": args.mg_refresh}
     if args.mg_precision:
         mg_options["precision"] = args.mg_precision
 
-    def set_solver(precond, mg, grid_blocks):
-        st.options = dict(NEWTON, jax_solver={"precond": precond, "mg_options": mg, "grid_blocks": grid_blocks})
+    def set_solver(precond, mg, grid_blocks, krylov_tol=args.krylov_tol, newton=NEWTON):
+        st.options = dict(newton, jax_solver={"precond": precond, "mg_options": mg, "grid_blocks": grid_blocks,
+                                              "tol": krylov_tol})
 
     set_solver(args.precond, mg_options, 0)
     clk = ClockSampler(local).start()
@@ -569,6 +590,9 @@ def main():
     prob.stats["krylov_iters"] = []
     passes0 = prob.stats["gp_passes"]
     newton = []
+    # the state at the start of the timed steps: the end-to-end run repeats the same load
+    # steps from it
+    start = (st.i, st.sol.clone(), None if st.prev is None else st.prev.clone(), [t.clone() for t in st.params])
     # the committed state at the start of the first timed step (copied before the clock
     # starts): the CPU baseline runs that same load step from it
     snap = None
@@ -600,6 +624,7 @@ def main():
     # end-to-end through the public API with pinned host buffers
     e2e = None
     if not args.no_e2e:
+        st.i, st.sol, st.prev, st.params = start[0], start[1], start[2], list(start[3])
         sol_h = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64).pin_memory()
         sol_h.copy_(st.sol.cpu())
         sig_h = torch.zeros(prob.num_cells * 9, dtype=torch.float64).pin_memory()
@@ -613,24 +638,39 @@ def main():
                "h2d_bytes_per_step": int(sol_h.numel() * 8), "d2h_bytes_per_step": int((sol_h.numel() + sig_h.numel()) * 8),
                "s_per_load_step": te / args.steps}
 
-    # the same load steps with the reference's Jacobi-preconditioned BiCGSTAB, for comparison
-    jacobi = None
-    if args.precond != 1 and not args.no_jacobi_leg:
-        saved = st.options
-        set_solver(1, None, 0)
-        st.step()
-        torch.cuda.synchronize()
-        k0 = len(prob.stats["krylov_iters"])
-        j0, j1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        j0.record()
-        for _ in range(2):
+    # the next load steps with the reference driver's own choices, for comparison: its initial
+    # guess (the last solution) with this arm's solver, then also its Jacobi-preconditioned
+    # BiCGSTAB (the drop-in's default configuration)
+    legs = {}
+    if not args.no_jacobi_leg:
+        saved, pred, f32t = st.options, st.predictor, prob.fp32_tangent
+        prob.fp32_tangent = False
+        for name, precond in (("previous_guess", args.precond), ("jacobi", 1)):
+            if precond == 1:
+                set_solver(1, None, 0, 1e-10, NEWTON_REF)
+            else:
+                set_solver(args.precond, st.options["jax_solver"]["mg_options"], st.options["jax_solver"]["grid_blocks"],
+                           1e-10, NEWTON_REF)
+            st.predictor = "previous"
             st.step()
-        j1.record()
-        torch.cuda.synchronize()
-        jacobi = {"precond": "jacobi (the reference's)", "steps": 2,
-                  "ms_per_step": max_over_ranks(j0.elapsed_time(j1) * 1e-3, world, "cuda") / 2 * 1e3,
-                  "krylov_iters": [int(k) for k in prob.stats["krylov_iters"][k0:]]}
-        st.options = saved
+            torch.cuda.synchronize()
+            k0 = len(prob.stats["krylov_iters"])
+            nl = []
+            j0, j1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            j0.record()
+            for _ in range(2):
+                st.step()
+                nl.append(prob.stats["newton_iters"])
+            j1.record()
+            torch.cuda.synchronize()
+            legs[name] = {"initial_guess": "last solution (the reference driver's)", "krylov_tol": 1e-10,
+                          "newton": "tol 1e-6 / rel_tol 1e-8 (the reference's)",
+                          "tangent": "fp64",
+                          "precond": {1: "jacobi (the reference's)", 3: "multigrid-vcycle"}.get(precond, precond),
+                          "steps": 2, "ms_per_step": max_over_ranks(j0.elapsed_time(j1) * 1e-3, world, "cuda") / 2 * 1e3,
+                          "newton_iters_per_step": nl, "krylov_iters": [int(k) for k in prob.stats["krylov_iters"][k0:]]}
+        st.options, st.predictor, prob.fp32_tangent = saved, pred, f32t
+    jacobi = legs.get("jacobi")
 
     # roofline of the dominant kernel (the persistent BiCGSTAB) and of the constitutive pass
     peaks = measured_peaks()
@@ -691,11 +731,15 @@ def main():
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": dict(workload_config(n, args.config), parallelism="replicas" if world > 1 else "single-gpu",
                           precond={0: "none", 1: "jacobi", 2: "block-jacobi-3x3", 3: "multigrid-vcycle"}[args.precond],
+                          krylov_tol=args.krylov_tol, tangent="fp32 (fp64 where the local scale test fails)"
+                          if args.fp32_tangent else "fp64",
+                          initial_guess={"linear": "linear extrapolation of the last two solutions",
+                                         "previous": "last solution"}[args.predictor],
                           mg_refresh=args.mg_refresh if args.precond == 3 else None),
            "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
            "roofline": dominant,
            "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof},
-           "region_shares": shares, "jacobi_leg": jacobi, "tuned_linear_solver": tuned,
+           "region_shares": shares, "reference_choice_legs": legs, "tuned_linear_solver": tuned,
            "cpu_baseline": cpu,
            "regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
            "newton_iters_per_step": newton, "krylov_iters": krylov, "gp_passes": passes,
@@ -722,7 +766,7 @@ class CountingLib:
     """Forwards to the C ABI and counts the kernels its calls launch (a fixed number per
     entry point, from the sources: the persistent BiCGSTAB is one launch plus the
     preconditioner set-up; every other listed entry point launches one kernel)."""
-    LAUNCHES = {"cpfem_gp_eval": 1, "cpfem_elem_assemble": 1, "cpfem_apply_dirichlet": 1, "cpfem_dot": 1,
+    LAUNCHES = {"cpfem_gp_eval": 1, "cpfem_elem_assemble": 1, "cpfem_elem_assemble_ex": 1, "cpfem_apply_dirichlet": 1, "cpfem_dot": 1,
                 "cpfem_bc_initial_guess": 1, "cpfem_axpy": 1, "cpfem_spmv": 1, "cpfem_bicgstab": 2,
                 "cpfem_bicgstab_ex": 2, "cpfem_cell_average": 1, "cpfem_segmented_dot": 1,
                 "cpfem_bicgstab_batched": 2, "cpfem_gp_vjp": 1}

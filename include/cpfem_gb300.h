@@ -107,7 +107,11 @@ typedef struct {
                                  2: Newton directions from an FP32 Jacobian / LU while the
                                    Jacobian's scale max_a d(dgamma_a)/d(tau_a) C11 <= 1e4
                                    (else FP64); the residual, its stop test and the tangent
-                                   stay FP64, so the converged state is the same root.
+                                   stay FP64, so the converged state is the same root;
+                                 4: the consistent tangent (dP/dF, and ds/dF for the
+                                   prediction) in FP32 under the same scale test (else
+                                   FP64): it is only the global Newton's Jacobian, so the
+                                   converged solution is unchanged.
                                  0 with s_warm = NULL: the reference's iterates. */
   const int32_t* order;       /* [num_gp] permutation or NULL (no cell list): thread t
                                  evaluates GP order[t].  Ordering GPs by their previous
@@ -262,6 +266,15 @@ int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* s
  * fixed).  With a list of cells that share no node (one colour of cpfem_color_cells) the
  * listed cells add without atomics; calling the colours in order gives a bitwise
  * reproducible assembly. */
+/* The same with the element stiffness formed in FP32 (k_precision = 1; 0 is FP64) and added
+ * to the FP64 values: for a tangent that only serves as the global Newton's Jacobian, so
+ * the FP64 residual and its stop rule decide the converged solution.  FP32 applies with a
+ * cell list (the coloured scatter); the residual is FP64 either way. */
+int cpfem_elem_assemble_ex(int32_t num_cells, const int32_t* cells, const double* shape_grads,
+                           const cpfem_sell_t* sell, const uint8_t* elem_pos,
+                           const int32_t* cell_list, int32_t num_listed,
+                           const double* pk1_w, const double* tangent_w,
+                           double* residual, double* values, int32_t k_precision, void* stream);
 
 /* Greedy cell colouring (host): cells of one colour share no node.  color [num_cells]. */
 int cpfem_color_cells(int32_t num_cells, const int32_t* cells, int32_t num_nodes, int32_t* color,

@@ -171,6 +171,7 @@ SIGNATURES = {
     "cpfem_gp_eval": (ctypes.c_int, [ctypes.POINTER(Material), ctypes.POINTER(GPArgs), _P]),
     "cpfem_gp_vjp": (ctypes.c_int, [ctypes.POINTER(Material), ctypes.POINTER(VjpArgs), _P]),
     "cpfem_elem_assemble": (ctypes.c_int, [_I32, _P, _P, _SP, _P, _P, _I32, _P, _P, _P, _P, _P]),
+    "cpfem_elem_assemble_ex": (ctypes.c_int, [_I32, _P, _P, _SP, _P, _P, _I32, _P, _P, _P, _P, _I32, _P]),
     "cpfem_color_cells": (ctypes.c_int, [_I32, _P, _I32, _P, _P]),
     "cpfem_apply_dirichlet": (ctypes.c_int, [_I32, _P, _P, _P, _P, _SP, _P, _P]),
     "cpfem_bc_initial_guess": (ctypes.c_int, [_I64, _I32, _P, _P, _P, _P, _P]),

@@ -56,7 +56,8 @@ int make_matdev(const cpfem_material_t* m, MatDev* o) {
 // ------------------------------------------------------------------------------------
 // Constitutive pass: one thread per Gauss point.
 // ------------------------------------------------------------------------------------
-template <int NS, bool TANGENT>
+// TMODE: 0 no tangent, 1 FP64 tangent, 2 FP32 tangent (FP64 where the scale test fails)
+template <int NS, int TMODE>
 __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_args_t a) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t G = a.num_gp;
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
     for (int c = 0; c < 9; ++c) a.s_out[c * G + gp] = Sg[c];
   }
   if (a.iters != nullptr) a.iters[gp] = st.iters;
-  if (TANGENT && a.tangent != nullptr) {
+  if (TMODE != 0 && a.tangent != nullptr) {
     double* tan = a.tangent;
     const bool keep_dsdf = predict && st.rn <= m.local_tol;
     auto store = [&](int kl, const double* col, const double* dsdf) {
@@ -218,14 +219,19 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
 #pragma unroll
         for (int k = 0; k < 6; ++k) a.s_dsdf[(6 * kl + k) * G + gp] = dsdf[k];
     };
-    cp_tangent<NS>(m, cc, F, Gm, st, H, W, Y, idet, store);
+    if (TMODE == 2 && tangent_f32_ok<NS>(st, cc))
+      cp_tangent_t<NS, float>(m, cc, F, Gm, st, H, W, Y, idet, store);
+    else
+      cp_tangent<NS>(m, cc, F, Gm, st, H, W, Y, idet, store);
   }
 }
 
 // ------------------------------------------------------------------------------------
 // Element residual / tangent: one thread per (cell, node a) owns rows (a, 0..2).
+// KT is the precision of the element stiffness arithmetic (FP64, or FP32 for a tangent
+// that only serves as the Newton Jacobian); the residual is always FP64.
 // ------------------------------------------------------------------------------------
-template <bool WITH_K, bool ATOMIC>
+template <bool WITH_K, bool ATOMIC, typename KT = double>
 __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ clist,
                                                        int32_t ncl, const int32_t* __restrict__ cells,
                                                        const double* __restrict__ sg,
@@ -241,13 +247,13 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
   if (li >= ncl) return;
   const int64_t e = (clist != nullptr) ? clist[li] : li;
   const int64_t G = (int64_t)E * 8;
-  double K[3][24];
+  KT K[3][24];
   double Rr[3] = {0.0, 0.0, 0.0};
   if (WITH_K) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int c = 0; c < 24; ++c) K[i][c] = 0.0;
+      for (int c = 0; c < 24; ++c) K[i][c] = KT(0);
   }
 #pragma unroll 1
   for (int q = 0; q < 8; ++q) {
@@ -258,23 +264,24 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
     for (int i = 0; i < 3; ++i)
       Rr[i] = fma(Pw[(3 * i) * G + gp], ga0, fma(Pw[(3 * i + 1) * G + gp], ga1, fma(Pw[(3 * i + 2) * G + gp], ga2, Rr[i])));
     if (WITH_K) {
-      double Gm[27];
+      const KT a0 = (KT)ga0, a1 = (KT)ga1, a2 = (KT)ga2;
+      KT Gm[27];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int kL = 0; kL < 9; ++kL)
-          Gm[9 * i + kL] = fma(ga0, Dw[(int64_t)(9 * (3 * i + 0) + kL) * G + gp],
-                           fma(ga1, Dw[(int64_t)(9 * (3 * i + 1) + kL) * G + gp],
-                               ga2 * Dw[(int64_t)(9 * (3 * i + 2) + kL) * G + gp]));
+          Gm[9 * i + kL] = cp_fma(a0, (KT)Dw[(int64_t)(9 * (3 * i + 0) + kL) * G + gp],
+                           cp_fma(a1, (KT)Dw[(int64_t)(9 * (3 * i + 1) + kL) * G + gp],
+                                  a2 * (KT)Dw[(int64_t)(9 * (3 * i + 2) + kL) * G + gp]));
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
-        const double gb0 = sgq[3 * b], gb1 = sgq[3 * b + 1], gb2 = sgq[3 * b + 2];
+        const KT gb0 = (KT)sgq[3 * b], gb1 = (KT)sgq[3 * b + 1], gb2 = (KT)sgq[3 * b + 2];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            K[i][3 * b + k] = fma(Gm[9 * i + 3 * k], gb0, fma(Gm[9 * i + 3 * k + 1], gb1,
-                              fma(Gm[9 * i + 3 * k + 2], gb2, K[i][3 * b + k])));
+            K[i][3 * b + k] = cp_fma(Gm[9 * i + 3 * k], gb0, cp_fma(Gm[9 * i + 3 * k + 1], gb1,
+                              cp_fma(Gm[9 * i + 3 * k + 2], gb2, K[i][3 * b + k])));
       }
     }
   }
@@ -297,8 +304,8 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           double* v = &vals[base + 32 * (9 * pos + 3 * i + k)];
-          if (ATOMIC) atomicAdd(v, K[i][3 * b + k]);
-          else *v += K[i][3 * b + k];
+          if (ATOMIC) atomicAdd(v, (double)K[i][3 * b + k]);
+          else *v += (double)K[i][3 * b + k];
         }
     }
   }
@@ -388,10 +395,12 @@ static int launch_gp(const MatDev& md, const cpfem_gp_args_t& a, cudaStream_t s)
   const int64_t work = a.cell_list != nullptr ? 8 * (int64_t)a.num_listed : a.num_gp;
   if (work == 0) return CPFEM_OK;
   const unsigned blocks = (unsigned)ceil_div(work, threads);
-  if (a.tangent != nullptr)
-    k_gp_eval<NS, true><<<blocks, threads, 0, s>>>(md, a);
+  if (a.tangent != nullptr && (a.local_flags & 4))
+    k_gp_eval<NS, 2><<<blocks, threads, 0, s>>>(md, a);
+  else if (a.tangent != nullptr)
+    k_gp_eval<NS, 1><<<blocks, threads, 0, s>>>(md, a);
   else
-    k_gp_eval<NS, false><<<blocks, threads, 0, s>>>(md, a);
+    k_gp_eval<NS, 0><<<blocks, threads, 0, s>>>(md, a);
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;
 }
@@ -437,6 +446,14 @@ int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* s
                         const cpfem_sell_t* sell, const uint8_t* elem_pos, const int32_t* cell_list,
                         int32_t num_listed, const double* pk1_w, const double* tangent_w, double* residual,
                         double* values, void* stream) {
+  return cpfem_elem_assemble_ex(num_cells, cells, shape_grads, sell, elem_pos, cell_list, num_listed, pk1_w,
+                                tangent_w, residual, values, 0, stream);
+}
+
+int cpfem_elem_assemble_ex(int32_t num_cells, const int32_t* cells, const double* shape_grads,
+                           const cpfem_sell_t* sell, const uint8_t* elem_pos, const int32_t* cell_list,
+                           int32_t num_listed, const double* pk1_w, const double* tangent_w, double* residual,
+                           double* values, int32_t k_precision, void* stream) {
   if (num_cells == 0) return CPFEM_OK;
   CPFEM_REQUIRE(num_cells > 0 && cells && shape_grads && pk1_w, "bad element arguments");
   CPFEM_REQUIRE((values == nullptr) == (tangent_w == nullptr), "values and tangent_w go together");
@@ -448,8 +465,13 @@ int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* s
   const unsigned blocks = (unsigned)ceil_div((int64_t)ncl * 8, threads);
   cudaStream_t s = (cudaStream_t)stream;
   const int64_t* goff = (values != nullptr) ? sell->group_off : nullptr;
+  CPFEM_REQUIRE(k_precision == 0 || k_precision == 1, "k_precision must be 0 (FP64) or 1 (FP32)");
   if (cell_list != nullptr) {
-    if (values != nullptr)
+    if (values != nullptr && k_precision == 1)
+      k_elem_assemble<true, false, float><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads,
+                                                                    goff, elem_pos, pk1_w, tangent_w, residual,
+                                                                    values);
+    else if (values != nullptr)
       k_elem_assemble<true, false><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads, goff,
                                                              elem_pos, pk1_w, tangent_w, residual, values);
     else

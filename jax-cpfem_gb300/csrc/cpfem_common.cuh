@@ -88,6 +88,32 @@ CPFEM_HD void mm3_at(const double* A, const double* B, double* C) {
       C[3 * i + j] = fma(A[0 + i], B[0 + j], fma(A[3 + i], B[3 + j], A[6 + i] * B[6 + j]));
 }
 
+// FP32 versions of the 3x3 helpers, for the single-precision consistent tangent.
+CPFEM_HD void mm3(const float* A, const float* B, float* C) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      C[3 * i + j] = fmaf(A[3 * i + 0], B[0 + j], fmaf(A[3 * i + 1], B[3 + j], A[3 * i + 2] * B[6 + j]));
+}
+
+CPFEM_HD void inv3(const float* A, float* Ai) {
+  const float c00 = A[4] * A[8] - A[5] * A[7];
+  const float c01 = A[5] * A[6] - A[3] * A[8];
+  const float c02 = A[3] * A[7] - A[4] * A[6];
+  const float det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+  const float id = 1.0f / det;
+  Ai[0] = c00 * id;
+  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+  Ai[3] = c01 * id;
+  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+  Ai[6] = c02 * id;
+  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+}
+
 CPFEM_HD double det3(const double* A) {
   return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
          A[2] * (A[3] * A[7] - A[4] * A[6]);
@@ -122,6 +148,16 @@ CPFEM_HD void cubic_apply(const Cub& m, const double* e, double* t) {
   t[1] = fma(m.C11, e[1], m.C12 * (e[0] + e[2]));
   t[2] = fma(m.C11, e[2], m.C12 * (e[0] + e[1]));
   const double c2 = 2.0 * m.C44;
+  t[3] = c2 * e[3];
+  t[4] = c2 * e[4];
+  t[5] = c2 * e[5];
+}
+
+CPFEM_HD void cubic_apply(const Cub& m, const float* e, float* t) {
+  const float c11 = (float)m.C11, c12 = (float)m.C12, c2 = (float)(2.0 * m.C44);
+  t[0] = fmaf(c11, e[0], c12 * (e[1] + e[2]));
+  t[1] = fmaf(c11, e[1], c12 * (e[0] + e[2]));
+  t[2] = fmaf(c11, e[2], c12 * (e[0] + e[1]));
   t[3] = c2 * e[3];
   t[4] = c2 * e[4];
   t[5] = c2 * e[5];

@@ -292,37 +292,62 @@ CPFEM_HD void cp_stress(const double* F, const double* G /*Fp^-1_old R*/, const 
   mm3(F, Y, P);
 }
 
+// Slip tables in the precision of a tangent computation.
+CPFEM_HD double tan_p9(const MatDev& m, double, int a, int k) { return m.p9[a][k]; }
+CPFEM_HD float tan_p9(const MatDev& m, float, int a, int k) { return m.d32[a][k / 3] * m.n32[a][k % 3]; }
+CPFEM_HD double tan_pv(const MatDev& m, double, int a, int j) { return m.pv[a][j]; }
+CPFEM_HD float tan_pv(const MatDev& m, float, int a, int j) { return m.pv32[a][j]; }
+
+template <int NS>
+CPFEM_HD void tan_jacobian(const MatDev& m, const Cub& cc, const double* kk, const double* M, double* J) {
+  cp_jacobian<NS>(m, cc, kk, M, J);
+}
+template <int NS>
+CPFEM_HD void tan_jacobian(const MatDev& m, const Cub& cc, const double* kk, const double* M, float* J) {
+  cp_jacobian_f32<NS>(m, cc, kk, M, J);
+}
+
 // Consistent tangent at the converged state:
 // dP/dF = d_ik Y_lJ + (dP/ds)(ds/dF) with ds/dF = J^-1 C : sym(Fe_l[k,:] (x) H[l,:]),
 // the implicit-function tangent of f_jvp (models_copper.py:251-259).
 // The tangent column for F_kl is handed to store_col(kl, col[9], ds/dF_kl[6]) as soon as
 // it is known, so the 81 entries never need to be live at once.  Called after every other
 // output of the Gauss point is written, so only what it needs is live.
-template <int NS, class StoreCol>
-CPFEM_HD void cp_tangent(const MatDev& m, const Cub& cc, const double* F, const double* G /*Fp^-1_old R*/,
-                         const GPSolve<NS>& st, const double* H, const double* W, const double* Y, double idet,
-                         StoreCol store_col) {
+// T is the precision of the computation: FP64, or FP32 for a tangent that only serves as
+// the global Newton's Jacobian and the local solve's start prediction (the converged
+// state and stress, and the residual that decides convergence, stay FP64 either way).
+template <int NS, typename T, class StoreCol>
+CPFEM_HD void cp_tangent_t(const MatDev& m, const Cub& cc, const double* F64, const double* G64,
+                           const GPSolve<NS>& st, const double* H64, const double* W64, const double* Y64,
+                           double idet64, StoreCol store_col) {
+  T F[9], G[9], H[9], W[9], Y[9], B[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    F[k] = (T)F64[k]; G[k] = (T)G64[k]; H[k] = (T)H64[k]; W[k] = (T)W64[k]; Y[k] = (T)Y64[k];
+    B[k] = (T)st.B[k];
+  }
+  const T idet = (T)idet64;
   // dP/ds for the 6 symmetric basis directions
-  double Bi[9];
-  inv3(st.B, Bi);
-  double dPds[6][9];
+  T Bi[9];
+  inv3(B, Bi);
+  T dPds[6][9];
 #pragma unroll
   for (int mm = 0; mm < 6; ++mm) {
-    double dL[9];
+    T dL[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) dL[k] = 0.0;
+    for (int k = 0; k < 9; ++k) dL[k] = T(0);
 #pragma unroll
     for (int a = 0; a < NS; ++a) {
-      const double c = st.kk[a] * m.pv[a][mm];
+      const T c = (T)st.kk[a] * tan_pv(m, T(0), a, mm);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) dL[k] = fma(c, m.p9[a][k], dL[k]);
+      for (int k = 0; k < 9; ++k) dL[k] = cp_fma(c, tan_p9(m, T(0), a, k), dL[k]);
     }
-    double trace = 0.0;
+    T trace = T(0);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) trace = fma(Bi[3 * i + j], dL[3 * j + i], trace);
-    double dH[9], V[9], dY[9];
+      for (int j = 0; j < 3; ++j) trace = cp_fma(Bi[3 * i + j], dL[3 * j + i], trace);
+    T dH[9], V[9], dY[9];
     mm3(G, dL, dH);          // G dL  (= -dH)
     mm3(dH, W, V);           // V = (G dL) s H^T
     const int ei = (mm < 3) ? mm : ((mm == 3) ? 1 : 0);
@@ -331,51 +356,70 @@ CPFEM_HD void cp_tangent(const MatDev& m, const Cub& cc, const double* F, const 
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        double hh = H[3 * i + ei] * H[3 * j + ej];
-        if (mm >= 3) hh = fma(H[3 * i + ej], H[3 * j + ei], hh);
-        dY[3 * i + j] = fma(hh - V[3 * i + j] - V[3 * j + i], idet, Y[3 * i + j] * trace);
+        T hh = H[3 * i + ei] * H[3 * j + ej];
+        if (mm >= 3) hh = cp_fma(H[3 * i + ej], H[3 * j + ei], hh);
+        dY[3 * i + j] = cp_fma(hh - V[3 * i + j] - V[3 * j + i], idet, Y[3 * i + j] * trace);
       }
     mm3(F, dY, dPds[mm]);
   }
 
   // ds/dF column by column through the factorised Jacobian at the converged s
-  double J[36];
+  T J[36];
   int perm[6];
-  double dinv[6];
-  cp_jacobian<NS>(m, cc, st.kk, st.M, J);
+  T dinv[6];
+  tan_jacobian<NS>(m, cc, st.kk, st.M, J);
   lu_factor<6>(J, perm, dinv);
-  double Fe[9];
+  T Fe[9];
   mm3(F, H, Fe);
 #pragma unroll
   for (int kl = 0; kl < 9; ++kl) {
     const int k = kl / 3, l = kl % 3;
-    double a[3], b[3];
+    T a[3], b[3];
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
       a[t] = Fe[3 * k + t];
       b[t] = H[3 * l + t];
     }
-    double q[6], x[6];
+    T q[6], x[6];
     q[0] = a[0] * b[0];
     q[1] = a[1] * b[1];
     q[2] = a[2] * b[2];
-    q[3] = 0.5 * fma(a[1], b[2], a[2] * b[1]);
-    q[4] = 0.5 * fma(a[0], b[2], a[2] * b[0]);
-    q[5] = 0.5 * fma(a[0], b[1], a[1] * b[0]);
+    q[3] = T(0.5) * cp_fma(a[1], b[2], a[2] * b[1]);
+    q[4] = T(0.5) * cp_fma(a[0], b[2], a[2] * b[0]);
+    q[5] = T(0.5) * cp_fma(a[0], b[1], a[1] * b[0]);
     cubic_apply(cc, q, x);
     lu_solve<6>(J, perm, dinv, x);
-    double col[9];
+    double col[9], xd[6];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        double v = (i == k) ? Y[3 * l + j] : 0.0;
+        T v = (i == k) ? Y[3 * l + j] : T(0);
 #pragma unroll
-        for (int mm = 0; mm < 6; ++mm) v = fma(dPds[mm][3 * i + j], x[mm], v);
-        col[3 * i + j] = v;
+        for (int mm = 0; mm < 6; ++mm) v = cp_fma(dPds[mm][3 * i + j], x[mm], v);
+        col[3 * i + j] = (double)v;
       }
-    store_col(kl, col, x);
+#pragma unroll
+    for (int mm = 0; mm < 6; ++mm) xd[mm] = (double)x[mm];
+    store_col(kl, col, xd);
   }
+}
+
+template <int NS, class StoreCol>
+CPFEM_HD void cp_tangent(const MatDev& m, const Cub& cc, const double* F, const double* G, const GPSolve<NS>& st,
+                         const double* H, const double* W, const double* Y, double idet, StoreCol store_col) {
+  cp_tangent_t<NS, double>(m, cc, F, G, st, H, W, Y, idet, store_col);
+}
+
+// The FP32 tangent is used while the local Jacobian's scale max_a kk_a C11 is at most
+// kJ32Scale (as for the FP32 local directions), where its rounding leaves the tangent
+// accurate to ~1e-4 relative or better; stiffer points get the FP64 one.
+template <int NS>
+CPFEM_HD bool tangent_f32_ok(const GPSolve<NS>& st, const Cub& cc) {
+  double kmax = 0.0;
+#pragma unroll
+  for (int a = 0; a < NS; ++a) kmax = fmax(kmax, st.kk[a]);
+  return kmax * cc.C11 <= kJ32Scale;
 }
 
 // Explicit hardening and slip update after the local solve (models_copper.py:176-187;

@@ -214,6 +214,9 @@ class CrystalPlasticity:
         # Newton directions of the local solve from an FP32 Jacobian while its scale allows
         # (same residual, stop test and tangent in FP64: same converged state)
         self.fp32_local_jacobian = True
+        # the consistent tangent (the global Newton's Jacobian) in FP32 where the local
+        # Jacobian's scale allows; the residual and the converged state stay FP64
+        self.fp32_tangent = False
         self.custom_init(*additional_info)
 
     # ------------------------------------------------------------------ set-up
@@ -620,7 +623,8 @@ class CrystalPlasticity:
         else:
             a.elastic_table = _dev_ptr(self.elastic_table) if param_table is self.param_table else None
         a.weight_jxw = 1 if outs.pop("weight_jxw", False) else 0
-        a.local_flags = (1 if predict else 0) | (2 if (fast_local and self.fp32_local_jacobian) else 0)
+        a.local_flags = (1 if predict else 0) | (2 if (fast_local and self.fp32_local_jacobian) else 0) | \
+            (4 if (fast_local and self.fp32_tangent) else 0)
         cl = outs.pop("cell_list", None)
         if cl is not None:
             a.cell_list, a.num_listed = _dev_ptr(cl), int(cl.numel())
@@ -754,16 +758,19 @@ class CrystalPlasticity:
                 "slip_new": torch.empty((N, G), dtype=torch.float64, device=self.device)}
 
     def scatter(self, pw, dw, res, values):
-        """Element residual / tangent scatter, colour by colour (no atomics, fixed order)."""
+        """Element residual / tangent scatter, colour by colour (no atomics, fixed order);
+        the element stiffness in FP32 when the problem forms its tangent in FP32."""
         fe = self.fes[0]
         base = self.color_cells.data_ptr()
+        kp = 1 if (values is not None and self.fp32_tangent) else 0
         with self.region("elem_assemble"):
             for c in range(len(self.color_ptr) - 1):
                 c0, c1 = int(self.color_ptr[c]), int(self.color_ptr[c + 1])
-                _capi.check(self.lib.cpfem_elem_assemble(self.num_cells, _dev_ptr(fe.cells), _dev_ptr(fe.shape_grads),
-                                                         self.sell, _dev_ptr(self.elem_pos), base + 4 * c0, c1 - c0,
-                                                         _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res),
-                                                         _dev_ptr(values), _stream()))
+                _capi.check(self.lib.cpfem_elem_assemble_ex(self.num_cells, _dev_ptr(fe.cells),
+                                                            _dev_ptr(fe.shape_grads), self.sell,
+                                                            _dev_ptr(self.elem_pos), base + 4 * c0, c1 - c0,
+                                                            _dev_ptr(pw), _dev_ptr(dw), _dev_ptr(res),
+                                                            _dev_ptr(values), kp, _stream()))
 
     def apply_dirichlet(self, res, u, values=None):
         fe = self.fes[0]

@@ -192,5 +192,5 @@ def test_ad_wrapper_reference_loop(pkg, gpu):
     g = scale.grad.cpu().numpy()
     ref = np.array([tb[0] * theta[0], tb[1] * theta[1]])
     J = float(((s0 - target) ** 2).sum())
-    assert abs(float(obj) - J) < 1e-9 * J
+    assert abs(float(obj.detach()) - J) < 1e-9 * J
     assert np.abs(g - ref).max() < 1e-7 * np.abs(ref).max(), (g, ref)
