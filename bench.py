@@ -206,16 +206,23 @@ def measured_peaks():
         return {}
 
 
+FP64_PROBE = {"kernel": "k_dfma_probe", "threads": 256, "blocks_per_sm": 16, "chains_per_thread": 16,
+              "fma_per_loop_trip": 64, "loop_trips": 512, "repeats": 5}
+
+
 def fp64_peak(lib, torch):
-    """Measured FP64 FMA throughput of this GPU (TFLOP/s), from cpfem_probe_dfma."""
+    """Measured FP64 FMA throughput of this GPU (TFLOP/s), from cpfem_probe_dfma: the best
+    of FP64_PROBE["repeats"] timed launches (CUDA events), each ~10-20 ms of DFMAs."""
     out = torch.zeros(1, dtype=torch.float64, device="cuda")
     flops = np.zeros(1)
     sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks = FP64_PROBE["blocks_per_sm"] * sms
     best = 0.0
-    for _ in range(3):
+    lib.cpfem_probe_dfma(64, blocks, out.data_ptr(), flops.ctypes.data, torch.cuda.current_stream().cuda_stream)
+    for _ in range(FP64_PROBE["repeats"]):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        rc = lib.cpfem_probe_dfma(1024, 8 * sms, out.data_ptr(), flops.ctypes.data,
+        rc = lib.cpfem_probe_dfma(FP64_PROBE["loop_trips"], blocks, out.data_ptr(), flops.ctypes.data,
                                   torch.cuda.current_stream().cuda_stream)
         e1.record()
         torch.cuda.synchronize()
@@ -289,7 +296,7 @@ def krylov_iteration_cost(prob, precond=1):
     return bytes_it, flops_it, flops32_it
 
 
-def gp_flops_per_eval(num_slip, iters_mean, tangent=True, fp32_direction=True):
+def gp_flops_per_eval(num_slip, iters_mean, tangent=True, fp32_direction=True, fp32_tangent=False):
     """Algorithmic flops of one GP update (FMA = 2; pow, div, sqrt = 1 each), returned as
     (FP64, FP32): per local iteration one residual (tau 12N, power/slip 6N, L_p 18N, 3x3
     products and strain 130) in FP64, and one 6x6 Jacobian (per slip M^T d 18,
@@ -304,8 +311,9 @@ def gp_flops_per_eval(num_slip, iters_mean, tangent=True, fp32_direction=True):
     setup = 120 + residual
     tan = (jac + lu + 6 * (20 * N + 220) + 9 * 220) if tangent else 0
     direction = iters_mean * (jac + lu)
-    fp64 = setup + iters_mean * residual + tan + 60 + (0 if fp32_direction else direction)
-    return fp64, (direction if fp32_direction else 0.0)
+    fp64 = setup + iters_mean * residual + (0 if fp32_tangent else tan) + 60 + (0 if fp32_direction else direction)
+    fp32 = (direction if fp32_direction else 0.0) + (tan if fp32_tangent else 0.0)
+    return fp64, fp32
 
 
 def run_reference(args):
@@ -355,6 +363,11 @@ def run_reference(args):
 
 
 def run_adjoint_config(args, pkg, problem_mod, torch):
+    """configs[3] as its own JSON line."""
+    print(json.dumps(adjoint_record(args, pkg, problem_mod, torch)))
+
+
+def adjoint_record(args, pkg, problem_mod, torch):
     """configs[3]: gradient of the sigma_zz-curve misfit on the 32^3 / 64-grain RVE with
     respect to (h0, g0, gs, a, m) and the 64x3 Euler angles; backward / forward time."""
     from importlib import import_module
@@ -371,7 +384,9 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
     disps = STRAIN_STEP * np.arange(nsteps + 1)
     ts = DT * np.arange(nsteps + 1)
     # forward and transposed (adjoint) solves with the same preconditioner
-    mg = {"precision": args.mg_precision} if args.mg_precision else None
+    mg = dict(_workloads().TUNED_MG)
+    if args.mg_precision:
+        mg["precision"] = args.mg_precision
     h = adjoint.LoadHistory(prob, disps, ts, bc_fn, quat,
                             solver_options={"jax_solver": {"precond": args.precond, "mg_options": mg}},
                             adjoint_options={"precond": args.precond, "mg_options": mg})
@@ -417,7 +432,7 @@ def run_adjoint_config(args, pkg, problem_mod, torch):
         ad = float(tb @ d_t + (eb * d_e).sum())
         out["directional_fd_check"] = {"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(fd),
                                        "fd_local_solve": "S = 0 start, FP64 directions (the reference's iterates)"}
-    print(json.dumps(out))
+    return out
 
 
 def run_batch_config(args, pkg, torch):
@@ -485,6 +500,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--edge", type=int, default=N_EDGE, help="cube edge in cells (32 = the benchmark)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub-records", action="store_true",
+                    help="skip the configs[3] adjoint record appended to the default line")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
                     help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
@@ -592,7 +609,8 @@ def main():
     newton = []
     # the state at the start of the timed steps: the end-to-end run repeats the same load
     # steps from it
-    start = (st.i, st.sol.clone(), None if st.prev is None else st.prev.clone(), [t.clone() for t in st.params])
+    start = (st.i, st.sol.clone(), None if st.prev is None else st.prev.clone(), [t.clone() for t in st.params],
+             {k: prob._bufs[k].clone() for k in ("s_warm", "s_dsdf", "s_f", "gp_order") if k in prob._bufs})
     # the committed state at the start of the first timed step (copied before the clock
     # starts): the CPU baseline runs that same load step from it
     snap = None
@@ -624,7 +642,12 @@ def main():
     # end-to-end through the public API with pinned host buffers
     e2e = None
     if not args.no_e2e:
+        # the same load steps from the same state, local-solve starts included; the state is
+        # adopted before the clock starts
         st.i, st.sol, st.prev, st.params = start[0], start[1], start[2], list(start[3])
+        for k, v in start[4].items():
+            prob._bufs[k].copy_(v)
+        prob.set_params(st.params)
         sol_h = torch.zeros(prob.num_total_dofs_all_vars, dtype=torch.float64).pin_memory()
         sol_h.copy_(st.sol.cpu())
         sig_h = torch.zeros(prob.num_cells * 9, dtype=torch.float64).pin_memory()
@@ -680,7 +703,8 @@ def main():
     its_t = prob.stats.get("local_iters_mean", 6.0)
     gp_n, gp_ms = regions.get("gp_eval_tangent", (0, 0.0))
     gp_t = gp_ms * 1e-3 / max(gp_n, 1)
-    gp64, gp32 = gp_flops_per_eval(prob.num_slip, its_t, fp32_direction=prob.fp32_local_jacobian)
+    gp64, gp32 = gp_flops_per_eval(prob.num_slip, its_t, fp32_direction=prob.fp32_local_jacobian,
+                                   fp32_tangent=prob.fp32_tangent)
     gp_flops = G * gp64
     kr_n, kr_ms = regions.get("bicgstab", (0, 0.0))
     kr_its = sum(max(k, 0) for k in krylov)
@@ -717,7 +741,8 @@ def main():
                "unit": "TFLOP/s", "frac": (gp_flops / gp_t / 1e12) / fp64 if gp_t else None, "traffic": None,
                "kernel": "k_gp_eval<N,tangent>", "peak_source": "cpfem_probe_dfma (of measured)",
                "local_iters_mean": its_t, "fp64_flops_per_gp": gp64, "fp32_flops_per_gp": gp32,
-               "note": "FP64 flops counted with every local Newton direction in FP32 (a lower bound)"}
+               "note": "FP64 flops counted with every local Newton direction (and, with the FP32 tangent, every "
+                       "tangent) in FP32: a lower bound of the FP64 work"}
     shares = {"bicgstab": kr_ms / (t * 1e3), "gp_eval_tangent": gp_ms / (t * 1e3),
               "elem_assemble": regions.get("elem_assemble", (0, 0.0))[1] / (t * 1e3)}
     dominant = kr_roof if (kr_roof is not None and shares["bicgstab"] >= shares["gp_eval_tangent"]) else gp_roof
@@ -740,11 +765,15 @@ def main():
            "roofline": dominant,
            "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof},
            "region_shares": shares, "reference_choice_legs": legs, "tuned_linear_solver": tuned,
+           "fp64_peak": {"value": fp64, "unit": "TFLOP/s", "probe": FP64_PROBE},
            "cpu_baseline": cpu,
            "regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
            "newton_iters_per_step": newton, "krylov_iters": krylov, "gp_passes": passes,
            "gpu_launches": None}
     out["gpu_launches"] = counter.launches
+    if rank == 0 and world == 1 and args.config == "c1" and not args.no_sub_records:
+        # the differentiation form on the same RVE (configs[3]), after the timed region
+        out["sub_records"] = {"c3_adjoint": adjoint_record(args, pkg, problem_mod, torch)}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -763,9 +792,12 @@ def max_over_ranks(t, world, device):
 
 
 class CountingLib:
-    """Forwards to the C ABI and counts the kernels its calls launch (a fixed number per
-    entry point, from the sources: the persistent BiCGSTAB is one launch plus the
-    preconditioner set-up; every other listed entry point launches one kernel)."""
+    """Forwards to the C ABI and counts the kernels its calls launch, from the sources:
+    cpfem_bicgstab_ex is the persistent launch, plus the point preconditioner's set-up
+    (precond 1, 2) and the two true-residual kernels (flags bit 0); cpfem_mg_setup is the
+    level-0 block inverses, three directional Galerkin passes and a block inversion per
+    coarse level, and two FP32 copies per level for the FP32 V-cycle; every other listed
+    entry point launches one kernel."""
     LAUNCHES = {"cpfem_gp_eval": 1, "cpfem_elem_assemble": 1, "cpfem_elem_assemble_ex": 1, "cpfem_apply_dirichlet": 1, "cpfem_dot": 1,
                 "cpfem_bc_initial_guess": 1, "cpfem_axpy": 1, "cpfem_spmv": 1, "cpfem_bicgstab": 2,
                 "cpfem_bicgstab_ex": 2, "cpfem_cell_average": 1, "cpfem_segmented_dot": 1,
@@ -776,15 +808,25 @@ class CountingLib:
         self.launches = 0
         self.counting = False
 
+    @staticmethod
+    def _count(name, a, k):
+        if name == "cpfem_bicgstab_ex":
+            o = a[4]._obj
+            return 1 + (1 if o.precond in (1, 2) else 0) + (2 if o.flags & 1 else 0)
+        if name == "cpfem_mg_setup":
+            mg = a[0]._obj
+            return 1 + 4 * (mg.num_levels - 1) + (2 * mg.num_levels if mg.precision == 1 else 0)
+        return k
+
     def __getattr__(self, name):
         f = getattr(self._lib, name)
         k = self.LAUNCHES.get(name)
-        if k is None:
+        if k is None and name != "cpfem_mg_setup":
             return f
 
         def call(*a):
             if self.counting:
-                self.launches += k
+                self.launches += self._count(name, a, k)
             return f(*a)
         return call
 

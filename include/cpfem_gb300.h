@@ -420,7 +420,8 @@ typedef struct {
   const cpfem_mg_t* mg;   /* precond 3: a hierarchy set up for this matrix */
   int32_t grid_blocks;    /* blocks of the persistent launch; 0: one per 256 nodes, at most the
                              co-resident limit (larger requests are clamped to it) */
-  int32_t pad;
+  int32_t flags;          /* bit 0: also form ||b - A x||^2 of the returned x in the same launch
+                             (cpfem_bicgstab_last_stats_ex), for the caller's true-residual check */
 } cpfem_krylov_opts_t;
 int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
                       const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream);
@@ -453,6 +454,10 @@ int cpfem_bicgstab_noalloc(const cpfem_sell_t* sell, const double* values, const
  * a solve the way jax's BiCGSTAB state would be inspected (solver.py:34-40 keeps only x).
  */
 int cpfem_bicgstab_last_stats(double* out);
+/* The same scalars followed by ||b - A x||^2 (-1 unless cpfem_krylov_opts_t.flags bit 0 was
+ * set) and b.b: out[0..n) of those 9 values.  The ||Ax - b|| < 0.1 check of jax_solve
+ * (crystal_plasticity_OR_design/solver.py:43-46) reads them instead of a separate product. */
+int cpfem_bicgstab_last_stats_ex(double* out, int32_t n);
 
 /*
  * Ragged batch of independent systems (block-diagonal A over instances, instance i owning

@@ -147,7 +147,7 @@ class KrylovOpts(ctypes.Structure):
         ("atol", ctypes.c_double),
         ("mg", ctypes.POINTER(MGHierarchy)),
         ("grid_blocks", ctypes.c_int32),
-        ("pad", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
     ]
 
 
@@ -185,6 +185,7 @@ SIGNATURES = {
     "cpfem_bicgstab": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P, _P]),
     "cpfem_bicgstab_noalloc": (ctypes.c_int, [_SP, _P, _P, _P, _I32, _I32, _D, _D, _I32, _P, _P]),
     "cpfem_bicgstab_last_stats": (ctypes.c_int, [_P]),
+    "cpfem_bicgstab_last_stats_ex": (ctypes.c_int, [_P, _I32]),
     "cpfem_mg_slot_table": (ctypes.c_int, [_I32, _P, _P, _P, _P]),
     "cpfem_struct_size": (ctypes.c_size_t, [_I32]),
     "cpfem_mg_setup": (ctypes.c_int, [ctypes.POINTER(MGHierarchy), _P, _P]),

@@ -42,9 +42,14 @@ struct SolveOut {
   double rho, alpha, omega;   // scalars of the last iteration (rho: the one it started with)
   int restarts;
   int pad;
+  double true_rs;             // ||b - A x||^2 at the end (kKrylovTrueResidual), else -1
+  double bb;                  // b.b
 };
 
-static thread_local SolveOut g_last_solve = {0, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 0, 0};
+// cpfem_krylov_opts_t.flags: also form the true residual of the returned x
+constexpr int kKrylovTrueResidual = 1;
+
+static thread_local SolveOut g_last_solve = {0, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 0, 0, -1.0, 0.0};
 
 struct KWork {
   GridSync* sync;
@@ -834,6 +839,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
   }
   ok = grid_reduce<2>(v2, parts(), w.sync, gen, smem, bcast) && ok;
   const double atol2 = fmax(tol * tol * v2[0], atol * atol);
+  if (blockIdx.x == 0 && threadIdx.x == 0) w.out->bb = v2[0];   // b.b, written now: nothing stays live
   const double rs0 = fmax(v2[1], atol2);
   double rs = v2[1], rho_new = v2[1], rho = 1.0, alpha = 1.0, omega = 1.0;
   int k = 0, restarts = 0;
@@ -974,6 +980,7 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.out->true_rs = -1.0;
     w.out->restarts = restarts;
     w.out->k = k;
     w.out->error = ok ? 0 : 1;
@@ -983,6 +990,34 @@ __global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L,
     w.out->alpha = alpha;
     w.out->omega = omega;
   }
+}
+
+// ||b - A x||^2 in block partials (fixed grid, fixed order inside a block).
+template <bool TRANS>
+__global__ void __launch_bounds__(kVecThreads) k_true_residual(const cpfem_sell_t L, const double* __restrict__ vals,
+                                                               const double* __restrict__ b,
+                                                               const double* __restrict__ x, double* partials) {
+  __shared__ double smem[4 * 32];
+  double v[1] = {0.0};
+  for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < L.num_nodes;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    double acc[3];
+    sell_rows<TRANS, false>(L, vals, x, a, acc);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double r = b[3 * a + i] - acc[i];
+      v[0] = fma(r, r, v[0]);
+    }
+  }
+  block_sum<1>(v, smem);
+  if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partials, int n, double* out) {
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < n; i += 32) v[0] += partials[i];
+  warp_sum<1>(v);
+  if (threadIdx.x == 0) *out = v[0];
 }
 
 static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms, size_t dyn_smem = 0) {
@@ -997,7 +1032,8 @@ static int sm_count_and_blocks(const void* fn, int* blocks_per_sm, int* sms, siz
 template <bool TRANS>
 static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double* b, double* x, int precond,
                         double tol, double atol, int32_t maxiter, void* workspace, int32_t* info, cudaStream_t s,
-                        int max_restarts = 0, const cpfem_mg_t* mgp = nullptr, int grid_blocks = 0) {
+                        int max_restarts = 0, const cpfem_mg_t* mgp = nullptr, int grid_blocks = 0,
+                        int flags = 0) {
   KWork w;
   carve(workspace, L.num_nodes, &w);
   CPFEM_CUDA_TRY(cudaMemsetAsync(w.sync, 0, sizeof(GridSync), s));
@@ -1038,6 +1074,14 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
   int mi = maxiter, mr = max_restarts;
   void* args[] = {&Lc, &vals, &bb, &xx, &w, &pc, &tl, &at, &mi, &mr, &mg};
   CPFEM_CUDA_TRY(cudaLaunchCooperativeKernel(kfn, dim3((unsigned)blocks), dim3(kPThreads), args, dyn, s));
+  if (flags & kKrylovTrueResidual) {
+    // ||b - A x||^2 of the returned x: block partials, then one block sums them in order
+    // (deterministic), into the SolveOut read below -- no extra synchronisation
+    k_true_residual<TRANS><<<kVecBlocks, kVecThreads, 0, s>>>(L, vals, b, x, w.partials);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+    k_sum_partials<<<1, 32, 0, s>>>(w.partials, kVecBlocks, &w.out->true_rs);
+    CPFEM_CUDA_TRY(cudaGetLastError());
+  }
   SolveOut out;
   CPFEM_CUDA_TRY(cudaMemcpyAsync(&out, w.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, s));
   CPFEM_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1259,6 +1303,15 @@ int cpfem_bicgstab_last_stats(double* out) {
   return CPFEM_OK;
 }
 
+int cpfem_bicgstab_last_stats_ex(double* out, int32_t n) {
+  CPFEM_REQUIRE(out != nullptr && n >= 0, "bad stats arguments");
+  const double v[9] = {(double)g_last_solve.k, g_last_solve.rs, g_last_solve.atol2, g_last_solve.rho,
+                       g_last_solve.alpha, g_last_solve.omega, (double)g_last_solve.restarts,
+                       g_last_solve.true_rs, g_last_solve.bb};
+  for (int32_t i = 0; i < n && i < 9; ++i) out[i] = v[i];
+  return CPFEM_OK;
+}
+
 int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
                       const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream) {
   CPFEM_REQUIRE(info != nullptr, "info is null");
@@ -1282,9 +1335,9 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
   cudaStream_t s = (cudaStream_t)stream;
   if (opts->transpose)
     return run_bicgstab<true>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                              info, s, opts->max_restarts, opts->mg, opts->grid_blocks);
+                              info, s, opts->max_restarts, opts->mg, opts->grid_blocks, opts->flags);
   return run_bicgstab<false>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                             info, s, opts->max_restarts, opts->mg, opts->grid_blocks);
+                             info, s, opts->max_restarts, opts->mg, opts->grid_blocks, opts->flags);
 }
 
 int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x, int32_t precond,

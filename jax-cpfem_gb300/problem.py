@@ -697,7 +697,9 @@ class CrystalPlasticity:
         self.stats["gp_passes"] += 1
 
     def _check_status(self, status):
-        s = int(status.item())
+        self._check_status_bits(int(status.item()))
+
+    def _check_status_bits(self, s):
         if s & _capi.CPFEM_GP_BOUNDS:
             raise IndexError("an index gathered by a Gauss-point kernel was out of range")
         if s & _capi.CPFEM_GP_NONFINITE:

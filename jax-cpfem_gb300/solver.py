@@ -49,8 +49,9 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
+    # flags 1: the launch also forms ||b - A x|| of its x (read below with the stats)
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
-                            float(tol), float(atol), None, int(grid_blocks), 0)
+                            float(tol), float(atol), None, int(grid_blocks), 1)
     mg_options = dict(mg_options or {})
     if int(precond) == 3:
         if getattr(problem, "mg_fp64_only", False):
@@ -62,7 +63,12 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
         _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
                                           ctypes.byref(opts), _dev_ptr(ws), info.ctypes.data, _stream()))
     k, ok = int(info[0]), bool(info[1])
-    if int(precond) == 3 and opts.mg.contents.precision == 1 and not _fp32_solve_ok(problem, A, b, x, ok, tol, atol):
+    st = np.zeros(9)
+    _capi.check(lib.cpfem_bicgstab_last_stats_ex(st.ctypes.data, 9))
+    rn = math.sqrt(st[7]) if st[7] >= 0.0 else float("nan")
+    problem._true_res = (x, b, rn)   # jax_solve's ||Ax - b|| check reads it
+    if int(precond) == 3 and opts.mg.contents.precision == 1 and \
+            not _fp32_solve_ok(ok, rn, math.sqrt(st[8]), tol, atol):
         # the FP32 V-cycle failed on this system (near-singular: see cpfem_mg_t.precision);
         # solve again with the FP64 V-cycle, and keep FP64 for this problem from now on
         problem.mg_fp64_only = True
@@ -71,16 +77,11 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     return x, k, ok
 
 
-def _fp32_solve_ok(problem, A, b, x, converged, tol, atol):
-    """An FP32-preconditioned solve is kept when it converged and its true residual meets
-    the stop rule (with a factor 10 for the drift of the recursive residual)."""
-    if not converged:
-        return False
-    r = A.matvec(x)
-    r.sub_(b)
-    rn, bn = norm(problem, r), norm(problem, b)
-    problem._true_res = (x, b, rn)   # jax_solve's ||Ax - b|| check reuses it
-    return math.isfinite(rn) and rn <= 10.0 * max(tol * bn, atol)
+def _fp32_solve_ok(converged, rn, bn, tol, atol):
+    """An FP32-preconditioned solve is kept when it converged and its true residual rn =
+    ||b - A x|| (formed by the solve's own launch) meets the stop rule, with a factor 10
+    for the drift of the recursive residual."""
+    return converged and math.isfinite(rn) and rn <= 10.0 * max(tol * bn, atol)
 
 
 def jax_solve(problem, A, b, x0, precond=True, opts=None):
@@ -120,6 +121,35 @@ def linear_solver(problem, A, b, x0, solver_options):
         return torch.as_tensor(x, dtype=torch.float64, device=problem.device).reshape(-1).contiguous()
     raise NotImplementedError("only 'jax_solver' (device BiCGSTAB) and 'custom_solver' run on the GPU; "
                               "UMFPACK/PETSc host solvers are not part of the device path")
+
+
+def _norm_checked(problem, x, status):
+    """||x|| and the status word of the constitutive pass that produced x, read in one
+    device-to-host transfer; raises on a failed local solve as the pass's own check would."""
+    ws = problem._buf("dot_ws", (int(problem.lib.cpfem_dot_workspace_bytes(x.numel())) // 8 + 64,))
+    out = problem._buf("dot_out", (1,))
+    _capi.check(problem.lib.cpfem_dot(x.numel(), _dev_ptr(x), _dev_ptr(x), _dev_ptr(out), _dev_ptr(ws), _stream()))
+    both = torch.stack([out[0], status[0].to(torch.float64)]).cpu()
+    problem._check_status_bits(int(both[1]))
+    return math.sqrt(float(both[0]))
+
+
+def _update_deferred(problem, dofs):
+    """newton_update_helper with the status check left to the next norm (one sync)."""
+    u = dofs.reshape(-1)
+    res, values, status = problem.assemble(u, need_tangent=True)
+    problem.A_values = values
+    res = res.reshape(-1)
+    problem.apply_dirichlet(res, dofs, values)
+    return res, DeviceCSR(problem, values), status
+
+
+def _residual_deferred(problem, dofs):
+    """residual_bc(check=True, keep_trial=True) with the status check left to the norm."""
+    res, _, status = problem.assemble(dofs.reshape(-1), need_tangent=False, keep_trial=True)
+    res = res.reshape(-1)
+    problem.apply_dirichlet(res, dofs, None)
+    return res, status
 
 
 def newton_update_helper(problem, dofs):
@@ -200,8 +230,8 @@ def solver(problem, solver_options=None):
     tol = solver_options.get("tol", 1e-6)
     max_newton = solver_options.get("max_newton", 100)
 
-    res_vec, A = newton_update_helper(problem, dofs)
-    res_val = norm(problem, res_vec)
+    res_vec, A, status = _update_deferred(problem, dofs)
+    res_val = _norm_checked(problem, res_vec, status)
     res_val_initial = res_val
     rel_res_val = res_val / res_val_initial if res_val_initial > 0 else float("nan")
     history = [res_val]
@@ -217,16 +247,16 @@ def solver(problem, solver_options=None):
             # the last iterate needs no tangent: residual (and trial state) only, and the
             # tangent pass after all if the residual is not below the limit yet (its local
             # solves then start at their roots)
-            res_vec = residual_bc(problem, dofs, keep_trial=True)
-            res_val = norm(problem, res_vec)
+            res_vec, status = _residual_deferred(problem, dofs)
+            res_val = _norm_checked(problem, res_vec, status)
             if (res_val / res_val_initial > rel_tol) and (res_val > tol):
                 problem.stats["final_tangent_mispredicted"] = problem.stats.get("final_tangent_mispredicted", 0) + 1
                 res_vec = None
             else:
                 problem.stats["final_tangent_skipped"] = problem.stats.get("final_tangent_skipped", 0) + 1
         if res_vec is None:
-            res_vec, A = newton_update_helper(problem, dofs)
-            res_val = norm(problem, res_vec)
+            res_vec, A, status = _update_deferred(problem, dofs)
+            res_val = _norm_checked(problem, res_vec, status)
         rel_res_val = res_val / res_val_initial
         history.append(res_val)
         it += 1
