@@ -505,7 +505,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
                     help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
-    ap.add_argument("--no-tune", action="store_true", help="skip the linear-solver autotuning before warm-up ends")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the linear-solver autotuning during warm-up and use its stored choice for this "
+                         "workload (workloads.TUNED_MG)")
     ap.add_argument("--mg-precision", default=None, choices=["fp64", "fp32"],
                     help="fix the V-cycle precision (default: the autotuner's choice, FP64 untuned)")
     ap.add_argument("--no-jacobi-leg", action="store_true",
@@ -569,7 +571,12 @@ def main():
         st.options = dict(newton, jax_solver={"precond": precond, "mg_options": mg, "grid_blocks": grid_blocks,
                                               "tol": krylov_tol})
 
-    set_solver(args.precond, mg_options, 0)
+    if args.no_tune and args.precond == 3:
+        mg_options = dict(W.TUNED_MG, refresh=args.mg_refresh, **({"precision": args.mg_precision}
+                                                                  if args.mg_precision else {}))
+        set_solver(args.precond, mg_options, W.TUNED_GRID_BLOCKS)
+    else:
+        set_solver(args.precond, mg_options, 0)
     clk = ClockSampler(local).start()
     time.sleep(1.0)
     # warm-up with the timers on, so every kernel the timed steps use (including torch's

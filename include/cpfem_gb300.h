@@ -389,8 +389,9 @@ typedef struct {
                               and the stop rule is unchanged; only the iterates differ. */
   int32_t local_nodes;     /* levels >= 2 with at most this many nodes run inside one block
                               (0: 256) */
-  float* values32[CPFEM_MG_MAX_LEVELS];       /* precision 1: every level's operator in FP32,
-                                                 level 0 a copy of the system (setup) */
+  float* values32[CPFEM_MG_MAX_LEVELS];       /* precision 1: the operators of levels >= 1 in
+                                                 FP32 (setup); level 0 reads the system's FP64
+                                                 values, rounded in registers (may be NULL) */
   float* minv32[CPFEM_MG_MAX_LEVELS];         /* precision 1: [9*nodes] */
   float* x32[CPFEM_MG_MAX_LEVELS];            /* precision 1: [3*nodes] work vectors */
   float* t32[CPFEM_MG_MAX_LEVELS];

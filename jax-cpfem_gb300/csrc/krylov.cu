@@ -90,16 +90,36 @@ static size_t carve(void* base, int64_t n_nodes, KWork* w) {
 __device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 
+// An operator value in the precision R of the product.  FP64 -> FP32 by integer operations on
+// the two words of the double (exponent re-bias, mantissa truncated to 23 bits, magnitudes
+// below FP32's normal range flushed to zero), so the FP32 V-cycle can read the resident FP64
+// operator without a conversion instruction per value on GB300's narrow FP64 pipe.  The
+// truncation error (< 2^-23 relative) is below what an FP32 preconditioner resolves.
+template <typename R>
+__device__ __forceinline__ R opval(double v);
+template <>
+__device__ __forceinline__ double opval<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float opval<float>(double v) {
+  const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+  const int e = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+  const unsigned bits = (e <= 0) ? (hi & 0x80000000u)
+                                 : ((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+  return __uint_as_float(bits);
+}
+template <typename R>
+__device__ __forceinline__ R opval(float v) { return (R)v; }
+
 // Three rows of node a of A x (or A^T x), in the precision R of the values and x (FP64 for
 // the Krylov iteration, FP32 inside a single-precision V-cycle).  COHERENT selects L2
 // loads for x, needed when x was written by other blocks earlier in the same launch.
-template <bool TRANS, bool COHERENT, typename R>
-__device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const R* __restrict__ vals,
+template <bool TRANS, bool COHERENT, typename R, typename VT = R>
+__device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const VT* __restrict__ vals,
                                           const R* x, int64_t a, R* acc) {
   const int64_t g = a >> 5;
   const int lane = (int)(a & 31);
   const int64_t c0 = L.group_off[g] + lane;
-  const R* v0 = vals + 9 * L.group_off[g] + lane;
+  const VT* v0 = vals + 9 * L.group_off[g] + lane;
   const int w = L.group_width[g];
   // two accumulators per row (even / odd slots): six independent FMA chains keep the FP64
   // pipe fed at one thread per node
@@ -113,17 +133,17 @@ __device__ __forceinline__ void sell_rows(const cpfem_sell_t& L, const R* __rest
       x0 = __ldg(&x[3 * b]); x1 = __ldg(&x[3 * b + 1]); x2 = __ldg(&x[3 * b + 2]);
     }
     if (!TRANS) {
-      const R* vj = v0 + 288 * j;
-      a0 = mad(__ldg(&vj[0]), x0, mad(__ldg(&vj[32]), x1, mad(__ldg(&vj[64]), x2, a0)));
-      a1 = mad(__ldg(&vj[96]), x0, mad(__ldg(&vj[128]), x1, mad(__ldg(&vj[160]), x2, a1)));
-      a2 = mad(__ldg(&vj[192]), x0, mad(__ldg(&vj[224]), x1, mad(__ldg(&vj[256]), x2, a2)));
+      const VT* vj = v0 + 288 * j;
+      a0 = mad(opval<R>(__ldg(&vj[0])), x0, mad(opval<R>(__ldg(&vj[32])), x1, mad(opval<R>(__ldg(&vj[64])), x2, a0)));
+      a1 = mad(opval<R>(__ldg(&vj[96])), x0, mad(opval<R>(__ldg(&vj[128])), x1, mad(opval<R>(__ldg(&vj[160])), x2, a1)));
+      a2 = mad(opval<R>(__ldg(&vj[192])), x0, mad(opval<R>(__ldg(&vj[224])), x1, mad(opval<R>(__ldg(&vj[256])), x2, a2)));
     } else {
       // A^T[3a+i][3b+k] = A[3b+k][3a+i]: node b, slot tpos, row k, column i
       const int64_t tp = __ldg(&L.tpos[c0 + 32 * j]);
-      const R* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
-      a0 = mad(__ldg(&vb[0]), x0, mad(__ldg(&vb[96]), x1, mad(__ldg(&vb[192]), x2, a0)));
-      a1 = mad(__ldg(&vb[32]), x0, mad(__ldg(&vb[128]), x1, mad(__ldg(&vb[224]), x2, a1)));
-      a2 = mad(__ldg(&vb[64]), x0, mad(__ldg(&vb[160]), x1, mad(__ldg(&vb[256]), x2, a2)));
+      const VT* vb = vals + 9 * L.group_off[b >> 5] + (b & 31) + 288 * tp;
+      a0 = mad(opval<R>(__ldg(&vb[0])), x0, mad(opval<R>(__ldg(&vb[96])), x1, mad(opval<R>(__ldg(&vb[192])), x2, a0)));
+      a1 = mad(opval<R>(__ldg(&vb[32])), x0, mad(opval<R>(__ldg(&vb[128])), x1, mad(opval<R>(__ldg(&vb[224])), x2, a1)));
+      a2 = mad(opval<R>(__ldg(&vb[64])), x0, mad(opval<R>(__ldg(&vb[160])), x1, mad(opval<R>(__ldg(&vb[256])), x2, a2)));
     }
   };
   int j = 0;
@@ -295,11 +315,11 @@ __device__ __forceinline__ void mg_apply_minv(const R* __restrict__ minv, int64_
 
 // One damped block-Jacobi sweep at node a of level 0: T = X + omega Minv (B - A X) (A^T
 // when TRANS); B is the Krylov vector being preconditioned (FP64), the rest in precision R.
-template <bool TRANS, typename R>
-__device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const R* V, const R* minv, const double* B,
+template <bool TRANS, typename R, typename VT>
+__device__ __forceinline__ void mg_sweep(const cpfem_sell_t& S, const VT* V, const R* minv, const double* B,
                                          const R* X, R* T, R omega, int64_t a) {
   R acc[3], r[3], z[3];
-  sell_rows<TRANS, true>(S, V, X, a, acc);
+  sell_rows<TRANS, true, R, VT>(S, V, X, a, acc);
 #pragma unroll
   for (int i = 0; i < 3; ++i) r[i] = (R)B[3 * a + i] - acc[i];
   mg_apply_minv<TRANS>(minv, a, r, z);
@@ -736,7 +756,8 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     for (int k = 1; k < nsw; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, V, Mi, in, X, T, om, a);
+        // level 0 reads the system's FP64 values (no FP32 copy next to them in L2)
+        for (int64_t a = t0; a < n; a += stride) mg_sweep<TRANS>(S, vals0, Mi, in, X, T, om, a);
       } else {
         mgq_apply<TRANS, false>(mg, V, Mi, l, X, T, A.b(l), false, tq, sq, q);
       }
@@ -748,7 +769,7 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     if (l == 0) {
       for (int64_t a = t0; a < n; a += stride) {
         R acc[3];
-        sell_rows<TRANS, true>(S, V, X, a, acc);
+        sell_rows<TRANS, true, R, double>(S, vals0, X, a, acc);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
           const R rv = (R)in[3 * a + i] - acc[i];
@@ -782,7 +803,7 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
     for (int k = 0; k < mg.post_sweeps; ++k) {
       ok = grid_barrier(gs, gen) && ok;
       if (l == 0) {
-        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, V, Mi, in, X, T, om, a);
+        for (int64_t a = t0; a < S.num_nodes; a += stride) mg_sweep<TRANS>(S, vals0, Mi, in, X, T, om, a);
       } else {
         mgq_apply<TRANS, false>(mg, V, Mi, l, X, T, A.b(l), false, tq, sq, q);
       }
@@ -1115,7 +1136,8 @@ static int mg_check(const cpfem_mg_t* mg, const cpfem_sell_t* sell) {
     CPFEM_REQUIRE(mg->dims[l][0] >= 1 && mg->dims[l][1] >= 1 && mg->dims[l][2] >= 1 && n == mg->sell[l].num_nodes,
                   "multigrid dims do not match the level's node count");
     CPFEM_REQUIRE(sell_ok(&mg->sell[l]) && mg->minv[l], "multigrid level arrays missing");
-    CPFEM_REQUIRE(single ? (mg->values32[l] && mg->minv32[l] && mg->x32[l] && mg->t32[l]) : (mg->x[l] && mg->t[l]),
+    CPFEM_REQUIRE(single ? ((l == 0 || mg->values32[l]) && mg->minv32[l] && mg->x32[l] && mg->t32[l])
+                         : (mg->x[l] && mg->t[l]),
                   "multigrid work arrays missing");
     CPFEM_REQUIRE(mg->slot[l], "multigrid slot table missing");
     if (l + 1 < L) {
@@ -1274,12 +1296,14 @@ int cpfem_mg_setup(const cpfem_mg_t* mg, const double* values0, void* stream) {
     CPFEM_CUDA_TRY(cudaGetLastError());
   }
   if (mg->precision == 1) {
-    // the FP32 V-cycle's operators: rounded copies of the FP64 ones
+    // the FP32 V-cycle's coarse operators: rounded copies of the FP64 ones (level 0 reads
+    // the system's values directly)
     for (int l = 0; l < mg->num_levels; ++l) {
       const cpfem_sell_t& S = mg->sell[l];
-      k_to_f32<<<1216, 256, 0, s>>>((l == 0) ? values0 : mg->values[l], mg->values32[l], 0,
-                                    S.group_off + S.num_groups);
-      CPFEM_CUDA_TRY(cudaGetLastError());
+      if (l > 0) {
+        k_to_f32<<<1216, 256, 0, s>>>(mg->values[l], mg->values32[l], 0, S.group_off + S.num_groups);
+        CPFEM_CUDA_TRY(cudaGetLastError());
+      }
       const int64_t nm = 9 * (int64_t)S.num_nodes;
       k_to_f32<<<(unsigned)std::min<int64_t>(ceil_div(nm, 256), 1216), 256, 0, s>>>(mg->minv[l], mg->minv32[l], nm,
                                                                                    nullptr);

@@ -382,7 +382,7 @@ class CrystalPlasticity:
         """Select the V-cycle precision; the FP32 arrays are made on first use (they are
         filled by the next ``mg_setup``)."""
         mg.precision = 1 if precision == "fp32" else 0
-        if mg.precision == 0 or mg.values32[0]:
+        if mg.precision == 0 or mg.minv32[0]:
             return
         keep = self._mg_keep
 
@@ -394,7 +394,8 @@ class CrystalPlasticity:
         L = mg.num_levels
         for l, d in enumerate(self.mg_levels):
             n = d[0] * d[1] * d[2]
-            mg.values32[l] = buf(9 * int(self.mg_layouts[l][2][-1]))
+            if l > 0:   # level 0 reads the system's FP64 values
+                mg.values32[l] = buf(9 * int(self.mg_layouts[l][2][-1]))
             mg.minv32[l] = buf(9 * n)
             mg.x32[l], mg.t32[l] = buf(3 * n), buf(3 * n)
             if l + 1 < L:
