@@ -441,8 +441,14 @@ def run_batch_config(args, pkg, torch):
     from importlib import import_module
     batch = import_module("jax-cpfem_gb300.batch")
     inst = batch.sample_instances(args.instances, pkg.material.BENCH_STEEL, seed=SEED)
-    nsteps = args.load_steps or 2
+    nsteps = args.load_steps or 20
     disps = STRAIN_STEP * np.arange(1, nsteps + 1)
+    # both arms run the same per-instance algorithm: Jacobi BiCGSTAB (the ragged solver's),
+    # and the benchmark path's predictor, Krylov tolerance, FP32 tangent and Newton limit
+    fast = args.predictor == "linear"
+    newton = dict(NEWTON) if fast else dict(NEWTON_REF)
+    ktol = args.krylov_tol
+    serial_opts = dict(newton, jax_solver={"tol": ktol})
     # untimed warm-up of every kernel on a tiny batch (module loads, allocator growth)
     w = batch.Batch(batch.sample_instances(2, pkg.material.BENCH_STEEL, seed=SEED + 1, edges=(2,), grains=(2, 2)))
     w.step(STRAIN_STEP, DT)
@@ -451,11 +457,13 @@ def run_batch_config(args, pkg, torch):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b = batch.Batch(inst)
+    b.predictor = args.predictor
+    b.problem.fp32_tangent = bool(args.fp32_tangent)
     torch.cuda.synchronize()
     t_setup_batch = time.perf_counter() - t0
     b.problem.timing = True
     t0 = time.perf_counter()
-    szz = np.stack([b.step(d, DT).cpu().numpy() for d in disps], axis=1)
+    szz = np.stack([b.step(d, DT, ktol=ktol, **newton).cpu().numpy() for d in disps], axis=1)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     regions = b.problem.timer_ms()
@@ -467,10 +475,12 @@ def run_batch_config(args, pkg, torch):
     torch.cuda.empty_cache()
     t0 = time.perf_counter()
     prepared = batch.build_serial(inst)
+    for p_, _ in prepared:
+        p_.fp32_tangent = bool(args.fp32_tangent)
     torch.cuda.synchronize()
     t_setup_serial = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ref = batch.run_serial(inst, disps, DT, prepared=prepared)
+    ref = batch.run_serial(inst, disps, DT, prepared=prepared, solver_options=serial_opts, predictor=args.predictor)
     torch.cuda.synchronize()
     t_serial = time.perf_counter() - t0
     rel = float(np.abs(szz - ref).max() / np.abs(ref).max())
@@ -480,7 +490,10 @@ def run_batch_config(args, pkg, torch):
                       "data": "synthetic",
                       "config": {"workload": f"batch-{len(inst)}-rves-edges8-24", "instances": len(inst),
                                  "gauss_points": gps, "load_steps": nsteps,
-                                 "timed": "load steps only; problem set-up timed separately on both sides"},
+                                 "timed": "load steps only; problem set-up timed separately on both sides",
+                                 "both_arms": {"precond": "jacobi", "krylov_tol": ktol, "predictor": args.predictor,
+                                               "tangent": "fp32" if args.fp32_tangent else "fp64",
+                                               "newton": f"tol {newton['tol']:g} / rel_tol {newton['rel_tol']:g}"}},
                       "batched_s": t_batch, "serial_s": t_serial,
                       "setup_s": {"batched": t_setup_batch, "serial": t_setup_serial},
                       "with_setup_ratio": (t_serial + t_setup_serial) / (t_batch + t_setup_batch),

@@ -107,6 +107,10 @@ class Batch:
                                face_nodes(P, 2, 1.0) + o])
         self.order = np.argsort(-np.diff(self.node_off_np), kind="stable")   # largest first
         self.sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=dev)
+        self.prev = None
+        # the initial guess of each step's Newton solve: the last solution ("previous", the
+        # reference driver's) or 2 u_n - u_(n-1) ("linear", as workloads.LoadStepper)
+        self.predictor = "previous"
         self.params = p.internal_vars
         self.stats = {"newton_iters": [], "krylov_iters": []}
         self.host_s = {}
@@ -159,7 +163,10 @@ class Batch:
         """Batched global Newton for the current BCs, dt and state."""
         p = self.problem
         lib = p.lib
-        dofs = self.sol.clone()
+        if self.predictor == "linear" and self.prev is not None:
+            dofs = 2.0 * self.sol - self.prev
+        else:
+            dofs = self.sol.clone()
         trial = p.new_trial()
         with self._phase("assemble"):
             res, A = self._assemble(dofs, trial)
@@ -207,18 +214,19 @@ class Batch:
         self.stats["newton_iters"].append(newton_count)
         return dofs
 
-    def step(self, disp, dt):
-        """One load step of every instance; returns the per-instance mean cell sigma_zz."""
+    def step(self, disp, dt, **solve_options):
+        """One load step of every instance; returns the per-instance mean cell sigma_zz.
+        ``solve_options`` go to ``solve`` (rel_tol, tol, ktol, ...)."""
         p = self.problem
         p.dt = float(dt)
         with self._phase("bcs"):
             self.set_bcs(disp)
             p.set_params(self.params)
-        sol = self.solve()
+        sol = self.solve(**solve_options)
         with self._phase("post"):
             sig = p.compute_avg_stress(sol.reshape(-1, 3), self.params)
             self.params = p.update_int_vars_gp(sol.reshape(-1, 3), self.params)
-        self.sol = sol
+        self.prev, self.sol = self.sol, sol
         szz = torch.zeros(self.n, dtype=torch.float64, device=p.device)
         szz.index_add_(0, self.inst_of_cell, sig[:, 2, 2])
         return szz / self.cells_per_inst
@@ -235,20 +243,25 @@ def build_serial(instances, device=None):
     return out
 
 
-def run_serial(instances, disps, dt, device=None, prepared=None):
+def run_serial(instances, disps, dt, device=None, prepared=None, solver_options=None, predictor="previous"):
     """The same RVEs one at a time through the plain drop-in path (``prepared`` from
-    ``build_serial`` keeps the problem set-up out of a timed region)."""
+    ``build_serial`` keeps the problem set-up out of a timed region); ``solver_options`` and
+    ``predictor`` as the batch uses them."""
     prepared = prepared if prepared is not None else build_serial(instances, device)
     out = np.zeros((len(prepared), len(disps)))
+    base = dict(solver_options or {"jax_solver": {}})
     for k, (p, nodes) in enumerate(prepared):
         params = p.internal_vars
         sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
+        prev = None
         p.reset_local_start()
         for i, d in enumerate(disps):
             p.dt = float(dt)
             p.fes[0].set_dirichlet_lists(nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, float(d)])
             p.set_params(params)
-            sol = _solver.solver(p, {"jax_solver": {}, "initial_guess": [sol.reshape(-1, 3)]})[0].reshape(-1)
+            guess = 2.0 * sol - prev if (predictor == "linear" and prev is not None) else sol
+            prev = sol
+            sol = _solver.solver(p, dict(base, initial_guess=[guess.reshape(-1, 3)]))[0].reshape(-1)
             sig = p.compute_avg_stress(sol.reshape(-1, 3), params)
             params = p.update_int_vars_gp(sol.reshape(-1, 3), params)
             out[k, i] = float(sig[:, 2, 2].mean())
