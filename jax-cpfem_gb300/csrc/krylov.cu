@@ -378,33 +378,46 @@ __device__ __forceinline__ void sell_rows_quad(const cpfem_sell_t& L, const R* _
 
 constexpr int kMgMaxWidth = 27;                 // neighbour slots of a structured-box node
 
+// Staged (shared-memory) copies of a block-local level are skewed: the four lanes of a
+// node's quad read four consecutive slots, whose sliced-ELL rows (288 values, or 32 index
+// entries) start in the same bank, so every slot row is followed by 8 unused words.  Lanes
+// (node k, slot phase q) of a warp then read bank k + 8q: no bank conflicts.
+constexpr int64_t kStSkew = 8;
+__host__ __device__ constexpr int64_t st_val_index(int64_t i) { return i + kStSkew * (i / 288); }
+__host__ __device__ constexpr int64_t st_idx_index(int64_t i) { return i + kStSkew * (i >> 5); }
+constexpr int64_t kStValRow = 288 + kStSkew, kStIdxRow = 32 + kStSkew;
+
 // sell_rows_quad on a level staged in shared memory: values, x and the index tables
-// (group offsets, widths, columns, transposed slots as int32, mg_stage) all there.
+// (group offsets, widths, columns, transposed slots as int32, mg_stage) all there, the
+// values and the column / transposed-slot tables in the skewed order above (group offsets
+// are multiples of 32 slots, so a group's rows start at a whole skewed row).
 template <bool TRANS, typename R>
 __device__ __forceinline__ void sell_rows_quad_st(const int* ix, int ng, const R* vals, const R* x, int64_t a,
                                                   int q, R* acc) {
   const int* goff = ix;
   const int* gw = ix + ng + 1;
   const int* cols = gw + ng;
-  const int* tpos = cols + 32 * kMgMaxWidth * ng;
+  const int* tpos = cols + kStIdxRow * kMgMaxWidth * ng;
   const int g = (int)(a >> 5);
   const int lane = (int)(a & 31);
-  const int c0 = goff[g] + lane;
-  const R* v0 = vals + 9 * goff[g] + lane;
+  const int gs = goff[g];
+  const int c0 = gs + (int)kStSkew * (gs >> 5) + lane;               // st_idx_index(gs + lane)
+  const R* v0 = vals + 9 * gs + (int)kStSkew * (gs >> 5) + lane;     // st_val_index(9 gs + lane)
   const int w = gw[g];
   R a0 = R(0), a1 = R(0), a2 = R(0);
 #pragma unroll 2
   for (int j = q; j < w; j += 4) {
-    const int b = cols[c0 + 32 * j];
+    const int b = cols[c0 + (int)kStIdxRow * j];
     const R x0 = x[3 * b], x1 = x[3 * b + 1], x2 = x[3 * b + 2];
     if (!TRANS) {
-      const R* vb = v0 + 288 * j;
+      const R* vb = v0 + kStValRow * j;
       a0 = mad(vb[0], x0, mad(vb[32], x1, mad(vb[64], x2, a0)));
       a1 = mad(vb[96], x0, mad(vb[128], x1, mad(vb[160], x2, a1)));
       a2 = mad(vb[192], x0, mad(vb[224], x1, mad(vb[256], x2, a2)));
     } else {
-      const int tp = tpos[c0 + 32 * j];
-      const R* vb = vals + 9 * goff[b >> 5] + (b & 31) + 288 * tp;
+      const int tp = tpos[c0 + (int)kStIdxRow * j];
+      const int gb = goff[b >> 5];
+      const R* vb = vals + 9 * gb + (int)kStSkew * (gb >> 5) + (b & 31) + kStValRow * tp;
       a0 = mad(vb[0], x0, mad(vb[96], x1, mad(vb[192], x2, a0)));
       a1 = mad(vb[32], x0, mad(vb[128], x1, mad(vb[224], x2, a1)));
       a2 = mad(vb[64], x0, mad(vb[160], x1, mad(vb[256], x2, a2)));
@@ -601,8 +614,11 @@ struct MgShared {
 };
 
 // int32 entries of a staged level's layout: ng+1 group offsets, ng widths, and the column
-// and transposed-slot tables of 32 * kMgMaxWidth slots per group
-__host__ __device__ inline size_t mg_idx_words(int32_t ng) { return 2 * (size_t)ng + 1 + 2 * 32 * (size_t)kMgMaxWidth * ng; }
+// and transposed-slot tables of 32 * kMgMaxWidth slots per group (skewed: kStIdxRow words
+// per slot row)
+__host__ __device__ inline size_t mg_idx_words(int32_t ng) {
+  return 2 * (size_t)ng + 1 + 2 * (size_t)kStIdxRow * (size_t)kMgMaxWidth * ng;
+}
 
 __host__ __device__ inline MgShared mg_shared_layout(const cpfem_mg_t& mg, size_t real_bytes) {
   MgShared s{};
@@ -615,7 +631,7 @@ __host__ __device__ inline MgShared mg_shared_layout(const cpfem_mg_t& mg, size_
   size_t off_v = off;
   for (int m = lb; m < mg.num_levels; ++m) {
     s.val[m] = off_v;
-    off_v += 9 * 32 * (size_t)kMgMaxWidth * (size_t)mg.sell[m].num_groups;
+    off_v += (size_t)kStValRow * (size_t)kMgMaxWidth * (size_t)mg.sell[m].num_groups;
     s.minv[m] = off_v;
     off_v += 9 * (size_t)mg.sell[m].num_nodes;
     s.idx[m] = off_v;   // in 4-byte words, which the staged (FP32) layout's elements are
@@ -642,18 +658,18 @@ __device__ bool mg_stage(const cpfem_mg_t& mg, const MgArrays<R>& A, const MgSha
     const int64_t nv = 9 * S.group_off[S.num_groups];
     const R* V = A.values(m);
     const R* Mi = A.minv(m);
-    for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) sh[lay.val[m] + i] = V[i];
+    for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) sh[lay.val[m] + st_val_index(i)] = V[i];
     for (int64_t i = threadIdx.x; i < 9 * (int64_t)S.num_nodes; i += blockDim.x) sh[lay.minv[m] + i] = Mi[i];
     int* ix = reinterpret_cast<int*>(sh + lay.idx[m]);
     const int ng = S.num_groups;
     const int64_t ns = S.group_off[ng];
     int* cols = ix + 2 * ng + 1;
-    int* tpos = cols + 32 * kMgMaxWidth * ng;
+    int* tpos = cols + kStIdxRow * kMgMaxWidth * ng;
     for (int64_t i = threadIdx.x; i <= ng; i += blockDim.x) ix[i] = (int)S.group_off[i];
     for (int64_t i = threadIdx.x; i < ng; i += blockDim.x) ix[ng + 1 + i] = S.group_width[i];
     for (int64_t i = threadIdx.x; i < ns; i += blockDim.x) {
-      cols[i] = S.cols[i];
-      tpos[i] = (S.tpos != nullptr) ? S.tpos[i] : 0;
+      cols[st_idx_index(i)] = S.cols[i];
+      tpos[st_idx_index(i)] = (S.tpos != nullptr) ? S.tpos[i] : 0;
     }
   }
   __syncthreads();

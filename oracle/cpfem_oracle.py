@@ -686,3 +686,187 @@ def history_stress(points, cells, slip_table, C, grain_quat, cell_grain, theta, 
 def complex_step(fn, x, d, h=1e-30):
     """Directional derivative Im(fn(x + i h d)) / h of a real function (no cancellation)."""
     return np.imag(fn(np.asarray(x, dtype=np.complex128) + 1j * h * np.asarray(d))) / h
+
+
+# ----------------------------------------------------------------------------------
+# Arc-length continuation and dynamic relaxation (``crystal_plasticity_OR_design/solver.py:
+# 447-795``).  The reference solves their linear systems with UMFPACK; here scipy's sparse
+# LU stands in for it.  Neither routine updates internal variables: a caller commits the
+# state between steps (``update_int_vars_gp``), as with the Newton solver.
+# ----------------------------------------------------------------------------------
+def _direct(A, b):
+    import scipy.sparse.linalg as spla
+    return spla.spsolve(sp.csc_matrix(A), b)
+
+
+def _bc_vector(problem, n):
+    """``assign_bc(zeros)`` (``solver.py:137-145``): the BC values on their dofs."""
+    dofs, vals = problem.bc_dofs_vals()
+    u = np.zeros(n)
+    u[dofs] = vals
+    return u
+
+
+def _arc_length_lambda(a1, a2, a3, u, lam, prev_u, prev_lam, dub, dut, dir_u, dir_lam, psi2_w):
+    """The constraint's two roots and the one whose direction continues the previous
+    increment (``solver.py:480-508``); returns delta_lambda."""
+    disc = np.sqrt(a2 ** 2 - 4.0 * a1 * a3)
+    l1 = (-a2 + disc) / (2.0 * a1)
+    l2 = (-a2 - disc) / (2.0 * a1)
+    if not (np.isfinite(l1) and np.isfinite(l2)):
+        raise RuntimeError(f"no valid delta lambda: a1 = {a1}, a2 = {a2}, a3 = {a3}")
+
+    def dot(du1, dl1, du2, dl2):
+        return np.sum(du1 * du2) + psi2_w * dl1 * dl2
+    d1 = dot(dir_u, dir_lam, u + dub + l1 * dut - prev_u, lam + l1 - prev_lam)
+    d2 = dot(dir_u, dir_lam, u + dub + l2 * dut - prev_u, lam + l2 - prev_lam)
+    if abs(d1) < 1e-10 and abs(d2) < 1e-10:
+        return max(l1, l2)
+    return l1 if d1 > d2 else l2
+
+
+def arc_length_disp(problem, prev_u, prev_lam, prev_Du, prev_Dlam, Delta_l=0.1, psi=1.0, tol=1e-6,
+                    max_iter=100):
+    """Crisfield's arc length under displacement control (``solver.py:447-517``): the BC
+    values are scaled by lambda, the residual's BC rows are u - lambda * u_b.  Returns
+    (u, lambda, Delta u, Delta lambda) of the step.  ``max_iter`` is a cap the reference
+    does not have."""
+    bc_dofs, bc_vals = problem.bc_dofs_vals()
+    u = np.array(prev_u, dtype=np.float64)
+    lam = float(prev_lam)
+    u_b = _bc_vector(problem, problem.ndof)
+    w = psi ** 2 * np.sum(u_b ** 2)
+    dir_u, dir_lam = np.array(prev_Du, dtype=np.float64), float(prev_Dlam)
+    res_val, it = 1.0, 0
+    while res_val > tol:
+        if it >= max_iter:
+            raise RuntimeError(f"arc-length step did not converge in {max_iter} iterations")
+        res, A = problem.newton_update(u)
+        res = res.copy()
+        res[bc_dofs] = u[bc_dofs]
+        res[bc_dofs] -= bc_vals * lam
+        A = apply_bc_rows(A, bc_dofs)
+        res_val = np.linalg.norm(res)
+        dub = _direct(A, -res)
+        dut = _direct(A, u_b)
+        Du, Dlam = u - prev_u, lam - prev_lam
+        a1 = np.sum(dut ** 2) + w
+        a2 = 2.0 * np.sum((Du + dub) * dut) + 2.0 * w * Dlam
+        a3 = np.sum((Du + dub) ** 2) + w * Dlam ** 2 - Delta_l ** 2
+        dl = _arc_length_lambda(a1, a2, a3, u, lam, prev_u, prev_lam, dub, dut, dir_u, dir_lam, w)
+        lam = lam + dl
+        u = u + dub + dl * dut
+        dir_u, dir_lam = u - prev_u, lam - prev_lam
+        it += 1
+    return u, lam, dir_u, dir_lam
+
+
+def arc_length_force(problem, prev_u, prev_lam, prev_Du, prev_Dlam, q_vec, Delta_l=0.1, psi=1.0, tol=1e-6,
+                     max_iter=100):
+    """Crisfield's arc length under load control (``solver.py:522-590``): equilibrium
+    res(u) + lambda q = 0 with q's BC rows zeroed."""
+    bc_dofs, bc_vals = problem.bc_dofs_vals()
+    u = np.array(prev_u, dtype=np.float64)
+    lam = float(prev_lam)
+    q = np.array(q_vec, dtype=np.float64).copy()
+    q[bc_dofs] = 0.0
+    w = psi ** 2 * np.sum(q ** 2)
+    dir_u, dir_lam = np.array(prev_Du, dtype=np.float64), float(prev_Dlam)
+    res_val, it = 1.0, 0
+    while res_val > tol:
+        if it >= max_iter:
+            raise RuntimeError(f"arc-length step did not converge in {max_iter} iterations")
+        res, A = problem.newton_update(u)
+        res = res.copy()
+        res[bc_dofs] = u[bc_dofs]
+        res[bc_dofs] -= bc_vals
+        A = apply_bc_rows(A, bc_dofs)
+        res_val = np.linalg.norm(res + lam * q)
+        dub = _direct(A, -(res + lam * q))
+        dut = _direct(A, -q)
+        Du, Dlam = u - prev_u, lam - prev_lam
+        a1 = np.sum(dut ** 2) + w
+        a2 = 2.0 * np.sum((Du + dub) * dut) + 2.0 * w * Dlam
+        a3 = np.sum((Du + dub) ** 2) + w * Dlam ** 2 - Delta_l ** 2
+        dl = _arc_length_lambda(a1, a2, a3, u, lam, prev_u, prev_lam, dub, dut, dir_u, dir_lam, w)
+        lam = lam + dl
+        u = u + dub + dl * dut
+        dir_u, dir_lam = u - prev_u, lam - prev_lam
+        it += 1
+    return u, lam, dir_u, dir_lam
+
+
+def get_q_vec(problem):
+    """The residual at u = 0 (``solver.py:593-602``)."""
+    return problem.compute_residual(np.zeros(problem.ndof))
+
+
+def dr_damping(t, cmin, cmax):
+    """``calC`` (``solver.py:626-634``): c = 2 sqrt(t) clipped to [cmin, cmax]."""
+    t = max(t, 0.0)
+    return min(max(2.0 * np.sqrt(t), cmin), cmax)
+
+
+def dynamic_relax(problem, tol=1e-6, nKMat=50, initial_guess=None, max_iter=100000):
+    """Dynamic relaxation (``solver.py:656-795``): one linear step from u = 0, then explicit
+    damped pseudo-dynamics with the lumped mass M = h~^2/4 rowsum|K| until max|R| <= tol.
+    The reference's update sets qdot_old = qdot before qdotdot = qdot - qdot_old, so the
+    pseudo-acceleration is zero and the stiffness is never re-formed after the first; this
+    keeps that order.  ``max_iter`` is a cap the reference does not have.
+    Returns (dofs, iterations)."""
+    bc_dofs, bc_vals = problem.bc_dofs_vals()
+    n = problem.ndof
+    dofs = np.zeros(n)
+    res, A = problem.newton_update(dofs)
+    res = res.copy()
+    res[bc_dofs] = dofs[bc_dofs]
+    res[bc_dofs] -= bc_vals
+    A = apply_bc_rows(A, bc_dofs)
+    x0 = np.zeros(n)
+    x0[bc_dofs] = bc_vals
+    dofs = dofs + _direct(A, -res)
+    if initial_guess is not None:
+        dofs = np.array(initial_guess, dtype=np.float64).reshape(-1).copy()
+        dofs[bc_dofs] = bc_vals
+    cmin, cmax, h_tilde, h = 1e-3, 3.9, 1.1, 1.0
+
+    def vec(d):
+        r = problem.compute_residual(d).copy()
+        r[bc_dofs] = 0.0
+        return r
+
+    def mass(d):
+        _, K = problem.newton_update(d)
+        K = apply_bc_rows(K, bc_dofs)
+        return h_tilde * h_tilde / 4.0 * np.asarray(abs(K).sum(axis=1)).reshape(-1)
+    qdot_old, qdotdot, qdotdot_old = np.zeros(n), np.zeros(n), np.zeros(n)
+    R = vec(dofs)
+    M = mass(dofs)
+    q = dofs.copy()
+    qdot = -h / 2.0 * R / M
+    nIters = iKMat = 0
+    error = np.max(np.abs(R))
+    while error > tol:
+        if nIters >= max_iter:
+            raise RuntimeError(f"dynamic relaxation did not converge in {max_iter} iterations")
+        q_old, R_old = q.copy(), R
+        q = q + h * qdot
+        dofs = q.copy()
+        R = vec(dofs)
+        nIters += 1
+        iKMat += 1
+        error = np.max(np.abs(R))
+        S0 = np.dot((R - R_old) / h, qdot)
+        t = S0 / np.einsum("i,i,i", qdot, M, qdot)
+        c = dr_damping(t, cmin, cmax)
+        dq = q - q_old
+        ratio = np.divide(qdotdot - qdotdot_old, dq, out=np.zeros(n), where=dq != 0)
+        eps = h_tilde * h_tilde / 4.0 * np.abs(ratio)
+        if np.max(eps) > 1 and iKMat > nKMat:
+            iKMat = 0
+            M = mass(dofs)
+        qdot_old, qdotdot_old = qdot.copy(), qdotdot.copy()
+        qdot = (2.0 - c * h) / (2.0 + c * h) * qdot_old - 2.0 * h / (2.0 + c * h) * R / M
+        qdot_old = qdot.copy()
+        qdotdot = qdot - qdot_old
+    return dofs, nIters
