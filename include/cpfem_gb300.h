@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define CPFEM_ABI_VERSION 1
+#define CPFEM_ABI_VERSION 2
 #define CPFEM_MAX_SLIP 24
 
 enum cpfem_status {
@@ -131,6 +131,10 @@ typedef struct {
                                  ds/dF is that of a plastic state near the new one (not, for
                                  instance, right after a state commit, when the relaxed
                                  state's near-elastic ds/dF overshoots the flow stress). */
+  float* tangent32;           /* [81*num_gp] or NULL: with local_flags bit 4 and tangent == NULL,
+                                 dP/dF stored in FP32 (points whose tangent was formed in FP64
+                                 are rounded), for cpfem_elem_assemble_ex with k_precision 2;
+                                 half the tangent's memory and no conversion in the scatter */
 } cpfem_gp_args_t;
 
 /*
@@ -266,14 +270,17 @@ int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* s
  * fixed).  With a list of cells that share no node (one colour of cpfem_color_cells) the
  * listed cells add without atomics; calling the colours in order gives a bitwise
  * reproducible assembly. */
-/* The same with the element stiffness formed in FP32 (k_precision = 1; 0 is FP64) and added
- * to the FP64 values: for a tangent that only serves as the global Newton's Jacobian, so
- * the FP64 residual and its stop rule decide the converged solution.  FP32 applies with a
- * cell list (the coloured scatter); the residual is FP64 either way. */
+/* The same with a choice of precision for the tangent part: k_precision 0, the FP64 tangent
+ * and FP64 element stiffness (cpfem_elem_assemble); 1, the FP64 tangent (const double*)
+ * with the element stiffness formed in FP32; 2, the FP32 tangent of cpfem_gp_args_t's
+ * tangent32 (const float*) with the element stiffness formed in FP32.  The FP32 stiffness
+ * is added to the FP64 values: it is for a tangent that only serves as the global Newton's
+ * Jacobian, so the FP64 residual and its stop rule decide the converged solution.  The
+ * residual is FP64 in every case. */
 int cpfem_elem_assemble_ex(int32_t num_cells, const int32_t* cells, const double* shape_grads,
                            const cpfem_sell_t* sell, const uint8_t* elem_pos,
                            const int32_t* cell_list, int32_t num_listed,
-                           const double* pk1_w, const double* tangent_w,
+                           const double* pk1_w, const void* tangent_w,
                            double* residual, double* values, int32_t k_precision, void* stream);
 
 /* Greedy cell colouring (host): cells of one colour share no node.  color [num_cells]. */

@@ -72,6 +72,7 @@ class GPArgs(ctypes.Structure):
         ("s_warm", ctypes.c_void_p),
         ("s_dsdf", ctypes.c_void_p),
         ("s_f", ctypes.c_void_p),
+        ("tangent32", ctypes.c_void_p),
     ]
 
 
@@ -214,7 +215,7 @@ def load():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.cpfem_abi_version() != 1:
+    if lib.cpfem_abi_version() != 2:
         raise ImportError("libcpfem_gb300.so ABI version mismatch")
     for which, st in enumerate(STRUCTS):
         if lib.cpfem_struct_size(which) != ctypes.sizeof(st):

@@ -57,6 +57,7 @@ int make_matdev(const cpfem_material_t* m, MatDev* o) {
 // Constitutive pass: one thread per Gauss point.
 // ------------------------------------------------------------------------------------
 // TMODE: 0 no tangent, 1 FP64 tangent, 2 FP32 tangent (FP64 where the scale test fails)
+// stored in FP64, 3 the same stored in FP32 (tangent32)
 template <int NS, int TMODE>
 __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_args_t a) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,17 +210,24 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
     for (int c = 0; c < 9; ++c) a.s_out[c * G + gp] = Sg[c];
   }
   if (a.iters != nullptr) a.iters[gp] = st.iters;
-  if (TMODE != 0 && a.tangent != nullptr) {
-    double* tan = a.tangent;
+  if (TMODE != 0 && (a.tangent != nullptr || a.tangent32 != nullptr)) {
     const bool keep_dsdf = predict && st.rn <= m.local_tol;
-    auto store = [&](int kl, const double* col, const double* dsdf) {
+    // columns arrive in the precision they were formed in; FP32 storage (tangent32)
+    // takes an FP32 column as it is
+    auto store = [&](int kl, const auto* col, const auto* dsdf) {
+      if constexpr (TMODE == 3) {
+        const float w32 = f32_of(w);
 #pragma unroll
-      for (int c = 0; c < 9; ++c) tan[(int64_t)(9 * c + kl) * G + gp] = col[c] * w;
+        for (int c = 0; c < 9; ++c) a.tangent32[(int64_t)(9 * c + kl) * G + gp] = to_f32(col[c]) * w32;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) a.tangent[(int64_t)(9 * c + kl) * G + gp] = to_f64(col[c]) * w;
+      }
       if (keep_dsdf)
 #pragma unroll
-        for (int k = 0; k < 6; ++k) a.s_dsdf[(6 * kl + k) * G + gp] = dsdf[k];
+        for (int k = 0; k < 6; ++k) a.s_dsdf[(6 * kl + k) * G + gp] = to_f64(dsdf[k]);
     };
-    if (TMODE == 2 && tangent_f32_ok<NS>(st, cc))
+    if (TMODE >= 2 && tangent_f32_ok<NS>(st, cc))
       cp_tangent_t<NS, float>(m, cc, F, Gm, st, H, W, Y, idet, store);
     else
       cp_tangent<NS>(m, cc, F, Gm, st, H, W, Y, idet, store);
@@ -229,16 +237,24 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
 // ------------------------------------------------------------------------------------
 // Element residual / tangent: one thread per (cell, node a) owns rows (a, 0..2).
 // KT is the precision of the element stiffness arithmetic (FP64, or FP32 for a tangent
-// that only serves as the Newton Jacobian); the residual is always FP64.
+// that only serves as the Newton Jacobian), TT that of the stored tangent (FP32 storage
+// goes with FP32 arithmetic); the residual is always FP64.
 // ------------------------------------------------------------------------------------
-template <bool WITH_K, bool ATOMIC, typename KT = double>
+template <typename KT>
+__device__ __forceinline__ KT as_kt(double v) { return to_prec<KT>(v); }
+template <typename KT>
+__device__ __forceinline__ KT as_kt(float v);
+template <>
+__device__ __forceinline__ float as_kt<float>(float v) { return v; }
+
+template <bool WITH_K, bool ATOMIC, typename KT = double, typename TT = double>
 __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ clist,
                                                        int32_t ncl, const int32_t* __restrict__ cells,
                                                        const double* __restrict__ sg,
                                                        const int64_t* __restrict__ goff,
                                                        const uint8_t* __restrict__ epos,
                                                        const double* __restrict__ Pw,
-                                                       const double* __restrict__ Dw,
+                                                       const TT* __restrict__ Dw,
                                                        double* __restrict__ res,
                                                        double* __restrict__ vals) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -264,18 +280,18 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
     for (int i = 0; i < 3; ++i)
       Rr[i] = fma(Pw[(3 * i) * G + gp], ga0, fma(Pw[(3 * i + 1) * G + gp], ga1, fma(Pw[(3 * i + 2) * G + gp], ga2, Rr[i])));
     if (WITH_K) {
-      const KT a0 = (KT)ga0, a1 = (KT)ga1, a2 = (KT)ga2;
+      const KT a0 = as_kt<KT>(ga0), a1 = as_kt<KT>(ga1), a2 = as_kt<KT>(ga2);
       KT Gm[27];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int kL = 0; kL < 9; ++kL)
-          Gm[9 * i + kL] = cp_fma(a0, (KT)Dw[(int64_t)(9 * (3 * i + 0) + kL) * G + gp],
-                           cp_fma(a1, (KT)Dw[(int64_t)(9 * (3 * i + 1) + kL) * G + gp],
-                                  a2 * (KT)Dw[(int64_t)(9 * (3 * i + 2) + kL) * G + gp]));
+          Gm[9 * i + kL] = cp_fma(a0, as_kt<KT>(Dw[(int64_t)(9 * (3 * i + 0) + kL) * G + gp]),
+                           cp_fma(a1, as_kt<KT>(Dw[(int64_t)(9 * (3 * i + 1) + kL) * G + gp]),
+                                  a2 * as_kt<KT>(Dw[(int64_t)(9 * (3 * i + 2) + kL) * G + gp])));
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
-        const KT gb0 = (KT)sgq[3 * b], gb1 = (KT)sgq[3 * b + 1], gb2 = (KT)sgq[3 * b + 2];
+        const KT gb0 = as_kt<KT>(sgq[3 * b]), gb1 = as_kt<KT>(sgq[3 * b + 1]), gb2 = as_kt<KT>(sgq[3 * b + 2]);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -304,8 +320,8 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           double* v = &vals[base + 32 * (9 * pos + 3 * i + k)];
-          if (ATOMIC) atomicAdd(v, (double)K[i][3 * b + k]);
-          else *v += (double)K[i][3 * b + k];
+          if (ATOMIC) atomicAdd(v, to_f64(K[i][3 * b + k]));
+          else *v += to_f64(K[i][3 * b + k]);
         }
     }
   }
@@ -395,7 +411,9 @@ static int launch_gp(const MatDev& md, const cpfem_gp_args_t& a, cudaStream_t s)
   const int64_t work = a.cell_list != nullptr ? 8 * (int64_t)a.num_listed : a.num_gp;
   if (work == 0) return CPFEM_OK;
   const unsigned blocks = (unsigned)ceil_div(work, threads);
-  if (a.tangent != nullptr && (a.local_flags & 4))
+  if (a.tangent32 != nullptr)
+    k_gp_eval<NS, 3><<<blocks, threads, 0, s>>>(md, a);
+  else if (a.tangent != nullptr && (a.local_flags & 4))
     k_gp_eval<NS, 2><<<blocks, threads, 0, s>>>(md, a);
   else if (a.tangent != nullptr)
     k_gp_eval<NS, 1><<<blocks, threads, 0, s>>>(md, a);
@@ -436,6 +454,8 @@ int cpfem_gp_eval(const cpfem_material_t* mat, const cpfem_gp_args_t* args, void
   CPFEM_REQUIRE(a.order == nullptr || (a.cell_list == nullptr && a.status != nullptr),
                 "an evaluation order excludes a cell list and needs a status word");
   CPFEM_REQUIRE(a.slip_new == nullptr || a.slip != nullptr, "slip_new needs slip");
+  CPFEM_REQUIRE(a.tangent32 == nullptr || (a.tangent == nullptr && (a.local_flags & 4)),
+                "tangent32 needs local_flags bit 4 and excludes tangent");
   CPFEM_REQUIRE(md.qmode == 0 || md.num_slip % 3 == 0, "qmode 1 needs num_slip % 3 == 0");
   cudaStream_t s = (cudaStream_t)stream;
   if (md.num_slip == 12) return launch_gp<12>(md, a, s);
@@ -452,38 +472,41 @@ int cpfem_elem_assemble(int32_t num_cells, const int32_t* cells, const double* s
 
 int cpfem_elem_assemble_ex(int32_t num_cells, const int32_t* cells, const double* shape_grads,
                            const cpfem_sell_t* sell, const uint8_t* elem_pos, const int32_t* cell_list,
-                           int32_t num_listed, const double* pk1_w, const double* tangent_w, double* residual,
+                           int32_t num_listed, const double* pk1_w, const void* tangent_w, double* residual,
                            double* values, int32_t k_precision, void* stream) {
   if (num_cells == 0) return CPFEM_OK;
   CPFEM_REQUIRE(num_cells > 0 && cells && shape_grads && pk1_w, "bad element arguments");
   CPFEM_REQUIRE((values == nullptr) == (tangent_w == nullptr), "values and tangent_w go together");
   CPFEM_REQUIRE(values == nullptr || (sell && sell->group_off && elem_pos), "values need the layout");
   CPFEM_REQUIRE(cell_list == nullptr || (num_listed >= 0 && num_listed <= num_cells), "bad cell list");
+  CPFEM_REQUIRE(k_precision >= 0 && k_precision <= 2,
+                "k_precision must be 0 (FP64), 1 (FP32 stiffness) or 2 (FP32 tangent and stiffness)");
   const int32_t ncl = (cell_list != nullptr) ? num_listed : num_cells;
   if (ncl == 0) return CPFEM_OK;
   const int threads = 128;
   const unsigned blocks = (unsigned)ceil_div((int64_t)ncl * 8, threads);
   cudaStream_t s = (cudaStream_t)stream;
   const int64_t* goff = (values != nullptr) ? sell->group_off : nullptr;
-  CPFEM_REQUIRE(k_precision == 0 || k_precision == 1, "k_precision must be 0 (FP64) or 1 (FP32)");
-  if (cell_list != nullptr) {
-    if (values != nullptr && k_precision == 1)
-      k_elem_assemble<true, false, float><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads,
-                                                                    goff, elem_pos, pk1_w, tangent_w, residual,
-                                                                    values);
-    else if (values != nullptr)
-      k_elem_assemble<true, false><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads, goff,
-                                                             elem_pos, pk1_w, tangent_w, residual, values);
-    else
-      k_elem_assemble<false, false><<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads,
-                                                              nullptr, elem_pos, pk1_w, nullptr, residual, nullptr);
+  const double* t64 = static_cast<const double*>(tangent_w);
+  const float* t32 = static_cast<const float*>(tangent_w);
+  // a colour's cell list adds without atomics (bitwise reproducible); no list: atomics
+  auto run = [&](auto kernel, auto tangent) {
+    kernel<<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads, goff, elem_pos, pk1_w,
+                                      tangent, residual, values);
+  };
+  const bool listed = cell_list != nullptr;
+  if (values == nullptr) {
+    if (listed) run(k_elem_assemble<false, false>, (const double*)nullptr);
+    else run(k_elem_assemble<false, true>, (const double*)nullptr);
+  } else if (k_precision == 0) {
+    if (listed) run(k_elem_assemble<true, false>, t64);
+    else run(k_elem_assemble<true, true>, t64);
+  } else if (k_precision == 1) {
+    if (listed) run(k_elem_assemble<true, false, float>, t64);
+    else run(k_elem_assemble<true, true, float>, t64);
   } else {
-    if (values != nullptr)
-      k_elem_assemble<true, true><<<blocks, threads, 0, s>>>(num_cells, nullptr, ncl, cells, shape_grads, goff,
-                                                            elem_pos, pk1_w, tangent_w, residual, values);
-    else
-      k_elem_assemble<false, true><<<blocks, threads, 0, s>>>(num_cells, nullptr, ncl, cells, shape_grads, nullptr,
-                                                             elem_pos, pk1_w, nullptr, residual, nullptr);
+    if (listed) run(k_elem_assemble<true, false, float, float>, t32);
+    else run(k_elem_assemble<true, true, float, float>, t32);
   }
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;

@@ -144,7 +144,7 @@ template <int NS>
 CPFEM_HD void cp_jacobian_f32(const MatDev& m, const Cub& cc, const double* kk, const double* M, float* J) {
   float Mf[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Mf[k] = (float)M[k];
+  for (int k = 0; k < 9; ++k) Mf[k] = f32_of(M[k]);
   float* Q = J;
 #pragma unroll
   for (int i = 0; i < 36; ++i) Q[i] = 0.0f;
@@ -162,7 +162,7 @@ CPFEM_HD void cp_jacobian_f32(const MatDev& m, const Cub& cc, const double* kk, 
     q[3] = 0.5f * fmaf(w[1], n[2], w[2] * n[1]);
     q[4] = 0.5f * fmaf(w[0], n[2], w[2] * n[0]);
     q[5] = 0.5f * fmaf(w[0], n[1], w[1] * n[0]);
-    const float ka = (float)kk[a];
+    const float ka = f32_of(kk[a]);
     float c[6];
 #pragma unroll
     for (int j = 0; j < 6; ++j) c[j] = ka * m.pv32[a][j];
@@ -171,7 +171,7 @@ CPFEM_HD void cp_jacobian_f32(const MatDev& m, const Cub& cc, const double* kk, 
 #pragma unroll
       for (int j = 0; j < 6; ++j) Q[6 * i + j] = fmaf(q[i], c[j], Q[6 * i + j]);
   }
-  const float c11 = (float)cc.C11, c12 = (float)cc.C12, c44x2 = (float)(2.0 * cc.C44);
+  const float c11 = f32_of(cc.C11), c12 = f32_of(cc.C12), c44x2 = f32_of(2.0 * cc.C44);
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
     const float e0 = Q[j], e1 = Q[6 + j], e2 = Q[12 + j];
@@ -231,12 +231,12 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, 
           cp_jacobian_f32<NS>(m, cc, st.kk, st.M, J);
           lu_factor<6>(J, perm, dinv);
 #pragma unroll
-          for (int k = 0; k < 6; ++k) d32[k] = (float)(-r[k]);
+          for (int k = 0; k < 6; ++k) d32[k] = -f32_of(r[k]);
           lu_solve<6>(J, perm, dinv, d32);
           done = true;
 #pragma unroll
           for (int k = 0; k < 6; ++k) {
-            ds[k] = (double)d32[k];
+            ds[k] = f64_of(d32[k]);
             done = done && isfinite(ds[k]);
           }
         }
@@ -310,8 +310,8 @@ CPFEM_HD void tan_jacobian(const MatDev& m, const Cub& cc, const double* kk, con
 // Consistent tangent at the converged state:
 // dP/dF = d_ik Y_lJ + (dP/ds)(ds/dF) with ds/dF = J^-1 C : sym(Fe_l[k,:] (x) H[l,:]),
 // the implicit-function tangent of f_jvp (models_copper.py:251-259).
-// The tangent column for F_kl is handed to store_col(kl, col[9], ds/dF_kl[6]) as soon as
-// it is known, so the 81 entries never need to be live at once.  Called after every other
+// The tangent column for F_kl is handed to store_col(kl, col[9], ds/dF_kl[6]), both in
+// the precision T, as soon as it is known, so the 81 entries never need to be live at once.  Called after every other
 // output of the Gauss point is written, so only what it needs is live.
 // T is the precision of the computation: FP64, or FP32 for a tangent that only serves as
 // the global Newton's Jacobian and the local solve's start prediction (the converged
@@ -323,10 +323,13 @@ CPFEM_HD void cp_tangent_t(const MatDev& m, const Cub& cc, const double* F64, co
   T F[9], G[9], H[9], W[9], Y[9], B[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
-    F[k] = (T)F64[k]; G[k] = (T)G64[k]; H[k] = (T)H64[k]; W[k] = (T)W64[k]; Y[k] = (T)Y64[k];
-    B[k] = (T)st.B[k];
+    F[k] = to_prec<T>(F64[k]); G[k] = to_prec<T>(G64[k]); H[k] = to_prec<T>(H64[k]);
+    W[k] = to_prec<T>(W64[k]); Y[k] = to_prec<T>(Y64[k]); B[k] = to_prec<T>(st.B[k]);
   }
-  const T idet = (T)idet64;
+  const T idet = to_prec<T>(idet64);
+  T kkT[NS];
+#pragma unroll
+  for (int a = 0; a < NS; ++a) kkT[a] = to_prec<T>(st.kk[a]);
   // dP/ds for the 6 symmetric basis directions
   T Bi[9];
   inv3(B, Bi);
@@ -338,7 +341,7 @@ CPFEM_HD void cp_tangent_t(const MatDev& m, const Cub& cc, const double* F64, co
     for (int k = 0; k < 9; ++k) dL[k] = T(0);
 #pragma unroll
     for (int a = 0; a < NS; ++a) {
-      const T c = (T)st.kk[a] * tan_pv(m, T(0), a, mm);
+      const T c = kkT[a] * tan_pv(m, T(0), a, mm);
 #pragma unroll
       for (int k = 0; k < 9; ++k) dL[k] = cp_fma(c, tan_p9(m, T(0), a, k), dL[k]);
     }
@@ -389,7 +392,7 @@ CPFEM_HD void cp_tangent_t(const MatDev& m, const Cub& cc, const double* F64, co
     q[5] = T(0.5) * cp_fma(a[0], b[1], a[1] * b[0]);
     cubic_apply(cc, q, x);
     lu_solve<6>(J, perm, dinv, x);
-    double col[9], xd[6];
+    T col[9];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -397,11 +400,9 @@ CPFEM_HD void cp_tangent_t(const MatDev& m, const Cub& cc, const double* F64, co
         T v = (i == k) ? Y[3 * l + j] : T(0);
 #pragma unroll
         for (int mm = 0; mm < 6; ++mm) v = cp_fma(dPds[mm][3 * i + j], x[mm], v);
-        col[3 * i + j] = (double)v;
+        col[3 * i + j] = v;
       }
-#pragma unroll
-    for (int mm = 0; mm < 6; ++mm) xd[mm] = (double)x[mm];
-    store_col(kl, col, xd);
+    store_col(kl, col, x);
   }
 }
 

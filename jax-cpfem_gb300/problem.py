@@ -723,10 +723,16 @@ class CrystalPlasticity:
         status = self._buf("status", (1,), torch.int32)
         status.zero_()
         values = dw = None
+        tangent_key = "tangent"
         if need_tangent:
             values = self._buf("values", (self.num_values,))
             values.zero_()
-            dw = self._buf("tangent_w", (81, G))
+            if self.fp32_tangent:
+                # the FP32 tangent is stored in FP32 and scattered without conversion
+                dw = self._buf("tangent_w32", (81, G), torch.float32)
+                tangent_key = "tangent32"
+            else:
+                dw = self._buf("tangent_w", (81, G))
         with_trial = need_tangent or keep_trial
         ordered = self.sort_gps and with_trial and cell_list is None
         its = self._buf("iters", (G,), torch.int32) if (self.timing or ordered) else None
@@ -734,8 +740,8 @@ class CrystalPlasticity:
         if with_trial and trial is None:
             trial = self.new_trial()
         trial = trial if with_trial else {}
-        args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, tangent=dw, status=status, weight_jxw=True,
-                             iters=its, cell_list=cell_list, order=order, fast_local=True,
+        args = self._gp_args(self._state(), self.dt, u=u, pk1=pw, **{tangent_key: dw}, status=status,
+                             weight_jxw=True, iters=its, cell_list=cell_list, order=order, fast_local=True,
                              **self._warm_args(need_tangent), **trial)
         self._run_gp(args, "gp_eval_tangent" if need_tangent else "gp_eval_residual")
         if ordered:
@@ -765,7 +771,7 @@ class CrystalPlasticity:
         the element stiffness in FP32 when the problem forms its tangent in FP32."""
         fe = self.fes[0]
         base = self.color_cells.data_ptr()
-        kp = 1 if (values is not None and self.fp32_tangent) else 0
+        kp = 0 if values is None else (2 if dw.dtype == torch.float32 else (1 if self.fp32_tangent else 0))
         with self.region("elem_assemble"):
             for c in range(len(self.color_ptr) - 1):
                 c0, c1 = int(self.color_ptr[c]), int(self.color_ptr[c + 1])

@@ -266,3 +266,265 @@ def solver(problem, solver_options=None):
     problem.stats["res_history"] = history
     problem.stats["solve_time"] = time.time() - start
     return problem.unflatten_fn_sol_list(dofs)
+
+
+# ---------------------------------------------------------------------------------------
+# BC helpers on device vectors (``solver.py:119-192``).  The Dirichlet dofs of a problem are
+# unique (a dof named twice keeps its last value, as the reference's sequential .at[].set).
+# ---------------------------------------------------------------------------------------
+def _bc_index(problem):
+    fe = problem.fes[0]
+    return fe.bc_dofs.long(), fe.bc_vals
+
+
+def assign_bc(dofs, problem):
+    """``assign_bc``: a copy of dofs with the BC values on their dofs."""
+    idx, vals = _bc_index(problem)
+    out = _flat(dofs, problem.device).clone()
+    out[idx] = vals
+    return out
+
+
+def assign_zeros_bc(dofs, problem):
+    """``assign_zeros_bc``: a copy of dofs with zeros on the BC dofs."""
+    idx, _ = _bc_index(problem)
+    out = _flat(dofs, problem.device).clone()
+    out[idx] = 0.0
+    return out
+
+
+def assign_ones_bc(dofs, problem):
+    """``assign_ones_bc``: a copy of dofs with ones on the BC dofs."""
+    idx, _ = _bc_index(problem)
+    out = _flat(dofs, problem.device).clone()
+    out[idx] = 1.0
+    return out
+
+
+def copy_bc(dofs, problem):
+    """``copy_bc``: zeros except dofs' own values on the BC dofs."""
+    idx, _ = _bc_index(problem)
+    d = _flat(dofs, problem.device)
+    out = torch.zeros_like(d)
+    out[idx] = d[idx]
+    return out
+
+
+def apply_bc_vec(res_vec, dofs, problem, scale=1.0):
+    """``apply_bc_vec``: BC rows of the residual become dofs - scale * value."""
+    idx, vals = _bc_index(problem)
+    out = _flat(res_vec, problem.device).clone()
+    out[idx] = _flat(dofs, problem.device)[idx] - scale * vals
+    return out
+
+
+# ---------------------------------------------------------------------------------------
+# Arc-length continuation (Crisfield's form) and dynamic relaxation (``solver.py:447-795``).
+# The reference solves their linear systems with UMFPACK; here the device BiCGSTAB solves
+# them to ``DIRECT_SOLVE`` (relative 1e-12) unless ``solver_options`` name another solver
+# (``jax_solver`` options, or a ``custom_solver`` such as a host direct solver).  Neither
+# routine commits internal variables: the caller does, between steps, as with ``solver``.
+# ---------------------------------------------------------------------------------------
+DIRECT_SOLVE = {"jax_solver": {"tol": 1e-12, "atol": 1e-30, "maxiter": 100000}}
+
+
+def _solve_to(problem, A, b, solver_options):
+    opts = {k: (dict(v) if isinstance(v, dict) else v) for k, v in (solver_options or DIRECT_SOLVE).items()}
+    return linear_solver(problem, A, b.contiguous(), torch.zeros_like(b), opts)
+
+
+def _tangent_bc(problem, dofs, scale=1.0):
+    """Residual with BC rows dofs - scale * values and the row-eliminated tangent at dofs
+    (``newton_update_helper`` of the arc-length solvers, ``solver.py:452-459``)."""
+    res, values, status = problem.assemble(dofs, need_tangent=True)
+    problem._check_status(status)
+    problem.A_values = values
+    res = res.reshape(-1)
+    problem.apply_dirichlet(res, dofs, values)
+    if scale != 1.0:
+        idx, vals = _bc_index(problem)
+        res.index_add_(0, idx, (1.0 - scale) * vals)
+    return res.clone(), DeviceCSR(problem, values)
+
+
+def _pick_lambda(a1, a2, a3, u, lam, prev_u, prev_lam, dub, dut, dir_u, dir_lam, w):
+    """The two roots of the arc-length constraint and the one whose direction continues the
+    previous increment (``solver.py:480-508``)."""
+    disc = math.sqrt(a2 * a2 - 4.0 * a1 * a3) if a2 * a2 - 4.0 * a1 * a3 >= 0.0 else float("nan")
+    l1 = (-a2 + disc) / (2.0 * a1)
+    l2 = (-a2 - disc) / (2.0 * a1)
+    if not (math.isfinite(l1) and math.isfinite(l2)):
+        raise RuntimeError(f"no valid solutions for delta lambda, a1 = {a1}, a2 = {a2}, a3 = {a3}")
+    base = u - prev_u
+    dd = float(torch.dot(dir_u, base + dub))
+    dt = float(torch.dot(dir_u, dut))
+    d1 = dd + l1 * dt + w * dir_lam * (lam + l1 - prev_lam)
+    d2 = dd + l2 * dt + w * dir_lam * (lam + l2 - prev_lam)
+    if abs(d1) < 1e-10 and abs(d2) < 1e-10:
+        return max(l1, l2)
+    return l1 if d1 > d2 else l2
+
+
+def _arc_length(problem, prev_u_vec, prev_lamda, prev_Delta_u_vec, prev_Delta_lamda, Delta_l, psi, tol,
+                max_iter, solver_options, q_vec):
+    dev = problem.device
+    prev_u = _flat(prev_u_vec, dev).clone()
+    u = prev_u.clone()
+    lam = prev_lam = float(prev_lamda)
+    dir_u = _flat(prev_Delta_u_vec, dev).clone()
+    dir_lam = float(prev_Delta_lamda)
+    if q_vec is None:
+        drive = assign_bc(torch.zeros_like(u), problem)          # u_b
+    else:
+        drive = assign_zeros_bc(_flat(q_vec, dev), problem)      # q mapped
+    w = psi ** 2 * float(torch.dot(drive, drive))
+    res_val, it = 1.0, 0
+    while res_val > tol:
+        if it >= max_iter:
+            raise RuntimeError(f"arc-length step did not converge in {max_iter} iterations (res = {res_val})")
+        if q_vec is None:
+            res, A = _tangent_bc(problem, u, lam)
+            res_val = float(torch.linalg.vector_norm(res))
+            dub = _solve_to(problem, A, torch.neg(res), solver_options)
+            dut = _solve_to(problem, A, drive, solver_options)
+        else:
+            res, A = _tangent_bc(problem, u)
+            rq = res + lam * drive
+            res_val = float(torch.linalg.vector_norm(rq))
+            dub = _solve_to(problem, A, torch.neg(rq), solver_options)
+            dut = _solve_to(problem, A, torch.neg(drive), solver_options)
+        Du, Dlam = u - prev_u, lam - prev_lam
+        s = Du + dub
+        a1 = float(torch.dot(dut, dut)) + w
+        a2 = 2.0 * float(torch.dot(s, dut)) + 2.0 * w * Dlam
+        a3 = float(torch.dot(s, s)) + w * Dlam ** 2 - Delta_l ** 2
+        dl = _pick_lambda(a1, a2, a3, u, lam, prev_u, prev_lam, dub, dut, dir_u, dir_lam, w)
+        lam = lam + dl
+        u = u + dub + dl * dut
+        dir_u, dir_lam = u - prev_u, lam - prev_lam
+        it += 1
+    problem.stats["arc_length_iters"] = it
+    return u, lam, dir_u, dir_lam
+
+
+def arc_length_solver_disp_driven(problem, prev_u_vec, prev_lamda, prev_Delta_u_vec, prev_Delta_lamda,
+                                  Delta_l=0.1, psi=1.0, tol=1e-6, max_iter=100, solver_options=None):
+    """``solver.py:447-517``: one arc-length step under displacement control -- the BC
+    values scaled by lambda, constraint |Du|^2 + psi^2 Dlambda^2 |u_b|^2 = Delta_l^2.
+    Returns (u_vec, lamda, Delta_u_vec, Delta_lamda), u_vec flat on the device.
+    ``max_iter`` is a cap the reference does not have."""
+    return _arc_length(problem, prev_u_vec, prev_lamda, prev_Delta_u_vec, prev_Delta_lamda, Delta_l, psi, tol,
+                       max_iter, solver_options, None)
+
+
+def arc_length_solver_force_driven(problem, prev_u_vec, prev_lamda, prev_Delta_u_vec, prev_Delta_lamda, q_vec,
+                                   Delta_l=0.1, psi=1.0, tol=1e-6, max_iter=100, solver_options=None):
+    """``solver.py:522-590``: one arc-length step under load control, equilibrium
+    res(u) + lambda q = 0 with q's BC rows zeroed."""
+    return _arc_length(problem, prev_u_vec, prev_lamda, prev_Delta_u_vec, prev_Delta_lamda, Delta_l, psi, tol,
+                       max_iter, solver_options, q_vec)
+
+
+def get_q_vec(problem):
+    """``solver.py:593-602``: the residual at u = 0."""
+    u = torch.zeros(problem.num_total_dofs_all_vars, dtype=torch.float64, device=problem.device)
+    return problem.newton_update(problem.unflatten_fn_sol_list(u))[0].reshape(-1).clone()
+
+
+def _row_abs_sum(problem, values):
+    """sum_j |A_ij| of the device matrix (``np.absolute(KCSR).sum(axis=1)``)."""
+    rows = problem._bufs.get("csr_rows")
+    if rows is None:
+        indptr, _ = problem.csr_arrays()
+        rows = torch.from_numpy(np.repeat(np.arange(len(indptr) - 1), np.diff(indptr))).to(problem.device)
+        problem._bufs["csr_rows"] = rows
+    out = torch.zeros(problem.num_total_dofs_all_vars, dtype=torch.float64, device=problem.device)
+    out.index_add_(0, rows, values[problem.csr_map()].abs())
+    return out
+
+
+def assembleCSR(problem, dofs):
+    """``solver.py:607-623``: the tangent at dofs with unit BC rows (here on the device)."""
+    _, A = _tangent_bc(problem, _flat(dofs, problem.device))
+    return A
+
+
+def calC(t, cmin, cmax):
+    """``solver.py:626-634``: damping c = 2 sqrt(t) clipped to [cmin, cmax]."""
+    t = max(t, 0.0)
+    return min(max(2.0 * math.sqrt(t), cmin), cmax)
+
+
+def dynamic_relax_solve(problem, tol=1e-6, nKMat=50, nPrint=500, info=True, info_force=True, initial_guess=None,
+                        max_iter=1000000, solver_options=None):
+    """``solver.py:656-795``: one linear step from u = 0, then damped explicit
+    pseudo-dynamics with the lumped mass M = h~^2/4 sum_j |K_ij| until max|R| <= tol.  The
+    reference's update sets qdot_old = qdot before qdotdot = qdot - qdot_old, so its
+    pseudo-acceleration is zero and the mass is never re-formed; this keeps that order.
+    Returns the (num_nodes, 3) solution; ``max_iter`` is a cap the reference does not have.
+    Progress goes to the module logger every ``nPrint`` iterations."""
+    import logging
+    log = logging.getLogger(__name__)
+    dev = problem.device
+    n = problem.num_total_dofs_all_vars
+    dofs = torch.zeros(n, dtype=torch.float64, device=dev)
+    res, A = _tangent_bc(problem, dofs)
+    x0 = initial_increment(problem, dofs).clone()
+    opts = {k: (dict(v) if isinstance(v, dict) else v) for k, v in (solver_options or DIRECT_SOLVE).items()}
+    dofs = dofs + linear_solver(problem, A, torch.neg(res), x0, opts)
+    if initial_guess is not None:
+        dofs = assign_bc(initial_guess, problem)
+    cmin, cmax, h_tilde, h = 1e-3, 3.9, 1.1, 1.0
+    idx, _ = _bc_index(problem)
+
+    def vec(d):
+        r, _, status = problem.assemble(d, need_tangent=False)
+        problem._check_status(status)
+        r = r.reshape(-1).clone()
+        r[idx] = 0.0
+        return r
+
+    def mass(d):
+        _, K = _tangent_bc(problem, d)
+        return h_tilde * h_tilde / 4.0 * _row_abs_sum(problem, K.values)
+    R = vec(dofs)
+    M = mass(dofs)
+    q = dofs.clone()
+    qdot = -h / 2.0 * R / M
+    qdot_old = torch.zeros_like(q)
+    qdotdot = torch.zeros_like(q)
+    qdotdot_old = torch.zeros_like(q)
+    nIters = iKMat = 0
+    error = float(R.abs().max())
+    while error > tol:
+        if nIters >= max_iter:
+            raise RuntimeError(f"dynamic relaxation did not converge in {max_iter} iterations (max|R| = {error})")
+        q_old, R_old = q.clone(), R
+        q = q + h * qdot
+        dofs = q.clone()
+        R = vec(dofs)
+        nIters += 1
+        iKMat += 1
+        S0 = torch.dot((R - R_old) / h, qdot)
+        den = torch.dot(qdot * M, qdot)
+        dq = q - q_old
+        ratio = torch.where(dq != 0, (qdotdot - qdotdot_old) / torch.where(dq != 0, dq, torch.ones_like(dq)),
+                            torch.zeros_like(dq))
+        stats = torch.stack([R.abs().max(), S0, den, ratio.abs().max()]).cpu().numpy()
+        error = float(stats[0])
+        t = float(stats[1] / stats[2])
+        c = calC(t, cmin, cmax)
+        if h_tilde * h_tilde / 4.0 * float(stats[3]) > 1 and iKMat > nKMat:
+            iKMat = 0
+            M = mass(dofs)
+        qdot_old = qdot.clone()
+        qdotdot_old = qdotdot.clone()
+        qdot = (2.0 - c * h) / (2.0 + c * h) * qdot_old - 2.0 * h / (2.0 + c * h) * R / M
+        qdot_old = qdot.clone()
+        qdotdot = qdot - qdot_old
+        if (info or info_force) and nIters % nPrint == 1:
+            log.info("DR iteration %d: max force (residual) %g (tol %g), damping t %g, c %g", nIters, error, tol, t, c)
+    if not math.isfinite(error):
+        raise FloatingPointError("dynamic relaxation produced a non-finite residual")
+    problem.stats["dr_iters"] = nIters
+    return problem.unflatten_fn_sol_list(dofs)[0]

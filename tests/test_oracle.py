@@ -247,3 +247,52 @@ def test_complex_step_history_derivative_matches_central_differences():
     cs = O.complex_step(lambda eu: f(theta, eu), euler, d)
     fd = (f(theta, euler + 1e-4 * d) - f(theta, euler - 1e-4 * d)) / 2e-4
     assert np.abs(cs - fd).max() < 1e-5 * np.abs(cs).max(), (cs, fd)
+
+
+def _continuation_case(disp=2e-3):
+    pts, cells = O.box_mesh(2, 2, 2)
+    q = np.array([[0.9, 0.1, -0.3, 0.2]])
+    q /= np.linalg.norm(q)
+    prob = O.OracleProblem(pts, cells, O.FCC12, 204.6e3, 137.7e3, 126.2e3, q, np.zeros(8, int), gss_initial=90.0,
+                           h=500.0, t_sat=250.0, gss_a=2.25, xm=0.05, r=1.4, coplanar=True)
+    prob.dt = 0.1
+    prob.set_bcs([(O.face_nodes(pts, 0, 0.0), 0, 0.0), (O.face_nodes(pts, 1, 0.0), 1, 0.0),
+                  (O.face_nodes(pts, 2, 0.0), 2, 0.0), (O.face_nodes(pts, 2, 1.0), 2, disp)])
+    return prob
+
+
+def test_oracle_arc_length_step():
+    """Displacement-controlled arc-length steps (``solver.py:447-517``).  The loop tests the
+    residual of the iterate before its update, so a step started from an equilibrium makes
+    one update (the tangent predictor, sized by the constraint) and stops; a step started
+    off equilibrium iterates until the residual it starts an update from is below tol.
+    Each returned increment satisfies the arc-length constraint, and the BC rows follow
+    lambda."""
+    prob = _continuation_case()
+    ub = O._bc_vector(prob, prob.ndof)
+    dl = 0.4 * np.linalg.norm(ub)
+    bc_dofs, bc_vals = prob.bc_dofs_vals()
+    z = np.zeros(prob.ndof)
+    u, lam, du, dlam = O.arc_length_disp(prob, z, 0.0, z, 0.0, Delta_l=dl, tol=1e-8)
+    assert abs(np.sum(du ** 2) + dlam ** 2 * np.sum(ub ** 2) - dl ** 2) < 1e-10 * dl ** 2
+    assert np.abs(u[bc_dofs] - lam * bc_vals).max() < 1e-12
+    # the second step starts off equilibrium (the first was a predictor only) and corrects
+    calls = []
+    orig = prob.newton_update
+    prob.newton_update = lambda d, *a, **k: calls.append(1) or orig(d, *a, **k)
+    u2, lam2, du2, dlam2 = O.arc_length_disp(prob, u, lam, du, dlam, Delta_l=dl, tol=1e-8)
+    prob.newton_update = orig
+    assert len(calls) > 1 and lam2 > lam > 0
+    assert abs(np.sum(du2 ** 2) + dlam2 ** 2 * np.sum(ub ** 2) - dl ** 2) < 1e-10 * dl ** 2
+    assert np.abs(u2[bc_dofs] - lam2 * bc_vals).max() < 1e-12
+
+
+def test_oracle_dynamic_relaxation():
+    """Dynamic relaxation (``solver.py:656-795``) ends at the Newton solver's equilibrium,
+    to the effect of its max|R| tolerance."""
+    prob = _continuation_case(1e-3)
+    ud, its = O.dynamic_relax(prob, tol=1e-7)
+    assert its > 0
+    un, _ = O.solver(prob, {"tol": 1e-10, "rel_tol": 1e-14})
+    assert np.abs(ud - un).max() < 1e-6 * np.abs(un).max()
+    assert O.dr_damping(-1.0, 1e-3, 3.9) == 1e-3 and O.dr_damping(100.0, 1e-3, 3.9) == 3.9
