@@ -468,8 +468,9 @@ def run_batch_config(args, pkg, torch):
     t_batch = time.perf_counter() - t0
     regions = b.problem.timer_ms()
     host = dict(b.host_s)
-    newton = [int(x.max()) for x in b.stats["newton_iters"]]
+    newton_max = [int(x.max()) for x in b.stats["newton_iters"]]
     newton_mean = [float(x.mean()) for x in b.stats["newton_iters"]]
+    fallbacks = int(b.stats.get("predictor_fallbacks", 0))
     kry = [int(x.max()) for x in b.stats["krylov_iters"]]
     del b
     torch.cuda.empty_cache()
@@ -500,7 +501,8 @@ def run_batch_config(args, pkg, torch):
                       "max_rel_diff_vs_serial": rel,
                       "batched_regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
                       "batched_host_s": host,
-                      "batched_newton_iters": newton, "batched_newton_iters_mean": newton_mean,
+                      "batched_newton_iters": newton_max, "batched_newton_iters_mean": newton_mean,
+                      "batched_predictor_fallbacks": fallbacks,
                       "batched_krylov_iters_max": kry,
                       "batched_gp_updates_per_s": gps * nsteps / t_batch}))
 

@@ -24,6 +24,7 @@ from .material import MaterialSpec, random_quaternions
 from .mesh import Mesh, box_mesh, face_nodes, voronoi_grains
 from .problem import CrystalPlasticity, DeviceCSR, _stream
 from . import solver as _solver
+from .workloads import solve_with_fallback as _solve_with_fallback
 
 
 @dataclasses.dataclass
@@ -159,14 +160,22 @@ class Batch:
                                               out.data_ptr(), _stream()))
         return torch.sqrt(out).cpu().numpy()
 
-    def solve(self, rel_tol=1e-8, tol=1e-6, precond=1, ktol=1e-10, katol=1e-10, maxiter=10000, max_newton=100):
-        """Batched global Newton for the current BCs, dt and state."""
+    def solve(self, **options):
+        """Batched global Newton for the current BCs, dt and state (options of
+        ``_solve_from``), from the extrapolated guess under the ``"linear"`` predictor; if
+        that fails (an instance's extrapolation overshot into a state a local solve cannot
+        reach), again from the last solution, the reference driver's guess."""
+        if self.predictor == "linear" and self.prev is not None:
+            try:
+                return self._solve_from(2.0 * self.sol - self.prev, **options)
+            except (RuntimeError, FloatingPointError):
+                self.stats["predictor_fallbacks"] = self.stats.get("predictor_fallbacks", 0) + 1
+        return self._solve_from(self.sol.clone(), **options)
+
+    def _solve_from(self, dofs, rel_tol=1e-8, tol=1e-6, precond=1, ktol=1e-10, katol=1e-10, maxiter=10000,
+                    max_newton=100):
         p = self.problem
         lib = p.lib
-        if self.predictor == "linear" and self.prev is not None:
-            dofs = 2.0 * self.sol - self.prev
-        else:
-            dofs = self.sol.clone()
         trial = p.new_trial()
         with self._phase("assemble"):
             res, A = self._assemble(dofs, trial)
@@ -261,7 +270,7 @@ def run_serial(instances, disps, dt, device=None, prepared=None, solver_options=
             p.set_params(params)
             guess = 2.0 * sol - prev if (predictor == "linear" and prev is not None) else sol
             prev = sol
-            sol = _solver.solver(p, dict(base, initial_guess=[guess.reshape(-1, 3)]))[0].reshape(-1)
+            sol = _solve_with_fallback(_solver, p, base, guess, sol).reshape(-1)
             sig = p.compute_avg_stress(sol.reshape(-1, 3), params)
             params = p.update_int_vars_gp(sol.reshape(-1, 3), params)
             out[k, i] = float(sig[:, 2, 2].mean())

@@ -329,8 +329,14 @@ DIRECT_SOLVE = {"jax_solver": {"tol": 1e-12, "atol": 1e-30, "maxiter": 100000}}
 
 
 def _solve_to(problem, A, b, solver_options):
+    """A^-1 b from x0 = 0, solved for b / |b| and scaled back (a direct solver's answer does
+    not depend on the scale of b; the Krylov stop rule's absolute floor would)."""
     opts = {k: (dict(v) if isinstance(v, dict) else v) for k, v in (solver_options or DIRECT_SOLVE).items()}
-    return linear_solver(problem, A, b.contiguous(), torch.zeros_like(b), opts)
+    nb = float(torch.linalg.vector_norm(b))
+    if nb == 0.0:
+        return torch.zeros_like(b)
+    x = linear_solver(problem, A, (b / nb).contiguous(), torch.zeros_like(b), opts)
+    return x * nb
 
 
 def _tangent_bc(problem, dofs, scale=1.0):

@@ -97,7 +97,10 @@ class LoadStepper:
     dofs of equal load increments and close in the interior, so the first residual of a
     step is several times smaller and a plastic load step needs 3 Newton iterations instead
     of 5.  The stop rule is unchanged, so the converged solution is the same to the Newton
-    tolerance."""
+    tolerance.  An extrapolated guess can overshoot where the response turns plastic (the
+    second step doubles an elastic first one): a step whose solve fails from it (a local
+    solve that does not converge, a Newton or Krylov failure) is solved again from the
+    last solution, the reference driver's guess (counted in ``predictor_fallbacks``)."""
 
     def __init__(self, problem, solver_mod, workload, solver_options=None, predictor="previous"):
         import torch
@@ -123,9 +126,8 @@ class LoadStepper:
         guess = last
         if self.predictor == "linear" and self.prev is not None:
             guess = 2.0 * last - self.prev
-        opts = dict(self.options)
-        opts["initial_guess"] = [guess.reshape(-1, 3)]
-        sol = self.solver.solver(prob, opts)[0]
+        sol = solve_with_fallback(self.solver, prob, self.options, guess, last)
+        self.predictor_fallbacks = prob.stats.get("predictor_fallbacks", 0)
         sig = prob.compute_avg_stress(sol, self.params)
         self.params = prob.update_int_vars_gp(sol, self.params)
         self.prev = last
@@ -134,6 +136,21 @@ class LoadStepper:
             host_io[0].copy_(self.sol, non_blocking=True)
             host_io[1].copy_(sig.reshape(-1), non_blocking=True)
         return sig
+
+
+def solve_with_fallback(solver_mod, problem, options, guess, last):
+    """``solver`` from ``guess``; if that fails and ``guess`` is not ``last``, again from
+    ``last`` (the reference driver's guess)."""
+    opts = dict(options)
+    opts["initial_guess"] = [guess.reshape(-1, 3)]
+    try:
+        return solver_mod.solver(problem, opts)[0]
+    except (RuntimeError, FloatingPointError):
+        if guess is last:
+            raise
+    problem.stats["predictor_fallbacks"] = problem.stats.get("predictor_fallbacks", 0) + 1
+    opts["initial_guess"] = [last.reshape(-1, 3)]
+    return solver_mod.solver(problem, opts)[0]
 
 
 def fast_solver_options(precond=3, mg=None, grid_blocks=None, **newton):
