@@ -252,13 +252,12 @@ def spmv_roofline(prob, torch, lib, reps=50):
     return t, alg_bytes, 2.0 * nnz
 
 
-# DRAM bytes (read + write) per launch from the ncu capture summarised in
-# profiles/dram_fcc32_loadstep.md, on the 32^3 benchmark matrix: the standalone SpMV and
-# the persistent BiCGSTAB (the matrix is read from HBM once per solve, then from L2).
+# DRAM bytes (read + write) per launch from ncu captures on the 32^3 benchmark matrix: the
+# standalone SpMV (profiles/k_spmv_fcc32.md) and the persistent BiCGSTAB with the FP32
+# V-cycle (profiles/k_bicgstab_mg_fcc32.md; one Newton step's solve, ~12 iterations: the
+# matrix is read from HBM once per solve, then from L2).
 SPMV_DRAM_BYTES = {"c1": 72.4e6}
-# DRAM bytes of one k_bicgstab launch from ncu captures of the 32^3 bench matrix, by
-# (config, precond, V-cycle precision): Jacobi ~330 iterations, multigrid ~20-30
-KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 1, None): 75.7e6, ("c1", 3, "fp64"): 107.9e6, ("c1", 3, "fp32"): 3.684e9}
+KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 3, "fp32"): 88.8e6}
 
 
 def krylov_iteration_cost(prob, precond=1):
@@ -363,12 +362,12 @@ def run_reference(args):
 
 
 def run_adjoint_config(args, pkg, problem_mod, torch):
-    """configs[3] as its own JSON line."""
+    """The adjoint workload (gradient on the 32^3 RVE) as its own JSON line."""
     print(json.dumps(adjoint_record(args, pkg, problem_mod, torch)))
 
 
 def adjoint_record(args, pkg, problem_mod, torch):
-    """configs[3]: gradient of the sigma_zz-curve misfit on the 32^3 / 64-grain RVE with
+    """The adjoint workload: gradient of the sigma_zz-curve misfit on the 32^3 / 64-grain RVE with
     respect to (h0, g0, gs, a, m) and the 64x3 Euler angles; backward / forward time."""
     from importlib import import_module
     adjoint = import_module("jax-cpfem_gb300.adjoint")
@@ -436,7 +435,7 @@ def adjoint_record(args, pkg, problem_mod, torch):
 
 
 def run_batch_config(args, pkg, torch):
-    """configs[4]: 256 RVEs (edges 8..24, 8-64 grains, parameters +-20 %) batched in one
+    """The RVE batch: 256 RVEs (edges 8..24, 8-64 grains, parameters +-20 %) batched in one
     ragged launch per Newton stage vs the same solves one at a time."""
     from importlib import import_module
     batch = import_module("jax-cpfem_gb300.batch")
@@ -516,7 +515,8 @@ def main():
     ap.add_argument("--edge", type=int, default=N_EDGE, help="cube edge in cells (32 = the benchmark)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sub-records", action="store_true",
-                    help="skip the configs[3] adjoint record appended to the default line")
+                    help="skip the records appended to the default line: the adjoint on the same RVE and the "
+                         "10^3 copper and 64^3 BCC24 load histories")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
                     help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
@@ -612,7 +612,8 @@ def main():
             if args.mg_precision:   # a fixed precision is not searched
                 start["precision"] = args.mg_precision
                 search = tuple(kv for kv in search if kv[0] != "precision")
-            cfg, table = tuning.tune_linear_solver(prob, A, -res, x0, search=search, start=start)
+            cfg, table = tuning.tune_linear_solver(prob, A, -res, x0, search=search, start=start,
+                                                   tol=args.krylov_tol)
             mg_options = dict({k: v for k, v in cfg.items() if k != "grid_blocks"}, refresh=args.mg_refresh)
             set_solver(args.precond, mg_options, cfg["grid_blocks"])
             tuned = {"chosen": cfg, "candidates": len(table),
@@ -794,12 +795,29 @@ def main():
            "gpu_launches": None}
     out["gpu_launches"] = counter.launches
     if rank == 0 and world == 1 and args.config == "c1" and not args.no_sub_records:
-        # the differentiation form on the same RVE (configs[3]), after the timed region
-        out["sub_records"] = {"c3_adjoint": adjoint_record(args, pkg, problem_mod, torch)}
+        # the differentiation form on the same RVE, after the timed region, and the 10^3
+        # copper single crystal and the 64^3 BCC24 polycrystal
+        # over their whole load histories (10 and 30 steps: warm-up + timed), each in a
+        # process of its own
+        out["sub_records"] = {"c3_adjoint": adjoint_record(args, pkg, problem_mod, torch),
+                              "c0_copper": sub_bench(["--config", "c0", "--warmup", "3", "--steps", "7"]),
+                              "c2_bcc24": sub_bench(["--config", "c2", "--warmup", "3", "--steps", "27"])}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def sub_bench(flags):
+    """The JSON line of ``bench.py`` run with ``flags`` (and no CPU baseline, Jacobi legs or
+    sub-records) in a child process."""
+    cmd = [sys.executable, os.path.abspath(__file__), *flags, "--no-cpu-baseline", "--no-jacobi-leg",
+           "--no-sub-records"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"error": f"exit {r.returncode}: {(r.stderr or r.stdout).strip().splitlines()[-1:]}"}
+    return json.loads(lines[-1])
 
 
 def max_over_ranks(t, world, device):

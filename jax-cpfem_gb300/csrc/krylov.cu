@@ -833,8 +833,12 @@ __device__ void mg_vcycle(const cpfem_mg_t& mg, const double* __restrict__ vals0
 }
 
 // MGP: 0 the point preconditioners of precond 0..2, 1 the FP64 V-cycle, 2 the FP32 V-cycle.
+// The FP32 V-cycle runs one block per SM (every block reserves the shared memory of the
+// block-local levels), so it may take the whole register file: with up to 255 registers
+// the fine-level row products keep more loads in flight (219.8 vs 237.4 us per iteration at
+// 32^3, measured per phase).
 template <bool TRANS, int MGP>
-__global__ void __launch_bounds__(kPThreads, 3) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
+__global__ void __launch_bounds__(kPThreads, MGP == 2 ? 1 : 3) k_bicgstab(const cpfem_sell_t L, const double* __restrict__ vals,
                                                         const double* __restrict__ b, double* __restrict__ x,
                                                         KWork w, int precond, double tol, double atol,
                                                         int maxiter, int max_restarts, const cpfem_mg_t mg) {

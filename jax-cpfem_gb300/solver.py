@@ -325,17 +325,25 @@ def apply_bc_vec(res_vec, dofs, problem, scale=1.0):
 # (``jax_solver`` options, or a ``custom_solver`` such as a host direct solver).  Neither
 # routine commits internal variables: the caller does, between steps, as with ``solver``.
 # ---------------------------------------------------------------------------------------
-DIRECT_SOLVE = {"jax_solver": {"tol": 1e-12, "atol": 1e-30, "maxiter": 100000}}
+DIRECT_SOLVE = {"jax_solver": {"tol": 1e-12, "atol": 1e-30, "maxiter": 100000, "restart_on_breakdown": True}}
 
 
 def _solve_to(problem, A, b, solver_options):
-    """A^-1 b from x0 = 0, solved for b / |b| and scaled back (a direct solver's answer does
-    not depend on the scale of b; the Krylov stop rule's absolute floor would)."""
+    """A^-1 b for the row-eliminated A, solved for b / |b| and scaled back (a direct solver's
+    answer does not depend on the scale of b; the Krylov stop rule's absolute floor would).
+    The start has the Dirichlet components of the answer (A's unit rows give them): a start
+    of zero would make the first residual, and so BiCGSTAB's shadow vector, live on the
+    Dirichlet dofs alone, orthogonal to every later residual (a breakdown at once when the
+    right-hand side is u_b)."""
     opts = {k: (dict(v) if isinstance(v, dict) else v) for k, v in (solver_options or DIRECT_SOLVE).items()}
     nb = float(torch.linalg.vector_norm(b))
     if nb == 0.0:
         return torch.zeros_like(b)
-    x = linear_solver(problem, A, (b / nb).contiguous(), torch.zeros_like(b), opts)
+    bn = (b / nb).contiguous()
+    idx, _ = _bc_index(problem)
+    x0 = torch.zeros_like(b)
+    x0[idx] = bn[idx]
+    x = linear_solver(problem, A, bn, x0, opts)
     return x * nb
 
 

@@ -32,14 +32,15 @@ SEARCH = (("precision", ("fp64", "fp32")),
           ("grid_blocks", (0, 76, 104, 152, 304)))
 
 
-def _time_solve(problem, A, b, x0, cfg, reps):
+def _time_solve(problem, A, b, x0, cfg, reps, tol=1e-10):
     mg = {k: cfg[k] for k in MG_KEYS}
-    _solver.bicgstab(problem, A, b, x0, precond=3, mg_options=mg, grid_blocks=cfg["grid_blocks"])
+    _solver.bicgstab(problem, A, b, x0, precond=3, tol=tol, mg_options=mg, grid_blocks=cfg["grid_blocks"])
     best, its, ok = float("inf"), None, True
     for _ in range(reps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        _, k, conv = _solver.bicgstab(problem, A, b, x0, precond=3, mg_options=mg, grid_blocks=cfg["grid_blocks"])
+        _, k, conv = _solver.bicgstab(problem, A, b, x0, precond=3, tol=tol, mg_options=mg,
+                                      grid_blocks=cfg["grid_blocks"])
         e1.record()
         torch.cuda.synchronize()
         best = min(best, e0.elapsed_time(e1))
@@ -47,12 +48,13 @@ def _time_solve(problem, A, b, x0, cfg, reps):
     return best, its, ok
 
 
-def tune_linear_solver(problem, A, b, x0, reps=2, search=SEARCH, start=None):
-    """Coordinate search over the multigrid / launch settings on the system A x = b.
+def tune_linear_solver(problem, A, b, x0, reps=2, search=SEARCH, start=None, tol=1e-10):
+    """Coordinate search over the multigrid / launch settings on the system A x = b, solved
+    to the relative tolerance the caller will use (``tol``).
     Returns (best configuration dict, list of (configuration, ms, iterations))."""
     cfg = dict(DEFAULT if start is None else start)
     table = []
-    ms, its, ok = _time_solve(problem, A, b, x0, cfg, reps)
+    ms, its, ok = _time_solve(problem, A, b, x0, cfg, reps, tol)
     table.append((dict(cfg), ms, its))
     best_ms = ms if ok else float("inf")
     for key, values in search:
@@ -62,7 +64,7 @@ def tune_linear_solver(problem, A, b, x0, reps=2, search=SEARCH, start=None):
             trial = dict(cfg)
             trial[key] = v
             try:
-                t_ms, t_its, t_ok = _time_solve(problem, A, b, x0, trial, reps)
+                t_ms, t_its, t_ok = _time_solve(problem, A, b, x0, trial, reps, tol)
             except (ValueError, RuntimeError):
                 continue
             table.append((dict(trial), t_ms, t_its))
