@@ -442,12 +442,14 @@ def run_batch_config(args, pkg, torch):
     inst = batch.sample_instances(args.instances, pkg.material.BENCH_STEEL, seed=SEED)
     nsteps = args.load_steps or 20
     disps = STRAIN_STEP * np.arange(1, nsteps + 1)
-    # both arms run the same per-instance algorithm: Jacobi BiCGSTAB (the ragged solver's),
-    # and the benchmark path's predictor, Krylov tolerance, FP32 tangent and Newton limit
+    # both arms run the same per-instance algorithm: Jacobi or 3x3 block-Jacobi BiCGSTAB (the
+    # ragged solver's preconditioners), and the benchmark path's predictor, Krylov tolerance,
+    # FP32 tangent and Newton limit
     fast = args.predictor == "linear"
     newton = dict(NEWTON) if fast else dict(NEWTON_REF)
     ktol = args.krylov_tol
-    serial_opts = dict(newton, jax_solver={"tol": ktol})
+    pc = args.batch_precond
+    serial_opts = dict(newton, jax_solver={"tol": ktol, "precond": {1: True, 2: "block3"}[pc]})
     # untimed warm-up of every kernel on a tiny batch (module loads, allocator growth)
     w = batch.Batch(batch.sample_instances(2, pkg.material.BENCH_STEEL, seed=SEED + 1, edges=(2,), grains=(2, 2)))
     w.step(STRAIN_STEP, DT)
@@ -462,7 +464,7 @@ def run_batch_config(args, pkg, torch):
     t_setup_batch = time.perf_counter() - t0
     b.problem.timing = True
     t0 = time.perf_counter()
-    szz = np.stack([b.step(d, DT, ktol=ktol, **newton).cpu().numpy() for d in disps], axis=1)
+    szz = np.stack([b.step(d, DT, ktol=ktol, precond=pc, **newton).cpu().numpy() for d in disps], axis=1)
     torch.cuda.synchronize()
     t_batch = time.perf_counter() - t0
     regions = b.problem.timer_ms()
@@ -491,7 +493,8 @@ def run_batch_config(args, pkg, torch):
                       "config": {"workload": f"batch-{len(inst)}-rves-edges8-24", "instances": len(inst),
                                  "gauss_points": gps, "load_steps": nsteps,
                                  "timed": "load steps only; problem set-up timed separately on both sides",
-                                 "both_arms": {"precond": "jacobi", "krylov_tol": ktol, "predictor": args.predictor,
+                                 "both_arms": {"precond": {1: "jacobi", 2: "block-jacobi-3x3"}[pc],
+                                               "krylov_tol": ktol, "predictor": args.predictor,
                                                "tangent": "fp32" if args.fp32_tangent else "fp64",
                                                "newton": f"tol {newton['tol']:g} / rel_tol {newton['rel_tol']:g}"}},
                       "batched_s": t_batch, "serial_s": t_serial,
@@ -518,8 +521,9 @@ def main():
                     help="skip the records appended to the default line: the adjoint on the same RVE and the "
                          "10^3 copper and 64^3 BCC24 load histories")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--mg-refresh", default="newton", choices=["newton", "step"],
-                    help="multigrid coarse operators rebuilt per Newton iteration (default) or once per load step")
+    ap.add_argument("--mg-refresh", default=BENCH["mg_refresh"], choices=["newton", "step"],
+                    help="multigrid coarse operators rebuilt once per load step (default: the preconditioner of a "
+                         "step's later Newton systems is the first one's) or per Newton iteration")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the linear-solver autotuning during warm-up and use its stored choice for this "
                          "workload (workloads.TUNED_MG)")
@@ -539,6 +543,9 @@ def main():
     ap.add_argument("--krylov-tol", type=float, default=BENCH["krylov_tol"],
                     help="relative tolerance of each Newton step's BiCGSTAB (the reference's: 1e-10; atol stays "
                          "1e-10): an inexact Newton step with the same Newton stop rule")
+    ap.add_argument("--batch-precond", type=int, default=1, choices=[1, 2],
+                    help="RVE batch: the preconditioner of both arms' BiCGSTAB, 1 Jacobi (the reference's) or "
+                         "2 3x3 block-Jacobi")
     ap.add_argument("--load-steps", type=int, default=0)
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--fd-check", action="store_true")

@@ -32,7 +32,7 @@ def test_tuner_coordinate_search_keeps_the_fastest_converging(tuning, monkeypatc
             "coarse_sweeps": {4: 0.2, 8: 0.0, 12: 0.7}, "grid_blocks": {0: 0.0, 152: -0.5, 304: -2.0}}
     seen = []
 
-    def fake_time(problem, A, b, x0, cfg, reps):
+    def fake_time(problem, A, b, x0, cfg, reps, tol=1e-10):
         seen.append(dict(cfg))
         if cfg["grid_blocks"] == 76:
             raise RuntimeError("rejected")
