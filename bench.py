@@ -257,7 +257,7 @@ def spmv_roofline(prob, torch, lib, reps=50):
 # V-cycle (profiles/k_bicgstab_mg_fcc32.md; one Newton step's solve, ~12 iterations: the
 # matrix is read from HBM once per solve, then from L2).
 SPMV_DRAM_BYTES = {"c1": 72.4e6}
-KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 3, "fp32"): 88.8e6}
+KRYLOV_DRAM_BYTES_PER_LAUNCH = {("c1", 3, "fp32"): 109.1e6}
 
 
 def krylov_iteration_cost(prob, precond=1):
