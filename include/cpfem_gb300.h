@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define CPFEM_ABI_VERSION 2
+#define CPFEM_ABI_VERSION 3
 #define CPFEM_MAX_SLIP 24
 
 enum cpfem_status {
@@ -407,7 +407,8 @@ typedef struct {
 } cpfem_mg_t;
 
 /* Host: sizeof of this header's structs as compiled into the library (0 material, 1 gp
- * args, 2 vjp args, 3 sell, 4 mg hierarchy, 5 krylov opts; 0 for any other value), so a
+ * args, 2 vjp args, 3 sell, 4 mg hierarchy, 5 krylov opts, 6 solve report; 0 for any other
+ * value), so a
  * binding can check its own mirror of each layout. */
 size_t cpfem_struct_size(int32_t which);
 /* Host: the slot table of one level from its node-block CSR pattern (rows sorted, as
@@ -419,6 +420,20 @@ int cpfem_mg_slot_table(int32_t num_nodes, const int32_t* dims, const int32_t* n
  * Galerkin coarse operators and their block-Jacobi inverses.  Once per new tangent. */
 int cpfem_mg_setup(const cpfem_mg_t* mg, const double* values0, void* stream);
 
+/* What one BiCGSTAB launch reports (cpfem_bicgstab_last_stats_ex returns its values; with
+ * cpfem_krylov_opts_t.flags bit 1 it is copied to the caller's memory instead). */
+typedef struct {
+  int32_t k;              /* iterations, or jax's breakdown code (-10 rho, -11 omega/alpha), or
+                             -12 (an FP32 V-cycle whose residual grew by 1e8 or went non-finite) */
+  int32_t error;          /* nonzero: a grid barrier gave up waiting; the solve is invalid */
+  double rs, atol2;       /* ||r||^2 of the recursion at the end, and the stop threshold
+                             max(tol^2 b.b, atol^2): converged when rs <= atol2 */
+  double rho, alpha, omega;   /* scalars of the last iteration */
+  int32_t restarts, pad;
+  double true_rs;         /* ||b - A x||^2 of the returned x (flags bit 0), else -1 */
+  double bb;              /* b.b */
+} cpfem_solve_report_t;
+
 typedef struct {
   int32_t precond;        /* 0 none, 1 Jacobi (the reference), 2 3x3 block-Jacobi, 3 multigrid */
   int32_t transpose;      /* solve A^T x = b (precond 0..2) */
@@ -429,7 +444,13 @@ typedef struct {
   int32_t grid_blocks;    /* blocks of the persistent launch; 0: one per 256 nodes, at most the
                              co-resident limit (larger requests are clamped to it) */
   int32_t flags;          /* bit 0: also form ||b - A x||^2 of the returned x in the same launch
-                             (cpfem_bicgstab_last_stats_ex), for the caller's true-residual check */
+                             (cpfem_bicgstab_last_stats_ex), for the caller's true-residual check;
+                             bit 1: deferred report -- the call queues the copy of the launch's
+                             report to `report` on the stream and returns without waiting for
+                             the solve (info and the last-solve statistics are not updated);
+                             the caller reads `report` after its next synchronisation of the
+                             stream, and must treat report->error as a failed solve */
+  cpfem_solve_report_t* report;   /* flags bit 1: host memory (pinned, for an asynchronous copy) */
 } cpfem_krylov_opts_t;
 int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const double* b, double* x,
                       const cpfem_krylov_opts_t* opts, void* workspace, int32_t* info, void* stream);

@@ -138,6 +138,22 @@ class MGHierarchy(ctypes.Structure):
     ]
 
 
+class SolveReport(ctypes.Structure):
+    _fields_ = [
+        ("k", ctypes.c_int32),
+        ("error", ctypes.c_int32),
+        ("rs", ctypes.c_double),
+        ("atol2", ctypes.c_double),
+        ("rho", ctypes.c_double),
+        ("alpha", ctypes.c_double),
+        ("omega", ctypes.c_double),
+        ("restarts", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("true_rs", ctypes.c_double),
+        ("bb", ctypes.c_double),
+    ]
+
+
 class KrylovOpts(ctypes.Structure):
     _fields_ = [
         ("precond", ctypes.c_int32),
@@ -149,6 +165,7 @@ class KrylovOpts(ctypes.Structure):
         ("mg", ctypes.POINTER(MGHierarchy)),
         ("grid_blocks", ctypes.c_int32),
         ("flags", ctypes.c_int32),
+        ("report", ctypes.c_void_p),
     ]
 
 
@@ -197,7 +214,7 @@ SIGNATURES = {
 }
 
 # the order of cpfem_struct_size's argument
-STRUCTS = (Material, GPArgs, VjpArgs, Sell, MGHierarchy, KrylovOpts)
+STRUCTS = (Material, GPArgs, VjpArgs, Sell, MGHierarchy, KrylovOpts, SolveReport)
 
 _lib = None
 
@@ -215,7 +232,7 @@ def load():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.cpfem_abi_version() != 2:
+    if lib.cpfem_abi_version() != 3:
         raise ImportError("libcpfem_gb300.so ABI version mismatch")
     for which, st in enumerate(STRUCTS):
         if lib.cpfem_struct_size(which) != ctypes.sizeof(st):

@@ -34,20 +34,14 @@ struct GridSync {
   int pad;
 };
 
-struct SolveOut {
-  int k;
-  int error;
-  double rs;
-  double atol2;
-  double rho, alpha, omega;   // scalars of the last iteration (rho: the one it started with)
-  int restarts;
-  int pad;
-  double true_rs;             // ||b - A x||^2 at the end (kKrylovTrueResidual), else -1
-  double bb;                  // b.b
-};
+// the launch's report, written by the kernel into the workspace (the public layout)
+using SolveOut = cpfem_solve_report_t;
+static_assert(sizeof(SolveOut) == 72 && offsetof(SolveOut, true_rs) == 56, "solve report layout");
 
-// cpfem_krylov_opts_t.flags: also form the true residual of the returned x
+// cpfem_krylov_opts_t.flags: also form the true residual of the returned x; report
+// asynchronously instead of waiting for the solve
 constexpr int kKrylovTrueResidual = 1;
+constexpr int kKrylovDeferred = 2;
 
 static thread_local SolveOut g_last_solve = {0, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 0, 0, -1.0, 0.0};
 
@@ -1074,7 +1068,7 @@ template <bool TRANS>
 static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double* b, double* x, int precond,
                         double tol, double atol, int32_t maxiter, void* workspace, int32_t* info, cudaStream_t s,
                         int max_restarts = 0, const cpfem_mg_t* mgp = nullptr, int grid_blocks = 0,
-                        int flags = 0) {
+                        int flags = 0, cpfem_solve_report_t* report = nullptr) {
   KWork w;
   carve(workspace, L.num_nodes, &w);
   CPFEM_CUDA_TRY(cudaMemsetAsync(w.sync, 0, sizeof(GridSync), s));
@@ -1122,6 +1116,12 @@ static int run_bicgstab(const cpfem_sell_t& L, const double* vals, const double*
     CPFEM_CUDA_TRY(cudaGetLastError());
     k_sum_partials<<<1, 32, 0, s>>>(w.partials, kVecBlocks, &w.out->true_rs);
     CPFEM_CUDA_TRY(cudaGetLastError());
+  }
+  if (flags & kKrylovDeferred) {
+    // queued behind the solve and the true residual: the caller reads it after its next
+    // synchronisation of the stream
+    CPFEM_CUDA_TRY(cudaMemcpyAsync(report, w.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, s));
+    return CPFEM_OK;
   }
   SolveOut out;
   CPFEM_CUDA_TRY(cudaMemcpyAsync(&out, w.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, s));
@@ -1376,19 +1376,20 @@ int cpfem_bicgstab_ex(const cpfem_sell_t* sell, const double* values, const doub
   CPFEM_REQUIRE(opts->max_restarts >= 0, "max_restarts must be >= 0");
   CPFEM_REQUIRE(opts->grid_blocks >= 0, "grid_blocks must be >= 0");
   CPFEM_REQUIRE(!opts->transpose || sell->tpos != nullptr, "transpose needs tpos");
+  CPFEM_REQUIRE(!(opts->flags & kKrylovDeferred) || opts->report != nullptr, "a deferred report needs opts.report");
   cudaStream_t s = (cudaStream_t)stream;
   if (opts->transpose)
     return run_bicgstab<true>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                              info, s, opts->max_restarts, opts->mg, opts->grid_blocks, opts->flags);
+                              info, s, opts->max_restarts, opts->mg, opts->grid_blocks, opts->flags, opts->report);
   return run_bicgstab<false>(*sell, values, b, x, opts->precond, opts->tol, opts->atol, opts->maxiter, workspace,
-                             info, s, opts->max_restarts, opts->mg, opts->grid_blocks, opts->flags);
+                             info, s, opts->max_restarts, opts->mg, opts->grid_blocks, opts->flags, opts->report);
 }
 
 int cpfem_bicgstab(const cpfem_sell_t* sell, const double* values, const double* b, double* x, int32_t precond,
                    int32_t transpose, double tol, double atol, int32_t maxiter, void* workspace, int32_t* info,
                    void* stream) {
   CPFEM_REQUIRE(precond >= 0 && precond <= 2, "precond must be 0, 1 or 2 (multigrid: cpfem_bicgstab_ex)");
-  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol, nullptr, 0, 0};
+  const cpfem_krylov_opts_t o = {precond, transpose, maxiter, 0, tol, atol, nullptr, 0, 0, nullptr};
   return cpfem_bicgstab_ex(sell, values, b, x, &o, workspace, info, stream);
 }
 

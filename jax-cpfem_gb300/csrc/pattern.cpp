@@ -282,6 +282,7 @@ extern "C" size_t cpfem_struct_size(int32_t which) {
     case 3: return sizeof(cpfem_sell_t);
     case 4: return sizeof(cpfem_mg_t);
     case 5: return sizeof(cpfem_krylov_opts_t);
+    case 6: return sizeof(cpfem_solve_report_t);
     default: return 0;
   }
 }

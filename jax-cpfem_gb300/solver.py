@@ -36,22 +36,43 @@ def norm(problem, x):
     return math.sqrt(_dot(problem, x, x))
 
 
+class DeferredSolveFailed(Exception):
+    """A deferred BiCGSTAB solve (``bicgstab(..., deferred=True)``) did not pass its checks
+    when its report was read; the Newton iteration that used it is redone with a checked
+    solve."""
+
+
+def _report_buffer(problem):
+    """The problem's pinned host copy of a deferred solve's report."""
+    buf = getattr(problem, "_report_host", None)
+    if buf is None:
+        buf = problem._report_host = torch.zeros(ctypes.sizeof(_capi.SolveReport), dtype=torch.uint8).pin_memory()
+    return buf
+
+
 def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, restarts=0,
-             mg_options=None, grid_blocks=0):
+             mg_options=None, grid_blocks=0, deferred=False):
     """``jax.scipy.sparse.linalg.bicgstab`` on the device matrix (``solver.py:34-40``), one
     persistent cooperative launch.  precond: 0 none, 1 Jacobi 1/diag(A) (the
     reference), 2 3x3 block-Jacobi, 3 geometric multigrid V-cycle (structured box
     meshes; ``mg_options`` go to ``CrystalPlasticity.multigrid``).  restarts > 0 restarts at
     a breakdown instead of stopping there (jax stops).  Returns (x, iterations or breakdown
-    code, converged)."""
+    code, converged).  ``deferred``: the call returns as soon as the solve is queued, with
+    (x, None, None); its report is copied to pinned memory behind it and checked by
+    ``resolve_deferred`` after the caller's next synchronisation (``solver``'s Newton loop:
+    the residual norm of the next iterate), so the host prepares the next pass while the
+    solve runs."""
     lib = problem.lib
     x = x0.clone()
     nbytes = int(lib.cpfem_bicgstab_workspace_bytes(problem.num_nodes))
     ws = problem._buf("krylov_ws", (nbytes // 8 + 64,))
     info = np.zeros(2, dtype=np.int32)
-    # flags 1: the launch also forms ||b - A x|| of its x (read below with the stats)
+    # flags 1: the launch also forms ||b - A x|| of its x (read below with the stats);
+    # flags 2: the report goes to pinned memory without waiting
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
-                            float(tol), float(atol), None, int(grid_blocks), 1)
+                            float(tol), float(atol), None, int(grid_blocks), 1 | (2 if deferred else 0))
+    if deferred:
+        opts.report = _report_buffer(problem).data_ptr()
     mg_options = dict(mg_options or {})
     if int(precond) == 3:
         if getattr(problem, "mg_fp64_only", False):
@@ -62,6 +83,10 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     with problem.region("bicgstab"):
         _capi.check(lib.cpfem_bicgstab_ex(problem.sell, _dev_ptr(A.values), _dev_ptr(b), _dev_ptr(x),
                                           ctypes.byref(opts), _dev_ptr(ws), info.ctypes.data, _stream()))
+    if deferred:
+        problem._pending_solve = {"fp32": int(precond) == 3 and opts.mg.contents.precision == 1,
+                                  "tol": float(tol), "atol": float(atol)}
+        return x, None, None
     k, ok = int(info[0]), bool(info[1])
     st = np.zeros(9)
     _capi.check(lib.cpfem_bicgstab_last_stats_ex(st.ctypes.data, 9))
@@ -84,7 +109,30 @@ def _fp32_solve_ok(converged, rn, bn, tol, atol):
     return converged and math.isfinite(rn) and rn <= 10.0 * max(tol * bn, atol)
 
 
-def jax_solve(problem, A, b, x0, precond=True, opts=None):
+def resolve_deferred(problem):
+    """Check the report of the problem's deferred solve, if one is pending (call after a
+    synchronisation of the stream): the Krylov count joins ``stats``; a failed grid barrier,
+    an FP32 V-cycle solve that misses the stop rule (which switches the problem to the FP64
+    V-cycle, as the checked path does) or a true residual that fails ``jax_solve``'s
+    ``||Ax - b|| < 0.1`` raise ``DeferredSolveFailed``."""
+    p = getattr(problem, "_pending_solve", None)
+    if p is None:
+        return
+    problem._pending_solve = None
+    r = _capi.SolveReport.from_address(_report_buffer(problem).data_ptr())
+    rn = math.sqrt(r.true_rs) if r.true_rs >= 0.0 else float("nan")
+    if r.error:
+        raise DeferredSolveFailed("a grid barrier of the solve timed out")
+    if p["fp32"] and not _fp32_solve_ok(r.rs <= r.atol2, rn, math.sqrt(r.bb), p["tol"], p["atol"]):
+        problem.mg_fp64_only = True
+        problem.stats["mg_fp64_fallbacks"] = problem.stats.get("mg_fp64_fallbacks", 0) + 1
+        raise DeferredSolveFailed("the FP32 V-cycle solve missed the stop rule")
+    if not rn < 0.1:
+        raise DeferredSolveFailed(f"the solve's true residual is {rn}")
+    problem.stats["krylov_iters"].append(int(r.k))
+
+
+def jax_solve(problem, A, b, x0, precond=True, opts=None, deferred=False):
     """``solver.py:19-48``: BiCGSTAB, tol = atol = 1e-10, maxiter = 10000, then the
     ``||Ax - b|| < 0.1`` check."""
     opts = opts or {}
@@ -94,7 +142,10 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
     rs = 20 if rs is True else int(rs or 0)
     x, k, ok = bicgstab(problem, A, b, x0, precond=pc, tol=opts.get("tol", 1e-10),
                         atol=opts.get("atol", 1e-10), maxiter=opts.get("maxiter", 10000), restarts=rs,
-                        mg_options=opts.get("mg_options"), grid_blocks=opts.get("grid_blocks", 0))
+                        mg_options=opts.get("mg_options"), grid_blocks=opts.get("grid_blocks", 0),
+                        deferred=deferred)
+    if deferred:
+        return x
     problem.stats["krylov_iters"].append(k)
     last = getattr(problem, "_true_res", None)
     if last is not None and last[0] is x and last[1] is b:
@@ -109,13 +160,13 @@ def jax_solve(problem, A, b, x0, precond=True, opts=None):
     return x
 
 
-def linear_solver(problem, A, b, x0, solver_options):
-    """``solver.py:91-113``."""
+def linear_solver(problem, A, b, x0, solver_options, deferred=False):
+    """``solver.py:91-113``.  ``deferred`` applies to the device BiCGSTAB (``jax_solver``)."""
     if len(solver_options.keys() & set(_KEYS)) == 0:
         solver_options["jax_solver"] = {}
     if "jax_solver" in solver_options:
         o = solver_options["jax_solver"] or {}
-        return jax_solve(problem, A, b, x0, o.get("precond", True), o)
+        return jax_solve(problem, A, b, x0, o.get("precond", True), o, deferred=deferred)
     if "custom_solver" in solver_options:
         x = solver_options["custom_solver"](A, b, x0, solver_options)
         return torch.as_tensor(x, dtype=torch.float64, device=problem.device).reshape(-1).contiguous()
@@ -125,11 +176,14 @@ def linear_solver(problem, A, b, x0, solver_options):
 
 def _norm_checked(problem, x, status):
     """||x|| and the status word of the constitutive pass that produced x, read in one
-    device-to-host transfer; raises on a failed local solve as the pass's own check would."""
+    device-to-host transfer; checks a deferred solve's report first (the pass ran at the
+    iterate that solve produced), then raises on a failed local solve as the pass's own
+    check would."""
     ws = problem._buf("dot_ws", (int(problem.lib.cpfem_dot_workspace_bytes(x.numel())) // 8 + 64,))
     out = problem._buf("dot_out", (1,))
     _capi.check(problem.lib.cpfem_dot(x.numel(), _dev_ptr(x), _dev_ptr(x), _dev_ptr(out), _dev_ptr(ws), _stream()))
     both = torch.stack([out[0], status[0].to(torch.float64)]).cpu()
+    resolve_deferred(problem)
     problem._check_status_bits(int(both[1]))
     return math.sqrt(float(both[0]))
 
@@ -206,11 +260,11 @@ def line_search(problem, dofs, inc):
     return out
 
 
-def linear_incremental_solver(problem, res_vec, A, dofs, solver_options):
+def linear_incremental_solver(problem, res_vec, A, dofs, solver_options, deferred=False):
     """``solver.py:213-237``."""
     b = torch.neg(res_vec)
     x0 = initial_increment(problem, dofs)
-    inc = linear_solver(problem, A, b, x0, solver_options)
+    inc = linear_solver(problem, A, b, x0, solver_options, deferred=deferred)
     if solver_options.get("line_search_flag", False):
         return line_search(problem, dofs, inc)
     out = dofs.clone()
@@ -218,10 +272,27 @@ def linear_incremental_solver(problem, res_vec, A, dofs, solver_options):
     return out
 
 
+def _defers(problem, solver_options):
+    """Whether the Newton loop may defer the checks of its Krylov solves: the device
+    BiCGSTAB without a line search (whose trial points would use the unchecked increment),
+    unless the problem opts out (``problem.defer_krylov_checks = False``)."""
+    if not getattr(problem, "defer_krylov_checks", True) or solver_options.get("line_search_flag", False):
+        return False
+    keys = solver_options.keys() & set(_KEYS)
+    return not keys or keys == {"jax_solver"}
+
+
 def solver(problem, solver_options=None):
-    """Row-elimination Newton solve; returns ``[sol (num_nodes, 3)]``."""
+    """Row-elimination Newton solve; returns ``[sol (num_nodes, 3)]``.
+
+    Each iteration's BiCGSTAB is deferred (``bicgstab(deferred=True)``): the host queues the
+    next constitutive pass without waiting for the solve, and the solve's report is checked
+    together with that pass's residual norm; an iteration whose solve fails the check is
+    redone from its start with a checked solve, so the iterates and the result are those of
+    the checked loop."""
     solver_options = {} if solver_options is None else solver_options
     start = time.time()
+    problem._pending_solve = None
     if solver_options.get("initial_guess") is not None:
         dofs = _flat(solver_options["initial_guess"], problem.device).clone()
     else:
@@ -229,6 +300,7 @@ def solver(problem, solver_options=None):
     rel_tol = solver_options.get("rel_tol", 1e-8)
     tol = solver_options.get("tol", 1e-6)
     max_newton = solver_options.get("max_newton", 100)
+    defer = _defers(problem, solver_options)
 
     res_vec, A, status = _update_deferred(problem, dofs)
     res_val = _norm_checked(problem, res_vec, status)
@@ -238,10 +310,9 @@ def solver(problem, solver_options=None):
     it = 0
     limit = max(tol, rel_tol * res_val_initial)
     skip = getattr(problem, "skip_final_tangent", True)
-    while (rel_res_val > rel_tol) and (res_val > tol):
-        if it >= max_newton:
-            raise RuntimeError(f"global Newton did not converge in {max_newton} iterations (res = {res_val})")
-        dofs = linear_incremental_solver(problem, res_vec, A, dofs, solver_options)
+
+    def iteration(res_vec, A, dofs, deferred):
+        dofs = linear_incremental_solver(problem, res_vec, A, dofs, solver_options, deferred=deferred)
         res_vec = None
         if skip and _expect_converged(history, limit):
             # the last iterate needs no tangent: residual (and trial state) only, and the
@@ -257,6 +328,22 @@ def solver(problem, solver_options=None):
         if res_vec is None:
             res_vec, A, status = _update_deferred(problem, dofs)
             res_val = _norm_checked(problem, res_vec, status)
+        return res_vec, A, dofs, res_val
+
+    while (rel_res_val > rel_tol) and (res_val > tol):
+        if it >= max_newton:
+            raise RuntimeError(f"global Newton did not converge in {max_newton} iterations (res = {res_val})")
+        try:
+            res_vec, A, dofs, res_val = iteration(res_vec, A, dofs, defer)
+        except DeferredSolveFailed:
+            # redo the iteration from its start with a checked solve: the system at the
+            # iteration's start is formed again (its buffers now hold the failed iterate's)
+            problem.stats["deferred_redone"] = problem.stats.get("deferred_redone", 0) + 1
+            problem._pending_solve = None
+            dofs_start = dofs
+            res_vec, A, status = _update_deferred(problem, dofs_start)
+            _norm_checked(problem, res_vec, status)
+            res_vec, A, dofs, res_val = iteration(res_vec, A, dofs_start, False)
         rel_res_val = res_val / res_val_initial
         history.append(res_val)
         it += 1

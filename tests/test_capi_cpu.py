@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol(lib):
     from importlib import import_module
     capi = import_module("jax-cpfem_gb300._capi")
     assert names == set(capi.SIGNATURES), names ^ set(capi.SIGNATURES)
-    assert lib.cpfem_abi_version() == 2
+    assert lib.cpfem_abi_version() == 3
 
 
 def test_struct_layouts_match_the_library(lib):
