@@ -56,6 +56,18 @@ int make_matdev(const cpfem_material_t* m, MatDev* o) {
 // ------------------------------------------------------------------------------------
 // Constitutive pass: one thread per Gauss point.
 // ------------------------------------------------------------------------------------
+struct TanIn {
+  double F[9], G[9], H[9], W[9], Y[9];
+};
+
+// The FP64 consistent tangent where the FP32 one's scale test fails: out of line, so the
+// FP32-tangent kernel's hot code stays small.
+template <int NS, class StoreCol>
+__device__ __noinline__ void cp_tangent_f64_cold(const MatDev& m, Cub cc, TanIn in, GPSolve<NS> st, double idet,
+                                                 StoreCol store) {
+  cp_tangent<NS>(m, cc, in.F, in.G, st, in.H, in.W, in.Y, idet, store);
+}
+
 // TMODE: 0 no tangent, 1 FP64 tangent, 2 FP32 tangent (FP64 where the scale test fails)
 // stored in FP64, 3 the same stored in FP32 (tangent32)
 template <int NS, int TMODE>
@@ -213,24 +225,39 @@ __global__ void __launch_bounds__(128) k_gp_eval(const MatDev m, const cpfem_gp_
   if (TMODE != 0 && (a.tangent != nullptr || a.tangent32 != nullptr)) {
     const bool keep_dsdf = predict && st.rn <= m.local_tol;
     // columns arrive in the precision they were formed in; FP32 storage (tangent32)
-    // takes an FP32 column as it is
-    auto store = [&](int kl, const auto* col, const auto* dsdf) {
+    // takes an FP32 column as it is.  Everything captured by value: the store may be handed
+    // to an out-of-line function.
+    float* const tan32 = a.tangent32;
+    double* const tan64 = a.tangent;
+    double* const dsdf_out = a.s_dsdf;
+    auto store = [=](int kl, const auto* col, const auto* dsdf) {
       if constexpr (TMODE == 3) {
         const float w32 = f32_of(w);
 #pragma unroll
-        for (int c = 0; c < 9; ++c) a.tangent32[(int64_t)(9 * c + kl) * G + gp] = to_f32(col[c]) * w32;
+        for (int c = 0; c < 9; ++c) tan32[(int64_t)(9 * c + kl) * G + gp] = to_f32(col[c]) * w32;
       } else {
 #pragma unroll
-        for (int c = 0; c < 9; ++c) a.tangent[(int64_t)(9 * c + kl) * G + gp] = to_f64(col[c]) * w;
+        for (int c = 0; c < 9; ++c) tan64[(int64_t)(9 * c + kl) * G + gp] = to_f64(col[c]) * w;
       }
       if (keep_dsdf)
 #pragma unroll
-        for (int k = 0; k < 6; ++k) a.s_dsdf[(6 * kl + k) * G + gp] = to_f64(dsdf[k]);
+        for (int k = 0; k < 6; ++k) dsdf_out[(6 * kl + k) * G + gp] = to_f64(dsdf[k]);
     };
-    if (TMODE >= 2 && tangent_f32_ok<NS>(st, cc))
-      cp_tangent_t<NS, float>(m, cc, F, Gm, st, H, W, Y, idet, store);
-    else
+    if constexpr (TMODE >= 2) {
+      if (tangent_f32_ok<NS>(st, cc)) {
+        cp_tangent_t<NS, float>(m, cc, F, Gm, st, H, W, Y, idet, store);
+      } else {
+        // the FP64 tangent is the cold path here: out of line, inputs by value
+        TanIn in;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          in.F[k] = F[k]; in.G[k] = Gm[k]; in.H[k] = H[k]; in.W[k] = W[k]; in.Y[k] = Y[k];
+        }
+        cp_tangent_f64_cold<NS>(m, cc, in, st, idet, store);
+      }
+    } else {
       cp_tangent<NS>(m, cc, F, Gm, st, H, W, Y, idet, store);
+    }
   }
 }
 

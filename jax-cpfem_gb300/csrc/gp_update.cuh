@@ -186,6 +186,39 @@ CPFEM_HD void cp_jacobian_f32(const MatDev& m, const Cub& cc, const double* kk, 
   }
 }
 
+// The FP64 Newton direction of the local solve, ds = -J^-1 r (the reference's).
+template <int NS>
+CPFEM_HD void cp_direction_f64(const MatDev& m, const Cub& cc, const double* kk, const double* M, const double* r,
+                               double* ds) {
+  double J[36];
+  int perm[6];
+  double dinv[6];
+  cp_jacobian<NS>(m, cc, kk, M, J);
+  lu_factor<6>(J, perm, dinv);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) ds[k] = -r[k];
+  lu_solve<6>(J, perm, dinv, ds);
+}
+
+template <int NS>
+struct DirIn {
+  double kk[NS];
+  double M[9];
+  double r[6];
+};
+struct Vec6 {
+  double v[6];
+};
+
+#ifdef __CUDACC__
+template <int NS>
+__device__ __noinline__ Vec6 cp_direction_f64_cold(const MatDev& m, Cub cc, DirIn<NS> in) {
+  Vec6 o;
+  cp_direction_f64<NS>(m, cc, in.kk, in.M, in.r, o.v);
+  return o;
+}
+#endif
+
 constexpr int kWarmStartIters = 8;   // a warm start still unconverged after this restarts from 0
 
 // Local Newton with the cut-half line search of models_copper.py:218-245: trial
@@ -242,14 +275,25 @@ CPFEM_HD void cp_local_newton(const MatDev& m, const Cub& cc, const double* Ct, 
         }
       }
       if (!done) {
-        double J[36];
-        int perm[6];
-        double dinv[6];
-        cp_jacobian<NS>(m, cc, st.kk, st.M, J);
-        lu_factor<6>(J, perm, dinv);
+#ifdef __CUDA_ARCH__
+        if (j32) {
+          // the cold path of FP32 directions: out of line, so its code and registers stay
+          // out of the hot loop (inputs and result by value: no local array escapes)
+          DirIn<NS> in;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) ds[k] = -r[k];
-        lu_solve<6>(J, perm, dinv, ds);
+          for (int a = 0; a < NS; ++a) in.kk[a] = st.kk[a];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) in.M[k] = st.M[k];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) in.r[k] = r[k];
+          const Vec6 d = cp_direction_f64_cold<NS>(m, cc, in);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) ds[k] = d.v[k];
+        } else
+#endif
+        {
+          cp_direction_f64<NS>(m, cc, st.kk, st.M, r, ds);
+        }
       }
     }
     const double rn0 = sub_cap == 1 ? 0.0 : st.rn;
