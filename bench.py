@@ -758,7 +758,7 @@ def main():
                    "algorithmic_bytes_per_iteration": kb, "flops_per_iteration": kf,
                    "fp32_flops_per_iteration": kf32,
                    "limiter": ("grid barriers and load latency (29 grid barriers per iteration; ncu: barrier "
-                               "and long-scoreboard stalls dominate, FP64 pipe 14-26 %)" if args.precond == 3
+                               "and long-scoreboard stalls dominate, FP64 pipe 15-17 %)" if args.precond == 3
                                else "FP64 pipe (the SpMVs)"),
                    "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm if hbm else None},
                    "peak_source": "cpfem_probe_dfma FP64 (of measured); HBM from MEASURED_PEAKS.json (of measured)"}
@@ -774,6 +774,26 @@ def main():
                "local_iters_mean": its_t, "fp64_flops_per_gp": gp64, "fp32_flops_per_gp": gp32,
                "note": "FP64 flops counted with every local Newton direction (and, with the FP32 tangent, every "
                        "tangent) in FP32: a lower bound of the FP64 work"}
+    # the coloured scatter: algorithmic bytes of a tangent scatter (per GP the tangent, the
+    # shape gradients and P read once; per cell the read-add-write of its 64 3x3 blocks and
+    # 24 residual entries) and of a residual-only one, over the scatter region's time
+    asm_n, asm_ms = regions.get("elem_assemble", (0, 0.0))
+    n_tan = regions.get("gp_eval_tangent", (0, 0.0))[0]
+    n_res = regions.get("gp_eval_residual", (0, 0.0))[0]
+    E = prob.num_cells
+    tan_b = 4 if prob.fp32_tangent else 8
+    bytes_tan = G * (81 * tan_b + 24 * 8 + 9 * 8) + E * (64 * 9 * 8 * 2 + 24 * 8 * 2)
+    bytes_res = G * (24 * 8 + 9 * 8) + E * 24 * 8 * 2
+    asm_roof = None
+    if asm_ms > 0:
+        asm_gbs = (n_tan * bytes_tan + n_res * bytes_res) / (asm_ms * 1e-3) / 1e9
+        asm_roof = {"bound": "hbm", "achieved": asm_gbs, "peak": hbm, "unit": "GB/s",
+                    "frac": asm_gbs / hbm if hbm else None, "traffic": None,
+                    "kernel": "k_elem_assemble (coloured scatter, %s tangent)" % ("FP32" if prob.fp32_tangent else
+                                                                                "FP64"),
+                    "algorithmic_bytes_per_tangent_scatter": bytes_tan,
+                    "algorithmic_bytes_per_residual_scatter": bytes_res, "scatters": [n_tan, n_res],
+                    "peak_source": "HBM from MEASURED_PEAKS.json (of measured)"}
     shares = {"bicgstab": kr_ms / (t * 1e3), "gp_eval_tangent": gp_ms / (t * 1e3),
               "elem_assemble": regions.get("elem_assemble", (0, 0.0))[1] / (t * 1e3)}
     dominant = kr_roof if (kr_roof is not None and shares["bicgstab"] >= shares["gp_eval_tangent"]) else gp_roof
@@ -794,7 +814,8 @@ def main():
                           mg_refresh=args.mg_refresh if args.precond == 3 else None),
            "s_per_load_step": t / args.steps, "clocks": clocks, "e2e": e2e,
            "roofline": dominant,
-           "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof},
+           "roofline_kernels": {"bicgstab": kr_roof, "spmv": spmv_roof, "gp_eval": gp_roof,
+                                "elem_assemble": asm_roof},
            "region_shares": shares, "reference_choice_legs": legs, "tuned_linear_solver": tuned,
            "fp64_peak": {"value": fp64, "unit": "TFLOP/s", "probe": FP64_PROBE},
            "cpu_baseline": cpu,
