@@ -272,6 +272,7 @@ def _restore(p, snap):
     fe = p.fes[0]
     p.dt = snap[0]
     fe.bc_dofs, fe.bc_vals = snap[1], snap[2]
+    fe._bc_dofs_np = None      # the next upload of lists compares against nothing
     fe.bc_token += 1
 
 

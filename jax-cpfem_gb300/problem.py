@@ -109,8 +109,17 @@ class FiniteElement:
             dofs, vals = uniq, vals[::-1][first]
         else:
             dofs, vals = np.zeros(0, np.int64), np.zeros(0)
-        self.bc_dofs = torch.tensor(dofs, dtype=torch.int32, device=self.device)
-        self.bc_vals = torch.tensor(vals, dtype=torch.float64, device=self.device)
+        # a load-step loop changes only the values: the dofs stay on the device, and the
+        # values go up from pinned memory without waiting for the device (a copy from
+        # pageable memory would wait for all queued work)
+        prev = getattr(self, "_bc_dofs_np", None)
+        if prev is None or not np.array_equal(prev, dofs):
+            self.bc_dofs = torch.tensor(dofs, dtype=torch.int32, device=self.device)
+            self._bc_dofs_np = dofs
+        staged = torch.from_numpy(np.ascontiguousarray(vals, dtype=np.float64))
+        if self.device.type == "cuda":
+            staged = staged.pin_memory()
+        self.bc_vals = staged.to(self.device, non_blocking=True)
         self.bc_token = getattr(self, "bc_token", 0) + 1
 
 
@@ -754,6 +763,7 @@ class CrystalPlasticity:
         self.scatter(pw, dw, res, values)
         if trial:
             self._trial = (self._trial_key(u), u, trial, status)
+            self._trial_checked = False
         return res, values, status
 
     def new_trial(self):
@@ -879,7 +889,8 @@ class CrystalPlasticity:
             sig = torch.empty((self.num_cells, 3, 3), dtype=torch.float64, device=self.device)
             _capi.check(self.lib.cpfem_cell_average(self.num_cells, _dev_ptr(self.fes[0].JxW),
                                                     _dev_ptr(tr["stress"]), _dev_ptr(sig), _stream()))
-            self._check_status(status)
+            if not getattr(self, "_trial_checked", False):
+                self._check_status(status)   # (the Newton loop has read it already: no wait then)
             E = self.num_cells
             new = [tr["fpi_new"].t().reshape(E, 8, 3, 3), tr["g_new"].t().reshape(E, 8, N),
                    tr["slip_new"].t().reshape(E, 8, N)] + list(params[3:])

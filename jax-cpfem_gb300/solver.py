@@ -185,6 +185,9 @@ def _norm_checked(problem, x, status):
     both = torch.stack([out[0], status[0].to(torch.float64)]).cpu()
     resolve_deferred(problem)
     problem._check_status_bits(int(both[1]))
+    # the status read here is that of the pass whose trial outputs the problem keeps (or
+    # of a pass after it): the post-processing need not read it again
+    problem._trial_checked = True
     return math.sqrt(float(both[0]))
 
 
