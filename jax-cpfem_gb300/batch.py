@@ -165,6 +165,9 @@ class Batch:
         ``_solve_from``), from the extrapolated guess under the ``"linear"`` predictor; if
         that fails (an instance's extrapolation overshot into a state a local solve cannot
         reach), again from the last solution, the reference driver's guess."""
+        # as workloads.LoadStepper: under the extrapolated guess, local starts are predicted
+        # from the second Newton pass of a step on
+        self.problem.predict_from_pass = 1 if self.predictor == "linear" else 2
         if self.predictor == "linear" and self.prev is not None:
             try:
                 return self._solve_from(2.0 * self.sol - self.prev, **options)
@@ -264,6 +267,7 @@ def run_serial(instances, disps, dt, device=None, prepared=None, solver_options=
         sol = torch.zeros(p.num_total_dofs_all_vars, dtype=torch.float64, device=p.device)
         prev = None
         p.reset_local_start()
+        p.predict_from_pass = 1 if predictor == "linear" else 2
         for i, d in enumerate(disps):
             p.dt = float(dt)
             p.fes[0].set_dirichlet_lists(nodes, [0, 1, 2, 2], [0.0, 0.0, 0.0, float(d)])

@@ -220,6 +220,10 @@ class CrystalPlasticity:
         # ... moved to first order along F: s_warm + ds/dF (F - F_warm), with the ds/dF of the
         # last tangent pass (no effect on the result, fewer local iterations)
         self.predict_local = True
+        # ... from this tangent pass under a committed state on (0: the first): after a
+        # commit, a pass at the last solution sees the relaxed, near-elastic state, whose
+        # ds/dF would overshoot the flow stress on the next pass
+        self.predict_from_pass = 2
         # Newton directions of the local solve from an FP32 Jacobian while its scale allows
         # (same residual, stop test and tangent in FP64: same converged state)
         self.fp32_local_jacobian = True
@@ -655,10 +659,9 @@ class CrystalPlasticity:
         return w
 
     def _warm_args(self, tangent=False):
-        """GP-pass arguments of the local Newton's start: the warm start, and from the third
-        tangent pass under the same committed state on the linear prediction (the first
-        tangent pass after a commit sees the relaxed, near-elastic state, whose ds/dF would
-        overshoot the flow stress on the next pass)."""
+        """GP-pass arguments of the local Newton's start: the warm start, and from tangent
+        pass ``predict_from_pass`` (counted from 0) under the same committed state on the
+        linear prediction."""
         w = self._warm()
         if w is None:
             return {}
@@ -672,7 +675,7 @@ class CrystalPlasticity:
             token, count = getattr(self, "_tangent_passes", (None, 0))
             if token != self._state_token:
                 count = 0
-            out["predict"] = count >= 2
+            out["predict"] = count >= self.predict_from_pass
             if tangent:
                 self._tangent_passes = (self._state_token, count + 1)
         return out

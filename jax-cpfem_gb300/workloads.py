@@ -109,6 +109,10 @@ class LoadStepper:
         self.prob, self.solver, self.w = problem, solver_mod, workload
         self.options = dict(solver_options or {})
         self.predictor = predictor
+        if predictor == "linear":
+            # the first Newton pass of a step is at the extrapolated, plastic state: the
+            # ds/dF it forms already predicts the second pass's local starts well
+            problem.predict_from_pass = 1
         self.i = 0
         self.params = problem.internal_vars
         self.sol = torch.zeros(problem.num_total_dofs_all_vars, dtype=torch.float64, device=problem.device)
