@@ -48,7 +48,11 @@ class Workload:
         return 8 * self.mesh.cells.shape[0]
 
     def bc_lists(self, disp):
-        return roller_lists(self.mesh, disp)
+        # the node lists depend on the mesh only: found once, not at every load step
+        nodes = self.__dict__.get("_roller_nodes")
+        if nodes is None:
+            nodes = self.__dict__["_roller_nodes"] = roller_lists(self.mesh, 0.0)[0]
+        return list(nodes), [0, 1, 2, 2], [0.0, 0.0, 0.0, float(disp)]
 
     def bc_triples(self, disp):
         nodes, comps, vals = roller_lists(self.mesh, disp)
