@@ -213,7 +213,10 @@ class CrystalPlasticity:
         self.stats = {"gp_passes": 0, "krylov_iters": [], "local_iters_max": 0}
         self.timing = False
         self.timers = {}
-        self.sort_gps = True     # order each tangent pass by the previous pass's local-Newton counts
+        # order each tangent pass by the previous pass's local-Newton counts (off: with warm,
+        # predicted starts and FP32 directions the counts vary little, and GPs in their
+        # natural order keep the state loads coalesced and need no sort)
+        self.sort_gps = False
         # start each GP's local Newton from its last converged S instead of S = 0 (same root
         # to the same tolerance; S = 0 again whenever the warm start does not converge)
         self.warm_start_local = True
