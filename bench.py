@@ -353,6 +353,7 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": dict(workload_config(args.edge), precond="jacobi", initial_guess="last solution",
+                          linear_solver="BiCGSTAB tol=atol=1e-10",
                           newton=f"tol {NEWTON_REF['tol']:g} / rel_tol {NEWTON_REF['rel_tol']:g}"),
            "impl": "reference",
            "cpu_baseline": cb,
