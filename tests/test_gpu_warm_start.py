@@ -28,6 +28,7 @@ def _case(pkg, problem_mod, n=6, grains=4, strain=3e-3):
 
 
 def _pass(prob, u):
+    prob.timing = True          # the pass then records every GP's local iteration count
     res, values, status = prob.assemble(u)
     assert int(status.item()) == 0
     return res.clone(), values.clone(), prob._bufs["iters"].clone()
@@ -132,3 +133,18 @@ def test_fp32_local_newton_direction_converges_to_the_same_root(pkg, gpu):
     assert float((r32 - r64).abs().max() / r64.abs().max()) < 1e-10
     assert float((v32 - v64).abs().max() / v64.abs().max()) < 1e-9
     assert float(i32.double().mean()) <= float(i64.double().mean()) + 0.5, (i32.double().mean(), i64.double().mean())
+
+
+def test_ordered_pass_gives_the_same_outputs(pkg, gpu):
+    """The optional evaluation order (GPs heaviest first by their previous local-Newton
+    counts) changes which thread evaluates a GP, not its result: bitwise equal outputs."""
+    problem_mod, _ = gpu
+    _, _, _, _, prob, u = _case(pkg, problem_mod)
+    prob.warm_start_local = False
+    prob.sort_gps = False
+    r0, v0, i0 = _pass(prob, u)
+    prob.sort_gps = True
+    _pass(prob, u)                      # forms the order from this pass's counts
+    assert "gp_order" in prob._bufs
+    r1, v1, i1 = _pass(prob, u)         # evaluated in that order
+    assert torch.equal(r1, r0) and torch.equal(v1, v0) and torch.equal(i1, i0)
