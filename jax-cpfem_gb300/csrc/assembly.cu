@@ -274,8 +274,12 @@ __device__ __forceinline__ KT as_kt(float v);
 template <>
 __device__ __forceinline__ float as_kt<float>(float v) { return v; }
 
-template <bool WITH_K, bool ATOMIC, typename KT = double, typename TT = double>
-__global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t* __restrict__ clist,
+// SPLIT threads share a (cell, node a): thread h of them forms the blocks of neighbours
+// b = h*8/SPLIT .. (h+1)*8/SPLIT - 1 (each recomputes the node's 27 tangent contractions),
+// so a colour's launch has SPLIT times the threads; every block of the matrix is still
+// written by one thread, in the same order.
+template <bool WITH_K, bool ATOMIC, typename KT = double, typename TT = double, int SPLIT = 1>
+__global__ void __launch_bounds__(128, SPLIT == 2 ? (sizeof(KT) == 4 ? 4 : 2) : 1) k_elem_assemble(int32_t E, const int32_t* __restrict__ clist,
                                                        int32_t ncl, const int32_t* __restrict__ cells,
                                                        const double* __restrict__ sg,
                                                        const int64_t* __restrict__ goff,
@@ -284,28 +288,34 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
                                                        const TT* __restrict__ Dw,
                                                        double* __restrict__ res,
                                                        double* __restrict__ vals) {
+  static_assert(SPLIT == 1 || SPLIT == 2, "SPLIT must be 1 or 2");
+  constexpr int NB = 8 / SPLIT;   // neighbours b per thread
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t li = tid >> 3;
-  const int a = (int)(tid & 7);
+  const int h = (SPLIT == 2) ? (int)(tid & 1) : 0;
+  const int64_t tn = (SPLIT == 2) ? (tid >> 1) : tid;
+  const int64_t li = tn >> 3;
+  const int a = (int)(tn & 7);
   if (li >= ncl) return;
   const int64_t e = (clist != nullptr) ? clist[li] : li;
   const int64_t G = (int64_t)E * 8;
-  KT K[3][24];
+  const int b0 = h * NB;
+  KT K[3][3 * NB];
   double Rr[3] = {0.0, 0.0, 0.0};
   if (WITH_K) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int c = 0; c < 24; ++c) K[i][c] = KT(0);
+      for (int c = 0; c < 3 * NB; ++c) K[i][c] = KT(0);
   }
 #pragma unroll 1
   for (int q = 0; q < 8; ++q) {
     const int64_t gp = e * 8 + q;
     const double* sgq = sg + gp * 24;
     const double ga0 = sgq[3 * a], ga1 = sgq[3 * a + 1], ga2 = sgq[3 * a + 2];
+    if (h == 0)
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-      Rr[i] = fma(Pw[(3 * i) * G + gp], ga0, fma(Pw[(3 * i + 1) * G + gp], ga1, fma(Pw[(3 * i + 2) * G + gp], ga2, Rr[i])));
+      for (int i = 0; i < 3; ++i)
+        Rr[i] = fma(Pw[(3 * i) * G + gp], ga0, fma(Pw[(3 * i + 1) * G + gp], ga1, fma(Pw[(3 * i + 2) * G + gp], ga2, Rr[i])));
     if (WITH_K) {
       const KT a0 = as_kt<KT>(ga0), a1 = as_kt<KT>(ga1), a2 = as_kt<KT>(ga2);
       KT Gm[27];
@@ -317,20 +327,21 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
                            cp_fma(a1, as_kt<KT>(Dw[(int64_t)(9 * (3 * i + 1) + kL) * G + gp]),
                                   a2 * as_kt<KT>(Dw[(int64_t)(9 * (3 * i + 2) + kL) * G + gp])));
 #pragma unroll
-      for (int b = 0; b < 8; ++b) {
+      for (int bl = 0; bl < NB; ++bl) {
+        const int b = b0 + bl;
         const KT gb0 = as_kt<KT>(sgq[3 * b]), gb1 = as_kt<KT>(sgq[3 * b + 1]), gb2 = as_kt<KT>(sgq[3 * b + 2]);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int k = 0; k < 3; ++k)
-            K[i][3 * b + k] = cp_fma(Gm[9 * i + 3 * k], gb0, cp_fma(Gm[9 * i + 3 * k + 1], gb1,
-                              cp_fma(Gm[9 * i + 3 * k + 2], gb2, K[i][3 * b + k])));
+            K[i][3 * bl + k] = cp_fma(Gm[9 * i + 3 * k], gb0, cp_fma(Gm[9 * i + 3 * k + 1], gb1,
+                               cp_fma(Gm[9 * i + 3 * k + 2], gb2, K[i][3 * bl + k])));
       }
     }
   }
   const int64_t na = cells[e * 8 + a];
   // a conflict-free cell list (one colour) adds without atomics, in a fixed order
-  if (res != nullptr)
+  if (res != nullptr && h == 0)
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       if (ATOMIC) atomicAdd(&res[3 * na + i], Rr[i]);
@@ -340,15 +351,15 @@ __global__ void __launch_bounds__(128) k_elem_assemble(int32_t E, const int32_t*
     // sliced-ELL slot of (node na, neighbour b): 9*goff[g] + 32*(9*pos + 3i + k) + lane
     const int64_t base = 9 * goff[na >> 5] + (na & 31);
 #pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const int64_t pos = epos[e * 64 + 8 * a + b];
+    for (int bl = 0; bl < NB; ++bl) {
+      const int64_t pos = epos[e * 64 + 8 * a + b0 + bl];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           double* v = &vals[base + 32 * (9 * pos + 3 * i + k)];
-          if (ATOMIC) atomicAdd(v, to_f64(K[i][3 * b + k]));
-          else *v += to_f64(K[i][3 * b + k]);
+          if (ATOMIC) atomicAdd(v, to_f64(K[i][3 * bl + k]));
+          else *v += to_f64(K[i][3 * bl + k]);
         }
     }
   }
@@ -511,29 +522,31 @@ int cpfem_elem_assemble_ex(int32_t num_cells, const int32_t* cells, const double
   const int32_t ncl = (cell_list != nullptr) ? num_listed : num_cells;
   if (ncl == 0) return CPFEM_OK;
   const int threads = 128;
-  const unsigned blocks = (unsigned)ceil_div((int64_t)ncl * 8, threads);
   cudaStream_t s = (cudaStream_t)stream;
   const int64_t* goff = (values != nullptr) ? sell->group_off : nullptr;
   const double* t64 = static_cast<const double*>(tangent_w);
   const float* t32 = static_cast<const float*>(tangent_w);
-  // a colour's cell list adds without atomics (bitwise reproducible); no list: atomics
-  auto run = [&](auto kernel, auto tangent) {
+  // a colour's cell list adds without atomics (bitwise reproducible); no list: atomics.
+  // The stiffness variants give each (cell, node) two threads (one colour of a structured
+  // box is too few threads otherwise), the residual-only one a thread.
+  auto run = [&](auto kernel, auto tangent, int split) {
+    const unsigned blocks = (unsigned)ceil_div((int64_t)ncl * 8 * split, threads);
     kernel<<<blocks, threads, 0, s>>>(num_cells, cell_list, ncl, cells, shape_grads, goff, elem_pos, pk1_w,
                                       tangent, residual, values);
   };
   const bool listed = cell_list != nullptr;
   if (values == nullptr) {
-    if (listed) run(k_elem_assemble<false, false>, (const double*)nullptr);
-    else run(k_elem_assemble<false, true>, (const double*)nullptr);
+    if (listed) run(k_elem_assemble<false, false>, (const double*)nullptr, 1);
+    else run(k_elem_assemble<false, true>, (const double*)nullptr, 1);
   } else if (k_precision == 0) {
-    if (listed) run(k_elem_assemble<true, false>, t64);
-    else run(k_elem_assemble<true, true>, t64);
+    if (listed) run(k_elem_assemble<true, false, double, double, 2>, t64, 2);
+    else run(k_elem_assemble<true, true, double, double, 2>, t64, 2);
   } else if (k_precision == 1) {
-    if (listed) run(k_elem_assemble<true, false, float>, t64);
-    else run(k_elem_assemble<true, true, float>, t64);
+    if (listed) run(k_elem_assemble<true, false, float, double, 2>, t64, 2);
+    else run(k_elem_assemble<true, true, float, double, 2>, t64, 2);
   } else {
-    if (listed) run(k_elem_assemble<true, false, float, float>, t32);
-    else run(k_elem_assemble<true, true, float, float>, t32);
+    if (listed) run(k_elem_assemble<true, false, float, float, 2>, t32, 2);
+    else run(k_elem_assemble<true, true, float, float, 2>, t32, 2);
   }
   CPFEM_CUDA_TRY(cudaGetLastError());
   return CPFEM_OK;
