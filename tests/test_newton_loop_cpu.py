@@ -1,0 +1,184 @@
+"""The global Newton loop's control flow (``crystal_plasticity_OR_design/solver.py:310-437``)
+and the checks of deferred Krylov solves, on the CPU: the device passes are replaced by a
+diagonal stand-in system f(u) = u^3 + u - c, so the loop's decisions (stop rule, the
+residual-only last pass, the redo of an iteration whose deferred solve fails its check,
+the iteration limit) run as they do on the GPU."""
+import ctypes
+import importlib
+import math
+
+import pytest
+import torch
+
+
+@pytest.fixture(scope="module")
+def solver_mod(pkg):
+    return importlib.import_module("jax-cpfem_gb300.solver")
+
+
+@pytest.fixture(scope="module")
+def capi(pkg):
+    return importlib.import_module("jax-cpfem_gb300._capi")
+
+
+C = torch.tensor([2.0, 10.0, -3.0], dtype=torch.float64)
+
+
+class StandIn:
+    """What the Newton loop reads of a problem, with counters of the passes it asks for."""
+
+    def __init__(self, fail_solves=()):
+        self.num_total_dofs_all_vars = 3
+        self.num_nodes = 1
+        self.device = torch.device("cpu")
+        self.stats = {"krylov_iters": []}
+        self._pending_solve = None
+        self.fail_solves = set(fail_solves)
+        self.solves = []          # the deferred flag of every linear solve
+        self.tangent_passes = 0
+        self.residual_passes = 0
+
+    def unflatten_fn_sol_list(self, dofs):
+        return [dofs.reshape(self.num_nodes, 3)]
+
+
+def _f(u):
+    return u ** 3 + u - C
+
+
+@pytest.fixture
+def stand_in(solver_mod, monkeypatch):
+    def update(problem, dofs):
+        problem.tangent_passes += 1
+        return _f(dofs), 3.0 * dofs ** 2 + 1.0, None
+
+    def residual(problem, dofs):
+        problem.residual_passes += 1
+        return _f(dofs), None
+
+    def norm_checked(problem, x, status):
+        # the deferred solve's report is read with the next norm, as on the device
+        if problem._pending_solve == "fail":
+            problem._pending_solve = None
+            raise solver_mod.DeferredSolveFailed("planted")
+        problem._pending_solve = None
+        return float(torch.linalg.norm(x))
+
+    def incremental(problem, res_vec, A, dofs, solver_options, deferred=False):
+        problem.solves.append(deferred)
+        if deferred and len(problem.solves) in problem.fail_solves:
+            problem._pending_solve = "fail"
+            return dofs + 100.0          # what a failed solve leaves must not survive
+        return dofs - res_vec / A
+
+    monkeypatch.setattr(solver_mod, "_update_deferred", update)
+    monkeypatch.setattr(solver_mod, "_residual_deferred", residual)
+    monkeypatch.setattr(solver_mod, "_norm_checked", norm_checked)
+    monkeypatch.setattr(solver_mod, "linear_incremental_solver", incremental)
+    return solver_mod
+
+
+def _reference_newton(tol, rel_tol):
+    """The reference loop written out: iterate while both stop tests fail."""
+    u = torch.zeros(3, dtype=torch.float64)
+    r0 = float(torch.linalg.norm(_f(u)))
+    r, it = r0, 0
+    while r / r0 > rel_tol and r > tol:
+        u = u - _f(u) / (3.0 * u ** 2 + 1.0)
+        r = float(torch.linalg.norm(_f(u)))
+        it += 1
+    return u, it
+
+
+def test_loop_matches_the_reference_iteration(stand_in):
+    prob = StandIn()
+    sol = stand_in.solver(prob, {"tol": 1e-10, "rel_tol": 1e-14})[0].reshape(-1)
+    u, it = _reference_newton(1e-10, 1e-14)
+    assert torch.equal(sol, u)
+    assert prob.stats["newton_iters"] == it
+    assert all(prob.solves)                               # every solve deferred
+    # the last iterate, predicted converged, gets a residual-only pass
+    assert prob.stats.get("final_tangent_skipped", 0) == 1 and prob.residual_passes == 1
+    assert prob.tangent_passes == it                      # the first system and every iterate but the last
+    assert prob.stats["res_history"][-1] < 1e-10
+
+
+def test_failed_deferred_solve_redoes_the_iteration(stand_in):
+    clean = StandIn()
+    ref = stand_in.solver(clean, {"tol": 1e-10, "rel_tol": 1e-14})[0]
+    prob = StandIn(fail_solves={2})
+    sol = stand_in.solver(prob, {"tol": 1e-10, "rel_tol": 1e-14})[0]
+    assert torch.equal(sol, ref)                          # the failed increment left no trace
+    assert prob.stats["deferred_redone"] == 1
+    assert prob.stats["newton_iters"] == clean.stats["newton_iters"]
+    assert prob.solves[1] is True and prob.solves[2] is False   # the redo is a checked solve
+
+
+def test_iteration_limit(stand_in):
+    with pytest.raises(RuntimeError, match="did not converge"):
+        stand_in.solver(StandIn(), {"tol": 1e-30, "rel_tol": 1e-30, "max_newton": 3})
+
+
+def test_defers_only_the_plain_device_solve(solver_mod):
+    class P:
+        pass
+
+    p = P()
+    assert solver_mod._defers(p, {})
+    assert solver_mod._defers(p, {"jax_solver": {}})
+    assert not solver_mod._defers(p, {"jax_solver": {}, "line_search_flag": True})
+    assert not solver_mod._defers(p, {"custom_solver": lambda *a: None})
+    p.defer_krylov_checks = False
+    assert not solver_mod._defers(p, {})
+
+
+def _report(capi, monkeypatch, solver_mod, **fields):
+    buf = torch.zeros(ctypes.sizeof(capi.SolveReport), dtype=torch.uint8)
+    r = capi.SolveReport.from_address(buf.data_ptr())
+    for k, v in dict(k=7, error=0, rs=1e-22, atol2=1e-20, true_rs=1e-22, bb=1.0).items():
+        setattr(r, k, fields.get(k, v))
+    monkeypatch.setattr(solver_mod, "_report_buffer", lambda problem: buf)
+
+
+def _pending(fp32):
+    class P:
+        pass
+
+    p = P()
+    p.stats = {"krylov_iters": []}
+    p._pending_solve = {"fp32": fp32, "tol": 1e-4, "atol": 1e-10}
+    return p
+
+
+def test_resolve_deferred_accepts_a_converged_report(solver_mod, capi, monkeypatch):
+    _report(capi, monkeypatch, solver_mod)
+    p = _pending(True)
+    solver_mod.resolve_deferred(p)
+    assert p.stats["krylov_iters"] == [7] and p._pending_solve is None
+    solver_mod.resolve_deferred(p)                        # nothing pending: no second count
+    assert p.stats["krylov_iters"] == [7]
+
+
+@pytest.mark.parametrize("fields, fp32, fallback", [
+    ({"error": 1}, False, False),                         # a grid barrier timed out
+    ({"true_rs": 0.04}, False, False),                    # ||b - Ax|| = 0.2 fails jax_solve's 0.1
+    ({"true_rs": -1.0}, False, False),                    # no true residual (NaN)
+    ({"rs": 1e-18}, True, True),                          # FP32 V-cycle: not converged
+    ({"true_rs": 1e-4}, True, True),                      # FP32 V-cycle: true residual off the stop rule
+])
+def test_resolve_deferred_rejects(solver_mod, capi, monkeypatch, fields, fp32, fallback):
+    _report(capi, monkeypatch, solver_mod, **fields)
+    p = _pending(fp32)
+    with pytest.raises(solver_mod.DeferredSolveFailed):
+        solver_mod.resolve_deferred(p)
+    assert p._pending_solve is None and p.stats["krylov_iters"] == []
+    assert getattr(p, "mg_fp64_only", False) == fallback
+
+
+def test_fp32_stop_rule(solver_mod):
+    ok = solver_mod._fp32_solve_ok
+    assert ok(True, 1e-5, 1.0, 1e-4, 1e-10)                # within the factor 10 of tol*||b||
+    assert not ok(True, 2e-3, 1.0, 1e-4, 1e-10)
+    assert not ok(False, 1e-9, 1.0, 1e-4, 1e-10)
+    assert not ok(True, math.nan, 1.0, 1e-4, 1e-10)
+    assert ok(True, 5e-10, 0.0, 1e-4, 1e-10)               # b = 0: the absolute limit
