@@ -2,7 +2,7 @@
 and the checks of deferred Krylov solves, on the CPU: the device passes are replaced by a
 diagonal stand-in system f(u) = u^3 + u - c, so the loop's decisions (stop rule, the
 residual-only last pass, the redo of an iteration whose deferred solve fails its check,
-the iteration limit) run as they do on the GPU."""
+the iteration limit, the load step's predictor fallback) run as they do on the GPU."""
 import ctypes
 import importlib
 import math
@@ -182,3 +182,33 @@ def test_fp32_stop_rule(solver_mod):
     assert not ok(False, 1e-9, 1.0, 1e-4, 1e-10)
     assert not ok(True, math.nan, 1.0, 1e-4, 1e-10)
     assert ok(True, 5e-10, 0.0, 1e-4, 1e-10)               # b = 0: the absolute limit
+
+
+def test_predictor_fallback(pkg):
+    """A load step whose solve fails from the extrapolated guess is solved again from the
+    last solution; a failure from the last solution itself is raised."""
+    workloads = importlib.import_module("jax-cpfem_gb300.workloads")
+
+    class Solver:
+        def __init__(self, bad):
+            self.bad, self.starts = bad, []
+
+        def solver(self, problem, opts):
+            g = opts["initial_guess"][0]
+            self.starts.append(g)
+            if any(g.data_ptr() == b.data_ptr() for b in self.bad):
+                raise RuntimeError("global Newton did not converge")
+            return [g + 1.0]
+
+    last = torch.zeros(2, 3, dtype=torch.float64)
+    guess = torch.ones(2, 3, dtype=torch.float64)
+    prob = StandIn()
+    s = Solver(bad=[guess])
+    out = workloads.solve_with_fallback(s, prob, {"tol": 1e-8}, guess, last)
+    assert torch.equal(out, last + 1.0) and prob.stats["predictor_fallbacks"] == 1
+    assert len(s.starts) == 2 and s.starts[1].data_ptr() == last.data_ptr()
+    prob = StandIn()
+    out = workloads.solve_with_fallback(Solver(bad=[]), prob, {}, guess, last)
+    assert torch.equal(out, guess + 1.0) and "predictor_fallbacks" not in prob.stats
+    with pytest.raises(RuntimeError):
+        workloads.solve_with_fallback(Solver(bad=[last]), StandIn(), {}, last, last)
