@@ -644,6 +644,7 @@ def main():
 
     prob.timing = True
     prob.stats["krylov_iters"] = []
+    prob.stats["solves_dropped"] = 0
     passes0 = prob.stats["gp_passes"]
     newton = []
     # the state at the start of the timed steps: the end-to-end run repeats the same load
@@ -673,6 +674,7 @@ def main():
     regions = prob.timer_ms()
     prob.timing = False
     krylov = list(prob.stats["krylov_iters"])
+    dropped = int(prob.stats.get("solves_dropped", 0))
     passes = prob.stats["gp_passes"] - passes0
     G = prob.num_gp
     value = world * G * args.steps / t
@@ -829,7 +831,7 @@ def main():
            "cpu_baseline": cpu,
            "regions_ms": {k: {"launches": v[0], "ms": v[1]} for k, v in regions.items()},
            "newton_iters_per_step": newton, "krylov_iters": krylov, "gp_passes": passes,
-           "gpu_launches": None}
+           "solves_dropped": dropped, "gpu_launches": None}
     out["gpu_launches"] = counter.launches
     if rank == 0 and world == 1 and args.config == "c1" and not args.no_sub_records:
         # the differentiation form on the same RVE, after the timed region, and the 10^3

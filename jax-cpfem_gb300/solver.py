@@ -42,12 +42,15 @@ class DeferredSolveFailed(Exception):
     solve."""
 
 
-def _report_buffer(problem):
-    """The problem's pinned host copy of a deferred solve's report."""
-    buf = getattr(problem, "_report_host", None)
-    if buf is None:
-        buf = problem._report_host = torch.zeros(ctypes.sizeof(_capi.SolveReport), dtype=torch.uint8).pin_memory()
-    return buf
+def _report_buffer(problem, slot=0):
+    """The problem's pinned host copies of deferred solves' reports: two slots, used in turn,
+    so a solve queued behind a residual norm cannot overwrite the report of the solve that
+    norm checks before the host has read it."""
+    bufs = getattr(problem, "_report_host", None)
+    if bufs is None:
+        n = ctypes.sizeof(_capi.SolveReport)
+        bufs = problem._report_host = [torch.zeros(n, dtype=torch.uint8).pin_memory() for _ in range(2)]
+    return bufs[slot]
 
 
 def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, maxiter=10000, restarts=0,
@@ -72,7 +75,8 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
     opts = _capi.KrylovOpts(int(precond), 1 if A.transposed else 0, int(maxiter), int(restarts),
                             float(tol), float(atol), None, int(grid_blocks), 1 | (2 if deferred else 0))
     if deferred:
-        opts.report = _report_buffer(problem).data_ptr()
+        slot = problem._report_slot = 1 - getattr(problem, "_report_slot", 1)
+        opts.report = _report_buffer(problem, slot).data_ptr()
     mg_options = dict(mg_options or {})
     if int(precond) == 3:
         if getattr(problem, "mg_fp64_only", False):
@@ -85,7 +89,7 @@ def bicgstab(problem, A: DeviceCSR, b, x0, precond=1, tol=1e-10, atol=1e-10, max
                                           ctypes.byref(opts), _dev_ptr(ws), info.ctypes.data, _stream()))
     if deferred:
         problem._pending_solve = {"fp32": int(precond) == 3 and opts.mg.contents.precision == 1,
-                                  "tol": float(tol), "atol": float(atol)}
+                                  "tol": float(tol), "atol": float(atol), "slot": slot}
         return x, None, None
     k, ok = int(info[0]), bool(info[1])
     st = np.zeros(9)
@@ -119,7 +123,7 @@ def resolve_deferred(problem):
     if p is None:
         return
     problem._pending_solve = None
-    r = _capi.SolveReport.from_address(_report_buffer(problem).data_ptr())
+    r = _capi.SolveReport.from_address(_report_buffer(problem, p.get("slot", 0)).data_ptr())
     rn = math.sqrt(r.true_rs) if r.true_rs >= 0.0 else float("nan")
     if r.error:
         raise DeferredSolveFailed("a grid barrier of the solve timed out")
@@ -174,21 +178,59 @@ def linear_solver(problem, A, b, x0, solver_options, deferred=False):
                               "UMFPACK/PETSc host solvers are not part of the device path")
 
 
-def _norm_checked(problem, x, status):
-    """||x|| and the status word of the constitutive pass that produced x, read in one
-    device-to-host transfer; checks a deferred solve's report first (the pass ran at the
-    iterate that solve produced), then raises on a failed local solve as the pass's own
-    check would."""
-    ws = problem._buf("dot_ws", (int(problem.lib.cpfem_dot_workspace_bytes(x.numel())) // 8 + 64,))
-    out = problem._buf("dot_out", (1,))
-    _capi.check(problem.lib.cpfem_dot(x.numel(), _dev_ptr(x), _dev_ptr(x), _dev_ptr(out), _dev_ptr(ws), _stream()))
-    both = torch.stack([out[0], status[0].to(torch.float64)]).cpu()
-    resolve_deferred(problem)
-    problem._check_status_bits(int(both[1]))
+class _NormCopy:
+    """||x||^2 and the status word of the pass that produced x, on their way to the
+    problem's pinned host buffer behind the work queued so far, with an event after the
+    copy: the host may queue more work before ``wait`` reads them.  One copy per problem is
+    in flight at a time (each is waited for before the next is queued)."""
+
+    def __init__(self, problem, x, status):
+        ws = problem._buf("dot_ws", (int(problem.lib.cpfem_dot_workspace_bytes(x.numel())) // 8 + 64,))
+        out = problem._buf("dot_out", (1,))
+        _capi.check(problem.lib.cpfem_dot(x.numel(), _dev_ptr(x), _dev_ptr(x), _dev_ptr(out), _dev_ptr(ws),
+                                          _stream()))
+        host = getattr(problem, "_norm_host", None)
+        if host is None:
+            host = problem._norm_host = torch.zeros(2, dtype=torch.float64).pin_memory()
+            problem._norm_event = torch.cuda.Event()
+        host.copy_(torch.stack([out[0], status[0].to(torch.float64)]), non_blocking=True)
+        problem._norm_event.record()
+        self.host, self.event = host, problem._norm_event
+
+    def wait(self):
+        self.event.synchronize()
+        return float(self.host[0]), int(self.host[1])
+
+
+def _norm_queue(problem, x, status):
+    """The first half of ``_norm_checked``: queue the norm and status copy; the ticket also
+    names the deferred solve whose report that copy follows."""
+    return problem._pending_solve, _NormCopy(problem, x, status)
+
+
+def _norm_wait(problem, ticket):
+    """The second half: wait for the copy, check the deferred solve it follows (the pass ran
+    at the iterate that solve produced), then raise on a failed local solve as the pass's
+    own check would.  A solve queued after the copy stays pending."""
+    pending, copy = ticket
+    sq, status_word = copy.wait()
+    later = problem._pending_solve if problem._pending_solve is not pending else None
+    problem._pending_solve = pending
+    try:
+        resolve_deferred(problem)
+    finally:
+        problem._pending_solve = later
+    problem._check_status_bits(status_word)
     # the status read here is that of the pass whose trial outputs the problem keeps (or
     # of a pass after it): the post-processing need not read it again
     problem._trial_checked = True
-    return math.sqrt(float(both[0]))
+    return math.sqrt(sq)
+
+
+def _norm_checked(problem, x, status):
+    """||x|| and the status word of the constitutive pass that produced x, read in one
+    device-to-host transfer; checks a deferred solve's report first, then the pass's status."""
+    return _norm_wait(problem, _norm_queue(problem, x, status))
 
 
 def _update_deferred(problem, dofs):
@@ -285,6 +327,15 @@ def _defers(problem, solver_options):
     return not keys or keys == {"jax_solver"}
 
 
+def _continues(history, limit):
+    """Whether the Newton loop will almost surely go on after the iterate being formed: the
+    quadratic model (``_expect_converged``) puts its residual above twice the stop limit, or
+    there is no contraction rate yet."""
+    if len(history) < 2 or not (history[-2] > 0.0 and history[-1] < history[-2]):
+        return True
+    return history[-1] ** 3 / history[-2] ** 2 > 2.0 * limit
+
+
 def solver(problem, solver_options=None):
     """Row-elimination Newton solve; returns ``[sol (num_nodes, 3)]``.
 
@@ -292,7 +343,12 @@ def solver(problem, solver_options=None):
     next constitutive pass without waiting for the solve, and the solve's report is checked
     together with that pass's residual norm; an iteration whose solve fails the check is
     redone from its start with a checked solve, so the iterates and the result are those of
-    the checked loop."""
+    the checked loop.  Where the loop will almost surely go on (``_continues``), the next
+    iteration's solve is queued behind the residual norm's copy, before the host waits for
+    it, so the device does not idle while the host reads the norm and decides
+    (``problem.queue_next_solve = False`` turns this off); a solve so queued whose iteration
+    never comes (the residual was below the limit after all) is dropped
+    (``stats["solves_dropped"]``)."""
     solver_options = {} if solver_options is None else solver_options
     start = time.time()
     problem._pending_solve = None
@@ -304,9 +360,19 @@ def solver(problem, solver_options=None):
     tol = solver_options.get("tol", 1e-6)
     max_newton = solver_options.get("max_newton", 100)
     defer = _defers(problem, solver_options)
+    ahead = defer and getattr(problem, "queue_next_solve", True)
 
-    res_vec, A, status = _update_deferred(problem, dofs)
-    res_val = _norm_checked(problem, res_vec, status)
+    def tangent_pass(dofs, deferred, go_on):
+        """The iterate's residual and tangent, and its norm read; with ``go_on`` the next
+        iteration's solve is queued before the read (returned, else None)."""
+        res_vec, A, status = _update_deferred(problem, dofs)
+        if not (ahead and deferred and go_on):
+            return res_vec, A, _norm_checked(problem, res_vec, status), None
+        ticket = _norm_queue(problem, res_vec, status)
+        queued = linear_incremental_solver(problem, res_vec, A, dofs, solver_options, deferred=True)
+        return res_vec, A, _norm_wait(problem, ticket), queued
+
+    res_vec, A, res_val, queued = tangent_pass(dofs, defer, True)
     res_val_initial = res_val
     rel_res_val = res_val / res_val_initial if res_val_initial > 0 else float("nan")
     history = [res_val]
@@ -314,9 +380,13 @@ def solver(problem, solver_options=None):
     limit = max(tol, rel_tol * res_val_initial)
     skip = getattr(problem, "skip_final_tangent", True)
 
-    def iteration(res_vec, A, dofs, deferred):
-        dofs = linear_incremental_solver(problem, res_vec, A, dofs, solver_options, deferred=deferred)
+    def iteration(res_vec, A, dofs, deferred, queued):
+        if queued is not None:
+            dofs = queued    # this iteration's solve, queued behind the last norm
+        else:
+            dofs = linear_incremental_solver(problem, res_vec, A, dofs, solver_options, deferred=deferred)
         res_vec = None
+        go_on = _continues(history, limit)
         if skip and _expect_converged(history, limit):
             # the last iterate needs no tangent: residual (and trial state) only, and the
             # tangent pass after all if the residual is not below the limit yet (its local
@@ -325,31 +395,34 @@ def solver(problem, solver_options=None):
             res_val = _norm_checked(problem, res_vec, status)
             if (res_val / res_val_initial > rel_tol) and (res_val > tol):
                 problem.stats["final_tangent_mispredicted"] = problem.stats.get("final_tangent_mispredicted", 0) + 1
-                res_vec = None
+                res_vec, go_on = None, True
             else:
                 problem.stats["final_tangent_skipped"] = problem.stats.get("final_tangent_skipped", 0) + 1
+        queued = None
         if res_vec is None:
-            res_vec, A, status = _update_deferred(problem, dofs)
-            res_val = _norm_checked(problem, res_vec, status)
-        return res_vec, A, dofs, res_val
+            res_vec, A, res_val, queued = tangent_pass(dofs, deferred, go_on)
+        return res_vec, A, dofs, res_val, queued
 
     while (rel_res_val > rel_tol) and (res_val > tol):
         if it >= max_newton:
             raise RuntimeError(f"global Newton did not converge in {max_newton} iterations (res = {res_val})")
         try:
-            res_vec, A, dofs, res_val = iteration(res_vec, A, dofs, defer)
+            res_vec, A, dofs, res_val, queued = iteration(res_vec, A, dofs, defer, queued)
         except DeferredSolveFailed:
             # redo the iteration from its start with a checked solve: the system at the
-            # iteration's start is formed again (its buffers now hold the failed iterate's)
+            # iteration's start is formed again (its buffers now hold the failed iterate's);
+            # a solve queued behind the failed check is dropped with it
             problem.stats["deferred_redone"] = problem.stats.get("deferred_redone", 0) + 1
             problem._pending_solve = None
             dofs_start = dofs
-            res_vec, A, status = _update_deferred(problem, dofs_start)
-            _norm_checked(problem, res_vec, status)
-            res_vec, A, dofs, res_val = iteration(res_vec, A, dofs_start, False)
+            res_vec, A, _, _ = tangent_pass(dofs_start, False, False)
+            res_vec, A, dofs, res_val, queued = iteration(res_vec, A, dofs_start, False, None)
         rel_res_val = res_val / res_val_initial
         history.append(res_val)
         it += 1
+    if queued is not None:
+        problem.stats["solves_dropped"] = problem.stats.get("solves_dropped", 0) + 1
+    problem._pending_solve = None
     if not math.isfinite(res_val):
         raise FloatingPointError("res_val contains NaN, stop the program!")
     problem.stats["newton_iters"] = it

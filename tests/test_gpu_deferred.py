@@ -1,6 +1,7 @@
 """The Newton loop's deferred Krylov checks: each iteration's BiCGSTAB report is read with
-the next residual norm, and an iteration whose solve fails the check is redone with a
-checked solve.  The deferred loop must give the checked loop's iterates exactly."""
+the next residual norm (and the next solve may be queued before that read), and an
+iteration whose solve fails the check is redone with a checked solve.  The deferred loop
+must give the checked loop's iterates exactly."""
 import importlib
 import os
 
@@ -24,22 +25,24 @@ def _history(stepper, steps):
 
 
 def test_deferred_checks_give_the_checked_iterates(pkg, gpu):
-    """The benchmark path on the 10^3 copper crystal, 4 load steps, deferred and checked:
-    bitwise the same stresses and solutions, the same Newton and Krylov counts."""
+    """The benchmark path on the 10^3 copper crystal, 4 load steps: deferred with the next
+    solve queued ahead of each norm read, deferred without it, and checked -- bitwise the
+    same stresses and solutions, the same Newton and Krylov counts."""
     problem_mod, solver_mod = gpu
     W = importlib.import_module("jax-cpfem_gb300.workloads")
     out = []
-    for defer in (True, False):
+    for defer, ahead in ((True, True), (True, False), (False, False)):
         w = W.copper_single_crystal()
         prob = problem_mod.CrystalPlasticity(w.mesh, additional_info=(w.quat, w.ori), material=w.spec)
         prob.defer_krylov_checks = defer
+        prob.queue_next_solve = ahead
         st = W.bench_stepper(prob, solver_mod, w)
         sig, sols = _history(st, 4)
         out.append((sig, sols, list(prob.stats["krylov_iters"]), prob.stats.get("deferred_redone", 0)))
-    (s1, u1, k1, r1), (s2, u2, k2, r2) = out
-    assert r1 == 0 and r2 == 0
-    assert k1 == k2
-    assert np.array_equal(s1, s2) and np.array_equal(u1, u2)
+    s0, u0, k0, _ = out[0]
+    for s, u, k, r in out:
+        assert r == 0 and k == k0
+        assert np.array_equal(s, s0) and np.array_equal(u, u0)
 
 
 def test_deferred_fp32_failure_is_redone(pkg, gpu):
@@ -50,7 +53,7 @@ def test_deferred_fp32_failure_is_redone(pkg, gpu):
     problem_mod, solver_mod = gpu
     L = 0.0295
     out = []
-    for defer in (True, False):
+    for defer in (True, False):   # deferred (with the next solve queued ahead) and checked
         mesh = pkg.box_mesh(20, 20, 20, L, L, L)
         prob = gpu_problem(pkg, problem_mod, pkg.material.CALIB_CASE4, mesh, GOLD["case4_quat"],
                            GOLD["case4_grain"].astype(np.int64))

@@ -1,8 +1,9 @@
 """The global Newton loop's control flow (``crystal_plasticity_OR_design/solver.py:310-437``)
 and the checks of deferred Krylov solves, on the CPU: the device passes are replaced by a
 diagonal stand-in system f(u) = u^3 + u - c, so the loop's decisions (stop rule, the
-residual-only last pass, the redo of an iteration whose deferred solve fails its check,
-the iteration limit, the load step's predictor fallback) run as they do on the GPU."""
+residual-only last pass, the next solve queued ahead of the norm read, the redo of an
+iteration whose deferred solve fails its check, the iteration limit, the load step's
+predictor fallback) run as they do on the GPU."""
 import ctypes
 import importlib
 import math
@@ -25,21 +26,24 @@ C = torch.tensor([2.0, 10.0, -3.0], dtype=torch.float64)
 
 
 class StandIn:
-    """What the Newton loop reads of a problem, with counters of the passes it asks for."""
+    """What the Newton loop reads of a problem, with a log of the passes it asks for."""
 
-    def __init__(self, fail_solves=()):
+    def __init__(self, fail_solves=(), queue_next_solve=True):
         self.num_total_dofs_all_vars = 3
         self.num_nodes = 1
         self.device = torch.device("cpu")
         self.stats = {"krylov_iters": []}
         self._pending_solve = None
+        self.queue_next_solve = queue_next_solve
         self.fail_solves = set(fail_solves)
         self.solves = []          # the deferred flag of every linear solve
-        self.tangent_passes = 0
-        self.residual_passes = 0
+        self.log = []             # "tangent", "residual", "solve", "wait" in the order asked for
 
     def unflatten_fn_sol_list(self, dofs):
         return [dofs.reshape(self.num_nodes, 3)]
+
+    def _check_status_bits(self, word):
+        assert word == 0
 
 
 def _f(u):
@@ -49,31 +53,47 @@ def _f(u):
 @pytest.fixture
 def stand_in(solver_mod, monkeypatch):
     def update(problem, dofs):
-        problem.tangent_passes += 1
+        problem.log.append("tangent")
         return _f(dofs), 3.0 * dofs ** 2 + 1.0, None
 
     def residual(problem, dofs):
-        problem.residual_passes += 1
+        problem.log.append("residual")
         return _f(dofs), None
 
-    def norm_checked(problem, x, status):
-        # the deferred solve's report is read with the next norm, as on the device
-        if problem._pending_solve == "fail":
-            problem._pending_solve = None
-            raise solver_mod.DeferredSolveFailed("planted")
+    class NormCopy:
+        """The norm's copy to the host; the value is ready at once on the CPU."""
+
+        def __init__(self, problem, x, status):
+            self.problem, self.sq = problem, float(x @ x)
+
+        def wait(self):
+            self.problem.log.append("wait")
+            return self.sq, 0
+
+    def resolve(problem):
+        # the report of the deferred solve this norm follows
+        p = problem._pending_solve
+        if p is None:
+            return
         problem._pending_solve = None
-        return float(torch.linalg.norm(x))
+        if p["fail"]:
+            raise solver_mod.DeferredSolveFailed("planted")
+        problem.stats["krylov_iters"].append(p["n"])
 
     def incremental(problem, res_vec, A, dofs, solver_options, deferred=False):
         problem.solves.append(deferred)
-        if deferred and len(problem.solves) in problem.fail_solves:
-            problem._pending_solve = "fail"
-            return dofs + 100.0          # what a failed solve leaves must not survive
+        problem.log.append("solve")
+        n = len(problem.solves)
+        if deferred:
+            problem._pending_solve = {"fail": n in problem.fail_solves, "n": n}
+            if n in problem.fail_solves:
+                return dofs + 100.0      # what a failed solve leaves must not survive
         return dofs - res_vec / A
 
     monkeypatch.setattr(solver_mod, "_update_deferred", update)
     monkeypatch.setattr(solver_mod, "_residual_deferred", residual)
-    monkeypatch.setattr(solver_mod, "_norm_checked", norm_checked)
+    monkeypatch.setattr(solver_mod, "_NormCopy", NormCopy)
+    monkeypatch.setattr(solver_mod, "resolve_deferred", resolve)
     monkeypatch.setattr(solver_mod, "linear_incremental_solver", incremental)
     return solver_mod
 
@@ -90,28 +110,51 @@ def _reference_newton(tol, rel_tol):
     return u, it
 
 
-def test_loop_matches_the_reference_iteration(stand_in):
-    prob = StandIn()
+@pytest.mark.parametrize("ahead", [True, False])
+def test_loop_matches_the_reference_iteration(stand_in, ahead):
+    prob = StandIn(queue_next_solve=ahead)
     sol = stand_in.solver(prob, {"tol": 1e-10, "rel_tol": 1e-14})[0].reshape(-1)
     u, it = _reference_newton(1e-10, 1e-14)
     assert torch.equal(sol, u)
     assert prob.stats["newton_iters"] == it
-    assert all(prob.solves)                               # every solve deferred
+    assert all(prob.solves) and len(prob.solves) == it   # every solve deferred, none dropped
+    assert prob.stats["krylov_iters"] == list(range(1, it + 1))   # every report read, in order
     # the last iterate, predicted converged, gets a residual-only pass
-    assert prob.stats.get("final_tangent_skipped", 0) == 1 and prob.residual_passes == 1
-    assert prob.tangent_passes == it                      # the first system and every iterate but the last
+    assert prob.stats.get("final_tangent_skipped", 0) == 1 and prob.log.count("residual") == 1
+    assert prob.log.count("tangent") == it                # the first system and every iterate but the last
     assert prob.stats["res_history"][-1] < 1e-10
+    # ahead: each tangent pass queues the next solve before its norm is read
+    pattern = ["tangent", "solve", "wait"] if ahead else ["tangent", "wait", "solve"]
+    tp = [i for i, e in enumerate(prob.log) if e == "tangent"]
+    assert all(prob.log[i:i + 3] == pattern for i in tp)
+    assert "solves_dropped" not in prob.stats and prob._pending_solve is None
 
 
-def test_failed_deferred_solve_redoes_the_iteration(stand_in):
+def test_unexpected_convergence_drops_the_queued_solve(stand_in):
+    """A guess that already meets the limit: the solve queued behind the first norm is
+    dropped, and the guess is returned."""
+    prob = StandIn()
+    sol = stand_in.solver(prob, {"tol": 20.0, "rel_tol": 1e-14})[0].reshape(-1)
+    assert torch.equal(sol, torch.zeros(3, dtype=torch.float64)) and prob.stats["newton_iters"] == 0
+    assert prob.stats["solves_dropped"] == 1 and prob.solves == [True] and prob.stats["krylov_iters"] == []
+    assert prob._pending_solve is None
+
+
+@pytest.mark.parametrize("ahead", [True, False])
+@pytest.mark.parametrize("fail", [1, 2, 3])
+def test_failed_deferred_solve_redoes_the_iteration(stand_in, ahead, fail):
     clean = StandIn()
     ref = stand_in.solver(clean, {"tol": 1e-10, "rel_tol": 1e-14})[0]
-    prob = StandIn(fail_solves={2})
+    prob = StandIn(fail_solves={fail}, queue_next_solve=ahead)
     sol = stand_in.solver(prob, {"tol": 1e-10, "rel_tol": 1e-14})[0]
     assert torch.equal(sol, ref)                          # the failed increment left no trace
     assert prob.stats["deferred_redone"] == 1
     assert prob.stats["newton_iters"] == clean.stats["newton_iters"]
-    assert prob.solves[1] is True and prob.solves[2] is False   # the redo is a checked solve
+    assert prob.solves.count(False) == 1                  # the redo is a checked solve
+    assert prob.solves[fail - 1] is True
+    # the failed solve and (ahead) the one queued behind it are never counted
+    assert fail not in prob.stats["krylov_iters"]
+    assert len(prob.stats["krylov_iters"]) == clean.stats["newton_iters"] - 1
 
 
 def test_iteration_limit(stand_in):
@@ -137,7 +180,7 @@ def _report(capi, monkeypatch, solver_mod, **fields):
     r = capi.SolveReport.from_address(buf.data_ptr())
     for k, v in dict(k=7, error=0, rs=1e-22, atol2=1e-20, true_rs=1e-22, bb=1.0).items():
         setattr(r, k, fields.get(k, v))
-    monkeypatch.setattr(solver_mod, "_report_buffer", lambda problem: buf)
+    monkeypatch.setattr(solver_mod, "_report_buffer", lambda problem, slot=0: buf)
 
 
 def _pending(fp32):
